@@ -1,0 +1,343 @@
+"""bench.py -- SZp fastmode1 float32 compress + decompress on GB300.
+
+Workload (one step): the 512^3 Fourier field (16 random modes, |k| 1-32,
+amplitude ~ |k|^-5/3, plus N(0,1e-3) noise; 512 MiB, larger than L2) is
+compressed with REL error bound (cycling 1e-2, 1e-3, 1e-4 step by step; the
+device computes the value range), block size 32, T segments (the OpenMP
+thread count of the host, as the reference decides it), then decompressed.
+Inputs are seeded synthetic data created in HBM before timing.
+
+value   uncompressed bytes per step (4n) / device time of the step's
+        compress + decompress, GB/s (CUDA events, max over ranks).
+e2e     the same metric through the host C API (szp_compress /
+        szp_decompress on pinned host buffers), copies included.
+roofline  the kernel with the most device time: algorithmic bytes per
+        launch / its average CUDA-event duration, against the measured HBM
+        copy bandwidth.
+cpu_baseline  the oracle (C restatement of the reference, OpenMP on all host
+        cores, same T) on a 2^25-value sample of the field.
+
+--impl reference times the reference's CPU algorithm (the oracle port; the
+reference sources are not on the GPU host) on the same workload.
+Multi-GPU: replicas only (each rank runs the same step on its own GPU).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "compress & decompress GB/s (uncompressed) vs HBM roofline; batched/served p50/p99"
+RELS = (1e-2, 1e-3, 1e-4)
+N_SIDE = 512
+L = 32
+CPU_SAMPLE = 1 << 25
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--side", type=int, default=N_SIDE)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if args.impl == "gb300":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def field(side, seed, device):
+    from szp_gb300.workloads import fourier3d_torch
+    return fourier3d_torch(side, seed, device=device)
+
+
+def cpu_port_roundtrip(port, x, rel, T, reps=1):
+    """Oracle port round trip; returns seconds per round trip."""
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        eb = port.rel_bound(x, rel)
+        s = port.compress(x, eb, L, T, 1)
+        port.decompress(s, x.size, L, T, 1)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best
+
+
+def run_reference(args, rank, world, pg):
+    """The reference's CPU algorithm on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    import torch
+    from oracle.oracle import Port
+    port = Port()
+    T = port.max_threads()
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    x = field(args.side, 2, dev).cpu().numpy()
+    xs = np.ascontiguousarray(x[:CPU_SAMPLE])
+    for i in range(args.warmup):
+        cpu_port_roundtrip(port, xs, RELS[i % 3], T)
+    times = []
+    for i in range(args.steps):
+        times.append(cpu_port_roundtrip(port, xs, RELS[i % 3], T))
+    total = sum(times)
+    gbs = 4.0 * xs.size * args.steps / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32->int32",
+        "data": "synthetic (seeded 512^3 Fourier field, first 2^25 values)",
+        "config": {"workload": "fourier512^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip",
+                   "n": int(xs.size), "segments": T, "block_size": L, "l2": "inputs > L2"},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": T, "kind": "port",
+                         "sample": "2^25 floats of the 512^3 field, compress+decompress per step"},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world, pg)
+        return
+    import torch
+    import szp_gb300 as szp
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    T = szp.get_segments()
+    side = args.side
+    n = side ** 3
+    x = field(side, 2 + rank, dev)
+    cap = szp.max_stream_bytes(n, L, T, 1)
+    d_stream = torch.empty(cap, dtype=torch.uint8, device=dev)
+    d_y = torch.empty(n, dtype=torch.float32, device=dev)
+    d_size = torch.zeros(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+
+    sizes = {}
+
+    def step(i):
+        rel = RELS[i % 3]
+        szp.compress_dev_async(x.data_ptr(), n, d_stream.data_ptr(), cap, d_size.data_ptr(), szp.REL, 0.0, rel,
+                               L, T, 1, st)
+        szp.decompress_dev_async(d_stream.data_ptr(), cap, d_size.data_ptr(), n, d_y.data_ptr(), L, T, 1, st)
+
+    # sizes per bound (also validates once)
+    for i, rel in enumerate(RELS):
+        sz = szp.compress_dev(x.data_ptr(), n, d_stream.data_ptr(), cap, szp.REL, 0.0, rel, L, T, 1, st)
+        sizes[rel] = sz
+    szp.set_timing(True)
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    assert szp.sync_status(st) == 0, szp.last_error()
+    for s in range(5):
+        szp.kernel_time(s)  # drop warm-up timings
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = szp.kernel_launches()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    launches = szp.kernel_launches() - l0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    status = szp.sync_status(st)
+    assert status == 0, szp.last_error()
+    ktimes = {name: szp.kernel_time(slot) for slot, name in
+              enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
+    szp.set_timing(False)
+    if pg:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+
+    mean_out = float(np.mean([sizes[RELS[i % 3]] for i in range(args.steps)]))
+    gbs = world * 4.0 * n * args.steps / (ms / 1e3) / 1e9
+    # per-kernel achieved bandwidth from algorithmic bytes
+    alg = {"rel_range": 4.0 * n, "compress": 4.0 * n + mean_out, "dec_setup": 8.0 * T,
+           "locate": mean_out + 4.0 * n / L, "decode": mean_out + 4.0 * n + 4.0 * n / L}
+    peak, peak_kind = measured_peak_gbs()
+    kern = {}
+    for k, (tot, cnt) in ktimes.items():
+        if cnt > 0 and tot > 0:
+            avg = tot / cnt
+            kern[k] = {"avg_ms": round(avg, 4), "launches": cnt, "gbs": round(alg[k] / (avg / 1e3) / 1e9, 1),
+                       "share": None}
+    tsum = sum(v["avg_ms"] * v["launches"] for v in kern.values())
+    for v in kern.values():
+        v["share"] = round(v["avg_ms"] * v["launches"] / tsum, 3) if tsum else None
+    dom = max(kern, key=lambda k: kern[k]["avg_ms"] * kern[k]["launches"])
+    ach = kern[dom]["gbs"]
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if os.path.exists(tfile):
+        for ln in open(tfile):
+            f = dict(kv.split("=", 1) for kv in ln.split() if "=" in kv)
+            if f.get("bench_kernel") == dom and "bytes_per_element" in f:
+                traffic = round(float(f["bytes_per_element"]) * n)
+    roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 3),
+            "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
+            "alg_bytes_per_launch": alg[dom]}
+
+    # ---- e2e through the host C API ----
+    e2e = None
+    if not args.no_e2e:
+        hx = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        hx.copy_(x)
+        hxn = hx.numpy()
+        for i in range(2):
+            s = szp.szp_compress(hxn, szp.REL, 0.0, RELS[i % 3], L)
+            szp.szp_decompress(s, n, L)
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            s = szp.szp_compress(hxn, szp.REL, 0.0, RELS[i % 3], L)
+            y = szp.szp_decompress(s, n, L)
+            h2d += 4 * n + len(s)
+            d2h += len(s) + 4 * n
+        dt = time.perf_counter() - t0
+        e2e = {"value": round(world * 4.0 * n * args.steps / dt / 1e9, 3), "unit": "GB/s",
+               "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
+               "api": "szp_compress/szp_decompress (host C ABI, pinned input)"}
+        del y
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle.oracle import Port
+        port = Port()
+        Tc = port.max_threads()
+        xs = np.ascontiguousarray(x[:CPU_SAMPLE].cpu().numpy())
+        cpu_port_roundtrip(port, xs, 1e-3, Tc)
+        sec = cpu_port_roundtrip(port, xs, 1e-3, Tc, reps=3)
+        cpu = {"value": round(4.0 * xs.size / sec / 1e9, 3), "unit": "GB/s", "cores": Tc, "kind": "port",
+               "sample": "2^25 floats of the field, REL 1e-3 round trip, best of 3"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32->int32",
+            "data": "synthetic (seeded 512^3 Fourier field generated in HBM)",
+            "config": {"workload": "fourier512^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip",
+                       "n": n, "segments": T, "block_size": L, "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (512 MiB)",
+                       "ratio": {str(r): round(4.0 * n / sizes[r], 3) for r in RELS}},
+            "compress_gbs": round(world * 4.0 * n / (kern["compress"]["avg_ms"] / 1e3 +
+                                                    kern.get("rel_range", {"avg_ms": 0})["avg_ms"] / 1e3) / 1e9, 2),
+            "decompress_gbs": round(world * 4.0 * n / sum(kern[k]["avg_ms"] / 1e3 for k in
+                                                          ("dec_setup", "locate", "decode") if k in kern) / 1e9, 2),
+            "kernels": kern,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,208 @@
+/*
+ * szp_gb300.h -- C ABI of libszp_gb300.so, a GB300 (sm_103a) implementation
+ * of SZp's float32 fastmode1 / fastmode2 codec.
+ *
+ * The first group of functions keeps the names, arguments, return values and
+ * ownership rules of SZp's own API, so a program linked against libszp can
+ * link against this library instead.  Compression and decompression run as
+ * CUDA kernels on the current device; host buffers are staged through device
+ * memory kept by the library.  Streams are byte-identical to the reference's
+ * for the same input, error bound, block size and segment count T.
+ *
+ * T, the number of contiguous segments of a stream, is the reference's
+ * OpenMP thread count: by default it is omp_get_max_threads() of the calling
+ * process (OMP_NUM_THREADS), exactly as the reference decides it, and
+ * szp_gb300_set_segments() overrides it.  A stream must be decompressed with
+ * the T it was made with (the reference has the same rule).
+ *
+ * Errors: the reference functions keep their conventions (NULL return, or an
+ * *outSize of 0 for the _arg compressors) and record a message readable with
+ * szp_gb300_last_error().  Extension functions return an SZP_GB300_* status.
+ */
+#ifndef SZP_GB300_H
+#define SZP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Constants with the reference's values (SZp/include/szp_defines.h:19-37). */
+#ifndef ABS
+#define ABS 0
+#endif
+#ifndef REL
+#define REL 1
+#endif
+#ifndef SZP_NONRANDOMACCESS
+#define SZP_NONRANDOMACCESS 1
+#endif
+#ifndef SZP_RANDOMACCESS
+#define SZP_RANDOMACCESS 2
+#endif
+#ifndef SZ_FLOAT
+#define SZ_FLOAT 0
+#endif
+#ifndef SZ_DOUBLE
+#define SZ_DOUBLE 1
+#endif
+
+/* ---- reference entry points ------------------------------------------- */
+
+/* Replaces SZp/include/szp.h:33 (SZp/src/szp.cc:23-116).  fastMode 1 or 2,
+ * dataType SZ_FLOAT, errBoundMode ABS or REL (REL: eb = (max-min)*(float)rel
+ * over the data).  Returns a malloc'd stream the caller free()s; *outSize
+ * gets its length.  NULL on error (SZ_DOUBLE is not provided). */
+unsigned char *szp_compress(int fastMode, int dataType, void *data, size_t *outSize, int errBoundMode,
+                            double absErrBound, double relBoundRatio, size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp.h:36 (SZp/src/szp.cc:118-179).  bytes is a whole
+ * stream (eb header first).  byteLength, ignored by the reference, bounds
+ * the bytes read here; a value smaller than the stream header makes the
+ * library find the length by walking the last segment on the host.  Returns
+ * a malloc'd float[nbEle] or NULL on error. */
+void *szp_decompress(int fastMode, int dataType, unsigned char *bytes, size_t byteLength, size_t nbEle,
+                     int blockSize);
+
+/* Replaces SZp/include/szp_float.h:30 (SZp/src/szp_float.cc:148-309). */
+unsigned char *szp_float_openmp_threadblock(float *oriData, size_t *outSize, float absErrBound, size_t nbEle,
+                                            int blockSize);
+
+/* Replaces SZp/include/szp_float.h:33 (SZp/src/szp_float.cc:314-480).  The
+ * reference's callers size output as 4 + 4*nbEle bytes (SZp/src/szp.cc:53);
+ * a stream that would not fit that is not written and *outSize is 0. */
+void szp_float_openmp_threadblock_arg(unsigned char *output, float *oriData, size_t *outSize, float absErrBound,
+                                      size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_float.h:36 (SZp/src/szp_float.cc:482-605): the
+ * T = 1 stream. */
+void szp_float_single_thread_arg(unsigned char *output, float *oriData, size_t *outSize, float absErrBound,
+                                 size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_float.h:39 (SZp/src/szp_float.cc:607-750).
+ * Same stream as szp_float_single_thread_arg; returns the bytes the GPU
+ * kernels moved (4*nbEle read + stream written), not the CPU's counter. */
+size_t szp_float_single_thread_arg_record(unsigned char *output, float *oriData, size_t *outSize,
+                                          float absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_float.h:43 (SZp/src/szp_float.cc:752-912). */
+unsigned char *szp_float_openmp_threadblock_randomaccess(float *oriData, size_t *outSize, float absErrBound,
+                                                         size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_float.h:47 (SZp/src/szp_float.cc:914-1076). */
+void szp_float_openmp_threadblock_randomaccess_arg(unsigned char *output, float *oriData, size_t *outSize,
+                                                   float absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szpd_float.h:21 (SZp/src/szpd_float.cc:23-128).
+ * cmpBytes points just past the 4-byte eb header, as in the reference. */
+float *szp_float_decompress_openmp_threadblock(size_t nbEle, float absErrBound, int blockSize,
+                                               unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_float.h:23 (SZp/src/szpd_float.cc:320-423). */
+void szp_float_decompress_openmp_threadblock_arg(float *newData, size_t nbEle, float absErrBound, int blockSize,
+                                                 unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_float.h:25 (SZp/src/szpd_float.cc:130-214). */
+void szp_float_decompress_single_thread_arg(float *newData, size_t nbEle, float absErrBound, int blockSize,
+                                            unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_float.h:27 (SZp/src/szpd_float.cc:216-318);
+ * returns the bytes the GPU kernels moved. */
+size_t szp_float_decompress_single_thread_arg_record(float *newData, size_t nbEle, float absErrBound,
+                                                     int blockSize, unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_float.h:29 (SZp/src/szpd_float.cc:425-531). */
+float *szp_float_decompress_openmp_threadblock_randomaccess(size_t nbEle, float absErrBound, int blockSize,
+                                                            unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_float.h:31 (SZp/src/szpd_float.cc:533-637). */
+void szp_float_decompress_openmp_threadblock_randomaccess_arg(float *newData, size_t nbEle, float absErrBound,
+                                                              int blockSize, unsigned char *cmpBytes);
+
+/* ---- extensions (no counterpart in the reference) ---------------------- */
+
+#define SZP_GB300_OK 0
+#define SZP_GB300_EINVAL -1     /* bad argument */
+#define SZP_GB300_ECUDA -2      /* CUDA runtime error */
+#define SZP_GB300_ECAPACITY -3  /* output buffer too small */
+#define SZP_GB300_ECORRUPT -4   /* malformed stream */
+#define SZP_GB300_ETIMEOUT -5   /* a device-side wait gave up */
+#define SZP_GB300_ENOMEM -6     /* allocation failed */
+
+/* Segment count T for the calls of this process; 0 restores the default
+ * (omp_get_max_threads()). */
+void szp_gb300_set_segments(int segments);
+int szp_gb300_get_segments(void);
+
+/* Message and status of the calling thread's last failed call. */
+const char *szp_gb300_last_error(void);
+int szp_gb300_last_status(void);
+
+/* Largest stream for nbEle floats (header included). */
+size_t szp_gb300_max_stream_bytes(size_t nbEle, int blockSize, int segments, int fastMode);
+
+/* Device-pointer compressor.  d_data and d_out are device memory; stream is
+ * a cudaStream_t (NULL: the library's stream of this thread).  segments <= 0
+ * uses the default T.  Waits for the stream size, stores it in *outSize and
+ * returns a status. */
+int szp_gb300_compress_dev(int fastMode, const float *d_data, size_t nbEle, int errBoundMode, double absErrBound,
+                           double relBoundRatio, int blockSize, int segments, unsigned char *d_out,
+                           size_t out_capacity, size_t *outSize, void *stream);
+
+/* As szp_gb300_compress_dev without waiting: the stream size is written to
+ * d_outSize (device, 8 bytes) when the kernels finish.  Check errors with
+ * szp_gb300_sync_status(). */
+int szp_gb300_compress_dev_async(int fastMode, const float *d_data, size_t nbEle, int errBoundMode,
+                                 double absErrBound, double relBoundRatio, int blockSize, int segments,
+                                 unsigned char *d_out, size_t out_capacity, unsigned long long *d_outSize,
+                                 void *stream);
+
+/* Device-pointer decompressor; asynchronous on stream.  d_bytes is a whole
+ * stream of byteLength bytes in device memory. */
+int szp_gb300_decompress_dev(int fastMode, const unsigned char *d_bytes, size_t byteLength, size_t nbEle,
+                             int blockSize, int segments, float *d_out, void *stream);
+
+/* As szp_gb300_decompress_dev, with the stream length read on the device
+ * from d_byteLength (8 bytes, e.g. the size written by
+ * szp_gb300_compress_dev_async); capacity bounds it.  Lets a compress ->
+ * decompress pipeline run without a host round trip. */
+int szp_gb300_decompress_dev_async(int fastMode, const unsigned char *d_bytes, size_t capacity,
+                                   const unsigned long long *d_byteLength, size_t nbEle, int blockSize,
+                                   int segments, float *d_out, void *stream);
+
+/* Waits for stream and returns the status of the device-side checks of the
+ * calling thread's last calls (capacity, corrupt stream, timeouts). */
+int szp_gb300_sync_status(void *stream);
+
+/* Non-fatal notices of the last call: bit 0 set when some |x/eb| >= 2^31 or
+ * x is NaN (undefined in the reference; quantized to INT32_MIN as its x86
+ * build does). */
+int szp_gb300_last_notices(void);
+
+/* The 34-entry bit-count table, thr[k] = smallest m with
+ * (int)log2f((float)m)+1 >= k, computed from this host's libm. */
+void szp_gb300_bitcount_thresholds(uint32_t *thr34);
+
+/* Runs the device bit-count rule on n device values (diagnostics). */
+int szp_gb300_bitcount_probe(const uint32_t *d_max, uint8_t *d_bc, size_t n, void *stream);
+
+/* Per-kernel timing with CUDA events on the launching stream.  When enabled,
+ * szp_gb300_kernel_ms(slot) returns the duration of the last launch of:
+ * 0 REL range, 1 compress, 2 decompress setup, 3 locate, 4 decode. */
+void szp_gb300_set_timing(int enable);
+double szp_gb300_kernel_ms(int slot);
+
+/* Sum of the durations (ms) of the launches of kernel `slot` timed since the
+ * last call (up to 1024), and their number in *launches. */
+double szp_gb300_kernel_time(int slot, int *launches);
+
+/* Number of kernels this library has launched in this process. */
+unsigned long long szp_gb300_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SZP_GB300_H */

@@ -1,0 +1,440 @@
+/*
+ * szp_oracle.c -- CPU restatement of SZp's fastmode1 (SZP_NONRANDOMACCESS) and
+ * fastmode2 (SZP_RANDOMACCESS) float32 codec.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the CUDA library is
+ * checked against; it is also the "port" CPU baseline timed by bench.py.  The
+ * product library (szp_gb300/) never links, loads or calls it.
+ *
+ * Parity is pinned: tests/test_oracle_golden.py checks every function here
+ * byte-for-byte against fixtures written by the reference library itself
+ * (tests/golden/make_golden.py builds and runs it), and, when the reference
+ * sources are present, against the freshly built reference on random inputs.
+ *
+ * Stream layout restated (fastmode1, SZp/src/szp_float.cc:148-309):
+ *   [eb : float32, big-endian]                       szp_float.cc:164, szp_CompressionToolkit.h:520-527
+ *   [off: size_t x T, native little-endian]          szp_float.cc:280-289
+ *   [segment 0] ... [segment T-1]                    szp_float.cc:291
+ * segment t covers elements [t*floor(n/T), (t+1)*floor(n/T)), the last one
+ * takes the remainder (szp_float.cc:186,194-199).  A non-empty segment is
+ *   [seed: int32 LE = q(x[lo])] {block}*            szp_float.cc:208-213
+ * and its blocks start at lo+1, lo+1+L, ... (last one may be shorter).
+ * block = [bc: u8]                                   szp_float.cc:253-262
+ *         if bc > 0: [sign bits MSB-first, ceil(m/8) bytes]  szp_TypeManager.cc:820-844
+ *                    [payload]                        szp_TypeManager.cc:13-94
+ * payload = m x (bc/8) bytes holding (v >> bc%8) little-endian, then the low
+ * bc%8 bits of every v as one MSB-first bit string (ceil(m*(bc%8)/8) bytes).
+ *
+ * fastmode2 (szp_float.cc:752-1076): segments as above, but every block starts
+ * at lo + k*L and carries its own int32 seed; the diffs cover the m-1 elements
+ * after the seed.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define SZO_OK 0
+#define SZO_ERR_ARG -1
+#define SZO_ERR_CAP -2
+#define SZO_ERR_STREAM -3
+#define SZO_ERR_NOMEM -4
+
+/* (int)log2f((float)max) + 1 for max > 0, else 0 -- szp_float.cc:253-262.
+ * The float conversion rounds to nearest and libm's log2f rounds its result,
+ * which makes the value one larger than the true bit width just below 2^k
+ * for k >= 21 (up to 33). */
+int szo_bitcount(uint32_t max)
+{
+    if (max == 0) return 0;
+    return (int)(log2f((float)max)) + 1;
+}
+
+/* q = (int)((double)x * (double)(1.0f/eb)) -- szp_float.cc:185,209,228.
+ * The product of two floats is exact in double, the cast truncates toward
+ * zero.  Out of range and NaN are undefined in C; x86-64 (cvttsd2si) returns
+ * INT32_MIN, which is what this restatement pins so that it gives the same
+ * answer on every host. */
+static inline int32_t quantize(float x, double inv)
+{
+    double p = (double)x * inv;
+    if (p > -2147483649.0 && p < 2147483648.0) return (int32_t)p;
+    return INT32_MIN;
+}
+
+static inline void put_u32le(unsigned char *p, uint32_t v)
+{
+    p[0] = (unsigned char)v; p[1] = (unsigned char)(v >> 8);
+    p[2] = (unsigned char)(v >> 16); p[3] = (unsigned char)(v >> 24);
+}
+static inline uint32_t get_u32le(const unsigned char *p)
+{
+    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+static inline void put_u64le(unsigned char *p, uint64_t v)
+{
+    for (int i = 0; i < 8; i++) p[i] = (unsigned char)(v >> (8 * i));
+}
+static inline uint64_t get_u64le(const unsigned char *p)
+{
+    uint64_t v = 0;
+    for (int i = 0; i < 8; i++) v |= (uint64_t)p[i] << (8 * i);
+    return v;
+}
+
+/* Bytes of one encoded block of m elements with bit count bc. */
+static inline size_t block_bytes(size_t m, int bc)
+{
+    if (bc == 0) return 1;
+    size_t B = (size_t)(bc / 8), r = (size_t)(bc % 8);
+    return 1 + (m + 7) / 8 + B * m + (r * m + 7) / 8;
+}
+
+/* Write one block (header, sign bits, byte planes, remainder bit string) for
+ * m magnitudes v[] and sign flags s[]; returns bytes written.  Follows
+ * szp_float.cc:253-274 with szp_TypeManager.cc:13-94,122-434,820-844. */
+static size_t put_block(unsigned char *o, const uint32_t *v, const unsigned char *s, size_t m, uint32_t max)
+{
+    int bc = szo_bitcount(max);
+    o[0] = (unsigned char)bc;
+    if (bc == 0) return 1;
+    unsigned char *p = o + 1;
+    size_t nsign = (m + 7) / 8;
+    memset(p, 0, nsign);
+    for (size_t j = 0; j < m; j++)
+        if (s[j]) p[j >> 3] |= (unsigned char)(0x80u >> (j & 7));
+    p += nsign;
+    int B = bc / 8, r = bc % 8;
+    for (size_t j = 0; j < m; j++) {
+        uint32_t hi = v[j] >> r;
+        for (int b = 0; b < B; b++) p[j * B + b] = (unsigned char)(hi >> (8 * b));
+    }
+    p += (size_t)B * m;
+    if (r) {
+        size_t nrem = (r * m + 7) / 8;
+        memset(p, 0, nrem);
+        uint32_t mask = (1u << r) - 1u;
+        for (size_t j = 0; j < m; j++) {
+            uint32_t lo = v[j] & mask;
+            for (int b = 0; b < r; b++) {
+                size_t bit = j * (size_t)r + (size_t)b; /* MSB of the r bits first */
+                if ((lo >> (r - 1 - b)) & 1u) p[bit >> 3] |= (unsigned char)(0x80u >> (bit & 7));
+            }
+        }
+    }
+    return block_bytes(m, bc);
+}
+
+/* Read one block of m elements at i; fills v[] and s[]; returns bytes
+ * consumed or 0 on a bad header.  Mirrors szpd_float.cc:79-117 with
+ * szp_TypeManager.cc:436-517,902-944. */
+static size_t get_block(const unsigned char *i, const unsigned char *end, uint32_t *v, unsigned char *s, size_t m)
+{
+    if (i >= end) return 0;
+    int bc = i[0];
+    if (bc > 33) return 0;
+    size_t nb = block_bytes(m, bc);
+    if ((size_t)(end - i) < nb) return 0;
+    if (bc == 0) {
+        for (size_t j = 0; j < m; j++) { v[j] = 0; s[j] = 0; }
+        return 1;
+    }
+    const unsigned char *p = i + 1;
+    for (size_t j = 0; j < m; j++) s[j] = (p[j >> 3] >> (7 - (j & 7))) & 1u;
+    p += (m + 7) / 8;
+    int B = bc / 8, r = bc % 8;
+    for (size_t j = 0; j < m; j++) {
+        uint32_t hi = 0;
+        for (int b = 0; b < B; b++) hi |= (uint32_t)p[j * B + b] << (8 * b);
+        v[j] = B ? (hi << r) : 0;
+    }
+    p += (size_t)B * m;
+    for (size_t j = 0; j < m && r; j++) {
+        uint32_t lo = 0;
+        for (int b = 0; b < r; b++) {
+            size_t bit = j * (size_t)r + (size_t)b;
+            lo = (lo << 1) | ((p[bit >> 3] >> (7 - (bit & 7))) & 1u);
+        }
+        v[j] |= lo;
+    }
+    return nb;
+}
+
+/* Segment bounds, szp_float.cc:186,194-199 and szpd_float.cc:40-47. */
+static inline void seg_bounds(size_t n, int T, int t, size_t *lo, size_t *hi)
+{
+    size_t tsz = n / (size_t)T;
+    *lo = (size_t)t * tsz;
+    *hi = (t == T - 1) ? n : (size_t)(t + 1) * tsz;
+}
+
+/* Upper bound of the stream size for (n, L, T) in either mode. */
+size_t szo_max_stream_bytes(size_t n, int L, int T, int mode)
+{
+    if (L <= 0 || T <= 0) return 0;
+    size_t full = block_bytes((size_t)L, 33);
+    size_t nblk = n / (size_t)L + (size_t)T + 1;
+    size_t per = (mode == 2) ? 4 : 0;
+    return 4 + 8 * (size_t)T + 4 * (size_t)T + nblk * (full + per);
+}
+
+/* Encode segment [lo,hi) into o; returns bytes.  Fastmode1 loop,
+ * szp_float.cc:206-275. */
+static size_t encode_segment_fm1(const float *x, size_t lo, size_t hi, double inv, size_t L,
+                                 unsigned char *o, uint32_t *v, unsigned char *s)
+{
+    if (lo >= hi) return 0;
+    size_t w = 0;
+    int32_t prior = quantize(x[lo], inv);
+    put_u32le(o, (uint32_t)prior);
+    w += 4;
+    for (size_t i = lo + 1; i < hi; i += L) {
+        size_t m = (i + L > hi) ? hi - i : L;
+        uint32_t max = 0;
+        for (size_t j = 0; j < m; j++) {
+            int32_t cur = quantize(x[i + j], inv);
+            uint32_t d = (uint32_t)cur - (uint32_t)prior; /* wrapping, as compiled x86 code does */
+            prior = cur;
+            s[j] = (int32_t)d < 0;
+            v[j] = s[j] ? 0u - d : d;
+            if (v[j] > max) max = v[j];
+        }
+        w += put_block(o + w, v, s, m, max);
+    }
+    return w;
+}
+
+/* Fastmode2 segment: every block restarts from its own seed,
+ * szp_float.cc:812-864. */
+static size_t encode_segment_fm2(const float *x, size_t lo, size_t hi, double inv, size_t L,
+                                 unsigned char *o, uint32_t *v, unsigned char *s)
+{
+    size_t w = 0;
+    for (size_t i = lo; i < hi; i += L) {
+        size_t m = (i + L > hi) ? hi - i : L;
+        int32_t prior = quantize(x[i], inv);
+        put_u32le(o + w, (uint32_t)prior);
+        w += 4;
+        uint32_t max = 0;
+        for (size_t j = 0; j + 1 < m; j++) {
+            int32_t cur = quantize(x[i + j + 1], inv);
+            uint32_t d = (uint32_t)cur - (uint32_t)prior;
+            prior = cur;
+            s[j] = (int32_t)d < 0;
+            v[j] = s[j] ? 0u - d : d;
+            if (v[j] > max) max = v[j];
+        }
+        w += put_block(o + w, v, s, m - 1, max);
+    }
+    return w;
+}
+
+/* Full compressor with explicit segment count T (the reference's OpenMP
+ * thread count).  mode 1 = fastmode1, 2 = fastmode2.  Writes into out
+ * (capacity cap) and returns SZO_OK or an error. */
+int szo_compress(const float *x, size_t n, float eb, int L, int T, int mode,
+                 unsigned char *out, size_t cap, size_t *out_size)
+{
+    if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !out || !out_size) return SZO_ERR_ARG;
+    size_t head = 4 + 8 * (size_t)T;
+    if (cap < head) return SZO_ERR_CAP;
+    /* float division stored in a double, szp_float.cc:185 */
+    double inv = (double)(1.0f / eb);
+    unsigned char ebb[4];
+    memcpy(ebb, &eb, 4);
+    out[0] = ebb[3]; out[1] = ebb[2]; out[2] = ebb[1]; out[3] = ebb[0];
+
+    size_t *sz = (size_t *)calloc((size_t)T, sizeof(size_t));
+    unsigned char **buf = (unsigned char **)calloc((size_t)T, sizeof(unsigned char *));
+    if (!sz || !buf) { free(sz); free(buf); return SZO_ERR_NOMEM; }
+    int fail = 0;
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+    for (int t = 0; t < T; t++) {
+        size_t lo, hi;
+        seg_bounds(n, T, t, &lo, &hi);
+        size_t len = hi > lo ? hi - lo : 0;
+        size_t nblk = len / (size_t)L + 2;
+        size_t bound = 4 + nblk * (block_bytes((size_t)L, 33) + 4);
+        buf[t] = (unsigned char *)malloc(bound);
+        uint32_t *v = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)L);
+        unsigned char *s = (unsigned char *)malloc((size_t)L);
+        if (!buf[t] || !v || !s) {
+#pragma omp atomic write
+            fail = 1;
+        } else if (mode == 1) {
+            sz[t] = encode_segment_fm1(x, lo, hi, inv, (size_t)L, buf[t], v, s);
+        } else {
+            sz[t] = encode_segment_fm2(x, lo, hi, inv, (size_t)L, buf[t], v, s);
+        }
+        free(v);
+        free(s);
+    }
+    int rc = SZO_OK;
+    if (fail) rc = SZO_ERR_NOMEM;
+    size_t total = head;
+    if (rc == SZO_OK) {
+        size_t off = 0;
+        for (int t = 0; t < T; t++) { put_u64le(out + 4 + 8 * (size_t)t, off); off += sz[t]; }
+        total = head + off;
+        if (total > cap) rc = SZO_ERR_CAP;
+    }
+    if (rc == SZO_OK) {
+        size_t off = head;
+        for (int t = 0; t < T; t++) { memcpy(out + off, buf[t], sz[t]); off += sz[t]; }
+        *out_size = total;
+    }
+    for (int t = 0; t < T; t++) free(buf[t]);
+    free(buf);
+    free(sz);
+    return rc;
+}
+
+/* Decoder for one fastmode1 segment, szpd_float.cc:59-118. */
+static int decode_segment_fm1(const unsigned char *p, const unsigned char *end, size_t lo, size_t hi,
+                              float eb, size_t L, float *y, uint32_t *v, unsigned char *s)
+{
+    if (lo >= hi) return SZO_OK;
+    if (end - p < 4) return SZO_ERR_STREAM;
+    int32_t prior = (int32_t)get_u32le(p);
+    p += 4;
+    y[lo] = (float)prior * eb;
+    for (size_t i = lo + 1; i < hi; i += L) {
+        size_t m = (i + L > hi) ? hi - i : L;
+        size_t nb = get_block(p, end, v, s, m);
+        if (!nb) return SZO_ERR_STREAM;
+        p += nb;
+        for (size_t j = 0; j < m; j++) {
+            uint32_t d = s[j] ? 0u - v[j] : v[j];
+            prior = (int32_t)((uint32_t)prior + d);
+            y[i + j] = (float)prior * eb;
+        }
+    }
+    return SZO_OK;
+}
+
+/* Decoder for one fastmode2 segment, szpd_float.cc:425-637. */
+static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, size_t lo, size_t hi,
+                              float eb, size_t L, float *y, uint32_t *v, unsigned char *s)
+{
+    for (size_t i = lo; i < hi; i += L) {
+        size_t m = (i + L > hi) ? hi - i : L;
+        if (end - p < 4) return SZO_ERR_STREAM;
+        int32_t prior = (int32_t)get_u32le(p);
+        p += 4;
+        y[i] = (float)prior * eb;
+        /* a one-element block has no header byte on the decode side, although
+         * the encoder wrote a 0 for it (szpd_float.cc:481 vs szp_float.cc:848);
+         * it can only be the last block of a segment, so nothing shifts. */
+        if (m == 1) continue;
+        size_t nb = get_block(p, end, v, s, m - 1);
+        if (!nb) return SZO_ERR_STREAM;
+        p += nb;
+        for (size_t j = 0; j + 1 < m; j++) {
+            uint32_t d = s[j] ? 0u - v[j] : v[j];
+            prior = (int32_t)((uint32_t)prior + d);
+            y[i + j + 1] = (float)prior * eb;
+        }
+    }
+    return SZO_OK;
+}
+
+/* Full decompressor: stream (len bytes, including the 4-byte eb header),
+ * explicit T.  Validates offsets against len. */
+int szo_decompress(const unsigned char *stream, size_t len, size_t n, int L, int T, int mode, float *y)
+{
+    if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !stream || (!y && n)) return SZO_ERR_ARG;
+    size_t head = 4 + 8 * (size_t)T;
+    if (len < head) return SZO_ERR_STREAM;
+    unsigned char ebb[4] = {stream[3], stream[2], stream[1], stream[0]};
+    float eb;
+    memcpy(&eb, ebb, 4);
+    const unsigned char *data = stream + head;
+    const unsigned char *end = stream + len;
+    int rc = SZO_OK;
+#pragma omp parallel for schedule(static, 1) num_threads(T)
+    for (int t = 0; t < T; t++) {
+        size_t lo, hi;
+        seg_bounds(n, T, t, &lo, &hi);
+        uint64_t off = get_u64le(stream + 4 + 8 * (size_t)t);
+        int r = SZO_OK;
+        if (lo < hi && off > (uint64_t)(end - data)) r = SZO_ERR_STREAM;
+        uint32_t *v = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)L);
+        unsigned char *s = (unsigned char *)malloc((size_t)L);
+        if (!v || !s) r = SZO_ERR_NOMEM;
+        if (r == SZO_OK) {
+            if (mode == 1) r = decode_segment_fm1(data + off, end, lo, hi, eb, (size_t)L, y, v, s);
+            else r = decode_segment_fm2(data + off, end, lo, hi, eb, (size_t)L, y, v, s);
+        }
+        free(v);
+        free(s);
+        if (r != SZO_OK) {
+#pragma omp critical
+            rc = r;
+        }
+    }
+    return rc;
+}
+
+/* REL bound: serial min/max and (max-min)*(float)rel in float,
+ * SZp/src/szp.cc:33-48. */
+float szo_rel_bound(const float *x, size_t n, double rel)
+{
+    if (n == 0) return 0.0f;
+    float mn = x[0], mx = x[0];
+    for (size_t i = 0; i < n; i++) {
+        float v = x[i];
+        if (mn > v) mn = v;
+        else if (mx < v) mx = v;
+    }
+    float range = mx - mn;
+    return range * (float)rel;
+}
+
+/* The 34 bit-count thresholds: thr[k] = smallest m >= 1 with
+ * szo_bitcount(m) >= k, k = 1..33 (thr[0] = 0).  Found by bisection, which
+ * is valid because bitcount is non-decreasing (checked exhaustively by the
+ * test suite). */
+void szo_bitcount_thresholds(uint32_t *thr)
+{
+    thr[0] = 0;
+    for (int k = 1; k <= 33; k++) {
+        uint64_t a = 1, b = 0xFFFFFFFFull; /* find smallest m in [a,b] with bc(m) >= k */
+        if (szo_bitcount((uint32_t)b) < k) { thr[k] = 0xFFFFFFFFu; continue; }
+        while (a < b) {
+            uint64_t mid = (a + b) / 2;
+            if (szo_bitcount((uint32_t)mid) >= k) b = mid; else a = mid + 1;
+        }
+        thr[k] = (uint32_t)a;
+    }
+}
+
+/* Exhaustive check that bitcount is non-decreasing over [1, 2^32) and agrees
+ * with the thresholds; returns the number of disagreements.  Used by tests. */
+uint64_t szo_bitcount_verify(const uint32_t *thr)
+{
+    uint64_t bad = 0;
+#pragma omp parallel for reduction(+ : bad) schedule(static)
+    for (int64_t hiw = 0; hiw < 65536; hiw++) {
+        for (uint32_t low = 0; low < 65536; low++) {
+            uint32_t m = ((uint32_t)hiw << 16) | low;
+            if (m == 0) continue;
+            int bc = szo_bitcount(m);
+            int k = 32 - __builtin_clz(m);
+            int want = k + (k < 33 && m >= thr[k + 1] ? 1 : 0);
+            if (bc != want) bad++;
+        }
+    }
+    return bad;
+}
+
+int szo_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,305 @@
+"""szp_gb300 -- Python mirror of SZp's C API over libszp_gb300.so.
+
+The functions keep the reference's names and argument meaning
+(SZp/include/szp.h:33-36, szp_float.h, szpd_float.h) and take numpy arrays
+for host data.  ``compress_dev`` / ``decompress_dev`` take raw device
+pointers (e.g. ``tensor.data_ptr()``) and a CUDA stream handle.
+
+Everything runs in the CUDA library; there is no CPU path.  The first call
+fails loudly when the library has not been built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+ABS, REL = 0, 1
+SZP_NONRANDOMACCESS, SZP_RANDOMACCESS = 1, 2
+SZ_FLOAT, SZ_DOUBLE = 0, 1
+
+OK, EINVAL, ECUDA, ECAPACITY, ECORRUPT, ETIMEOUT, ENOMEM = 0, -1, -2, -3, -4, -5, -6
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libszp_gb300.so")
+
+_sz = ctypes.c_size_t
+_szp = ctypes.POINTER(ctypes.c_size_t)
+_vp = ctypes.c_void_p
+
+
+_SIGS = []
+
+
+def _sig(name, res, args):
+    _SIGS.append((name, res, args))
+
+
+_sig("szp_compress", _vp, [ctypes.c_int, ctypes.c_int, _vp, _szp, ctypes.c_int, ctypes.c_double,
+                           ctypes.c_double, _sz, ctypes.c_int])
+_sig("szp_decompress", _vp, [ctypes.c_int, ctypes.c_int, _vp, _sz, _sz, ctypes.c_int])
+_sig("szp_float_openmp_threadblock", _vp, [_vp, _szp, ctypes.c_float, _sz, ctypes.c_int])
+_sig("szp_float_openmp_threadblock_arg", None, [_vp, _vp, _szp, ctypes.c_float, _sz, ctypes.c_int])
+_sig("szp_float_single_thread_arg", None, [_vp, _vp, _szp, ctypes.c_float, _sz, ctypes.c_int])
+_sig("szp_float_single_thread_arg_record", _sz, [_vp, _vp, _szp, ctypes.c_float, _sz, ctypes.c_int])
+_sig("szp_float_openmp_threadblock_randomaccess", _vp, [_vp, _szp, ctypes.c_float, _sz, ctypes.c_int])
+_sig("szp_float_openmp_threadblock_randomaccess_arg", None, [_vp, _vp, _szp, ctypes.c_float, _sz, ctypes.c_int])
+_sig("szp_float_decompress_openmp_threadblock", _vp, [_sz, ctypes.c_float, ctypes.c_int, _vp])
+_sig("szp_float_decompress_openmp_threadblock_arg", None, [_vp, _sz, ctypes.c_float, ctypes.c_int, _vp])
+_sig("szp_float_decompress_single_thread_arg", None, [_vp, _sz, ctypes.c_float, ctypes.c_int, _vp])
+_sig("szp_float_decompress_single_thread_arg_record", _sz, [_vp, _sz, ctypes.c_float, ctypes.c_int, _vp])
+_sig("szp_float_decompress_openmp_threadblock_randomaccess", _vp, [_sz, ctypes.c_float, ctypes.c_int, _vp])
+_sig("szp_float_decompress_openmp_threadblock_randomaccess_arg", None,
+     [_vp, _sz, ctypes.c_float, ctypes.c_int, _vp])
+_sig("szp_gb300_set_segments", None, [ctypes.c_int])
+_sig("szp_gb300_get_segments", ctypes.c_int, [])
+_sig("szp_gb300_last_error", ctypes.c_char_p, [])
+_sig("szp_gb300_last_status", ctypes.c_int, [])
+_sig("szp_gb300_last_notices", ctypes.c_int, [])
+_sig("szp_gb300_max_stream_bytes", _sz, [_sz, ctypes.c_int, ctypes.c_int, ctypes.c_int])
+_sig("szp_gb300_compress_dev", ctypes.c_int, [ctypes.c_int, _vp, _sz, ctypes.c_int, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp, _sz, _szp, _vp])
+_sig("szp_gb300_compress_dev_async", ctypes.c_int, [ctypes.c_int, _vp, _sz, ctypes.c_int, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp,
+                                                    _vp])
+_sig("szp_gb300_decompress_dev", ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, ctypes.c_int, ctypes.c_int, _vp, _vp])
+_sig("szp_gb300_decompress_dev_async", ctypes.c_int, [ctypes.c_int, _vp, _sz, _vp, _sz, ctypes.c_int,
+                                                      ctypes.c_int, _vp, _vp])
+_sig("szp_gb300_sync_status", ctypes.c_int, [_vp])
+_sig("szp_gb300_bitcount_thresholds", None, [_vp])
+_sig("szp_gb300_bitcount_probe", ctypes.c_int, [_vp, _vp, _sz, _vp])
+_sig("szp_gb300_set_timing", None, [ctypes.c_int])
+_sig("szp_gb300_kernel_ms", ctypes.c_double, [ctypes.c_int])
+_sig("szp_gb300_kernel_time", ctypes.c_double, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)])
+_sig("szp_gb300_kernel_launches", ctypes.c_ulonglong, [])
+
+_libc = ctypes.CDLL(None)
+_libc.free.argtypes = [_vp]
+_libc.free.restype = None
+
+
+class _Lib:
+    """Loads libszp_gb300.so on first use; raises if it has not been built."""
+
+    def __init__(self):
+        self._h = None
+
+    def _load(self):
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libszp_gb300.so is not built: run __graft_entry__.build() "
+                              "or python szp_gb300/build.py")
+        h = ctypes.CDLL(LIB_PATH)
+        for name, res, args in _SIGS:
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        self._h = h
+        return h
+
+    def __getattr__(self, name):
+        h = self.__dict__.get("_h") or self._load()
+        return getattr(h, name)
+
+
+_lib = _Lib()
+lib = _lib
+
+
+class SzpError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+def last_error():
+    return (_lib.szp_gb300_last_error() or b"").decode()
+
+
+def last_status():
+    return _lib.szp_gb300_last_status()
+
+
+def _raise(what):
+    raise SzpError(last_status(), "%s failed: %s" % (what, last_error()))
+
+
+def _f32(x):
+    return np.ascontiguousarray(x, dtype=np.float32).ravel()
+
+
+def set_segments(T):
+    """Fix the segment count T (0 = OpenMP default, like the reference)."""
+    _lib.szp_gb300_set_segments(int(T))
+
+
+def get_segments():
+    return _lib.szp_gb300_get_segments()
+
+
+def max_stream_bytes(n, block_size=32, segments=0, fast_mode=1):
+    return _lib.szp_gb300_max_stream_bytes(n, block_size, segments, fast_mode)
+
+
+def szp_compress(data, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0, block_size=32,
+                 fast_mode=SZP_NONRANDOMACCESS, data_type=SZ_FLOAT):
+    """szp_compress (SZp/include/szp.h:33) on a host float32 array -> bytes."""
+    x = _f32(data)
+    size = ctypes.c_size_t(0)
+    p = _lib.szp_compress(fast_mode, data_type, x.ctypes.data, ctypes.byref(size), err_bound_mode,
+                          abs_err_bound, rel_bound_ratio, x.size, block_size)
+    if not p:
+        _raise("szp_compress")
+    out = ctypes.string_at(p, size.value)
+    _libc.free(p)
+    return out
+
+
+def szp_decompress(stream, n, block_size=32, fast_mode=SZP_NONRANDOMACCESS, data_type=SZ_FLOAT,
+                   byte_length=None):
+    """szp_decompress (SZp/include/szp.h:36) -> float32 array of n values."""
+    buf = np.frombuffer(stream, dtype=np.uint8)
+    bl = buf.size if byte_length is None else byte_length
+    p = _lib.szp_decompress(fast_mode, data_type, buf.ctypes.data, bl, n, block_size)
+    if not p:
+        _raise("szp_decompress")
+    y = np.frombuffer(ctypes.string_at(p, 4 * n), dtype=np.float32).copy() if n else np.empty(0, np.float32)
+    _libc.free(p)
+    return y
+
+
+def szp_float_openmp_threadblock(data, abs_err_bound, block_size=32):
+    x = _f32(data)
+    size = ctypes.c_size_t(0)
+    p = _lib.szp_float_openmp_threadblock(x.ctypes.data, ctypes.byref(size), abs_err_bound, x.size, block_size)
+    if not p:
+        _raise("szp_float_openmp_threadblock")
+    out = ctypes.string_at(p, size.value)
+    _libc.free(p)
+    return out
+
+
+def _arg_compress(fn, data, abs_err_bound, block_size, capacity=None):
+    x = _f32(data)
+    cap = 4 + 4 * x.size if capacity is None else capacity
+    out = np.zeros(max(cap, 1), dtype=np.uint8)
+    size = ctypes.c_size_t(0)
+    getattr(_lib, fn)(out.ctypes.data, x.ctypes.data, ctypes.byref(size), abs_err_bound, x.size, block_size)
+    if size.value == 0:
+        _raise(fn)
+    return out[: size.value].tobytes()
+
+
+def szp_float_openmp_threadblock_arg(data, abs_err_bound, block_size=32):
+    return _arg_compress("szp_float_openmp_threadblock_arg", data, abs_err_bound, block_size)
+
+
+def szp_float_single_thread_arg(data, abs_err_bound, block_size=32):
+    return _arg_compress("szp_float_single_thread_arg", data, abs_err_bound, block_size)
+
+
+def szp_float_openmp_threadblock_randomaccess(data, abs_err_bound, block_size=32):
+    x = _f32(data)
+    size = ctypes.c_size_t(0)
+    p = _lib.szp_float_openmp_threadblock_randomaccess(x.ctypes.data, ctypes.byref(size), abs_err_bound, x.size,
+                                                       block_size)
+    if not p:
+        _raise("szp_float_openmp_threadblock_randomaccess")
+    out = ctypes.string_at(p, size.value)
+    _libc.free(p)
+    return out
+
+
+def szp_float_openmp_threadblock_randomaccess_arg(data, abs_err_bound, block_size=32):
+    return _arg_compress("szp_float_openmp_threadblock_randomaccess_arg", data, abs_err_bound, block_size)
+
+
+def _eb_of(stream):
+    return float(np.frombuffer(bytes(stream[:4])[::-1], dtype=np.float32)[0])
+
+
+def szp_float_decompress_openmp_threadblock(stream, n, block_size=32, fast_mode=1):
+    """Per-type decompressor: passes stream+4 and eb like the reference's callers."""
+    buf = np.frombuffer(stream, dtype=np.uint8)
+    eb = _eb_of(stream)
+    fn = (_lib.szp_float_decompress_openmp_threadblock if fast_mode == 1
+          else _lib.szp_float_decompress_openmp_threadblock_randomaccess)
+    p = fn(n, eb, block_size, buf.ctypes.data + 4)
+    if not p:
+        _raise("szp_float_decompress_openmp_threadblock")
+    y = np.frombuffer(ctypes.string_at(p, 4 * n), dtype=np.float32).copy() if n else np.empty(0, np.float32)
+    _libc.free(p)
+    return y
+
+
+def szp_float_decompress_arg(stream, n, block_size=32, which="openmp_threadblock_arg"):
+    buf = np.frombuffer(stream, dtype=np.uint8)
+    eb = _eb_of(stream)
+    y = np.empty(max(n, 1), dtype=np.float32)
+    getattr(_lib, "szp_float_decompress_" + which)(y.ctypes.data, n, eb, block_size, buf.ctypes.data + 4)
+    if last_status() != 0:
+        _raise("szp_float_decompress_" + which)
+    return y[:n]
+
+
+def compress_dev(d_data, n, d_out, capacity, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0,
+                 block_size=32, segments=0, fast_mode=1, stream=0):
+    """Device-pointer compressor; returns the stream size in bytes."""
+    size = ctypes.c_size_t(0)
+    rc = _lib.szp_gb300_compress_dev(fast_mode, d_data, n, err_bound_mode, abs_err_bound, rel_bound_ratio,
+                                     block_size, segments, d_out, capacity, ctypes.byref(size), stream or None)
+    if rc != 0:
+        raise SzpError(rc, "compress_dev failed: %s" % last_error())
+    return size.value
+
+
+def compress_dev_async(d_data, n, d_out, capacity, d_size, err_bound_mode=ABS, abs_err_bound=0.0,
+                       rel_bound_ratio=0.0, block_size=32, segments=0, fast_mode=1, stream=0):
+    rc = _lib.szp_gb300_compress_dev_async(fast_mode, d_data, n, err_bound_mode, abs_err_bound, rel_bound_ratio,
+                                           block_size, segments, d_out, capacity, d_size, stream or None)
+    if rc != 0:
+        raise SzpError(rc, "compress_dev_async failed: %s" % last_error())
+
+
+def decompress_dev(d_stream, length, n, d_out, block_size=32, segments=0, fast_mode=1, stream=0):
+    rc = _lib.szp_gb300_decompress_dev(fast_mode, d_stream, length, n, block_size, segments, d_out, stream or None)
+    if rc != 0:
+        raise SzpError(rc, "decompress_dev failed: %s" % last_error())
+
+
+def decompress_dev_async(d_stream, capacity, d_len, n, d_out, block_size=32, segments=0, fast_mode=1, stream=0):
+    """Decompress a device stream whose length sits in device memory at d_len."""
+    rc = _lib.szp_gb300_decompress_dev_async(fast_mode, d_stream, capacity, d_len, n, block_size, segments, d_out,
+                                             stream or None)
+    if rc != 0:
+        raise SzpError(rc, "decompress_dev_async failed: %s" % last_error())
+
+
+def sync_status(stream=0):
+    return _lib.szp_gb300_sync_status(stream or None)
+
+
+def bitcount_thresholds():
+    thr = np.zeros(34, dtype=np.uint32)
+    _lib.szp_gb300_bitcount_thresholds(thr.ctypes.data)
+    return thr
+
+
+def set_timing(on):
+    _lib.szp_gb300_set_timing(1 if on else 0)
+
+
+def kernel_ms(slot):
+    return _lib.szp_gb300_kernel_ms(slot)
+
+
+def kernel_time(slot):
+    """(total ms, launches) of kernel `slot` since the last read."""
+    cnt = ctypes.c_int(0)
+    ms = _lib.szp_gb300_kernel_time(slot, ctypes.byref(cnt))
+    return ms, cnt.value
+
+
+SLOT_REL, SLOT_COMPRESS, SLOT_SETUP, SLOT_LOCATE, SLOT_DECODE = range(5)
+
+
+def kernel_launches():
+    return int(_lib.szp_gb300_kernel_launches())

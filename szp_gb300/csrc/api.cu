@@ -1,0 +1,882 @@
+// api.cu -- host runtime and C ABI of libszp_gb300.so.
+//
+// Every calling host thread gets a Workspace per device: a CUDA stream, device
+// buffers that grow on demand and stay resident (input staging, stream
+// staging, look-back words, block index), and small pinned host scalars.
+// The reference entry points stage host buffers through it; the *_dev
+// extensions work on caller device memory.  No entry point falls back to the
+// CPU: without a usable GPU they fail with an error.
+#include <omp.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/szp_gb300.h"
+#include "szp_kernels.h"
+
+using namespace szp;
+
+namespace {
+
+// ---------------------------------------------------------------- errors --
+thread_local std::string t_err;
+thread_local int t_status = SZP_GB300_OK;
+thread_local int t_notices = 0;
+
+int fail(int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  t_status = status;
+  return status;
+}
+void clear_error() {
+  t_err.clear();
+  t_status = SZP_GB300_OK;
+}
+
+#define CU(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(SZP_GB300_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------- bit-count table --
+// thr[k] = smallest m >= 1 with (int)log2f((float)m)+1 >= k (k = 1..33), from
+// this host's libm, the same function the reference calls
+// (SZp/src/szp_float.cc:261).  Bisection is valid because the rule is
+// non-decreasing in m (the test suite checks all 2^32 values).
+int host_bitcount(uint32_t m) { return m ? (int)log2f((float)m) + 1 : 0; }
+
+BitcountTable make_table() {
+  BitcountTable t;
+  memset(&t, 0, sizeof t);
+  for (int k = 1; k <= kMaxBitCount; k++) {
+    uint64_t a = 1, b = 0xFFFFFFFFull;
+    if (host_bitcount((uint32_t)b) < k) {
+      t.thr[k] = 0xFFFFFFFFu;
+      continue;
+    }
+    while (a < b) {
+      uint64_t mid = (a + b) / 2;
+      if (host_bitcount((uint32_t)mid) >= k) b = mid; else a = mid + 1;
+    }
+    t.thr[k] = (uint32_t)a;
+  }
+  for (int k = kMaxBitCount + 1; k < 36; k++) t.thr[k] = 0xFFFFFFFFu;
+  return t;
+}
+
+const BitcountTable& table() {
+  static BitcountTable t = make_table();
+  return t;
+}
+
+// ------------------------------------------------------------- settings --
+std::mutex g_mu;
+int g_segments = 0;
+int g_timing = 0;
+unsigned long long g_launches = 0;
+
+int resolve_segments(int requested) {
+  if (requested > 0) return requested;
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_segments > 0) return g_segments;
+  }
+  int t = omp_get_max_threads();
+  return t > 0 ? t : 1;
+}
+
+void count_launches(int k) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_launches += (unsigned long long)k;
+}
+
+// ------------------------------------------------------------ workspace --
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = n < 256 ? 256 : n;
+    want += want / 8;  // grow with headroom
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Device scalars of one workspace.
+struct DevMisc {
+  LaunchState ls;
+  uint32_t err;
+  uint32_t rel_counter;
+  uint64_t out_size;
+  float eb;
+  float pad;
+};
+constexpr int kRelMaxGrid = 1024;
+
+enum { kSlotRel = 0, kSlotCompress, kSlotSetup, kSlotLocate, kSlotDecode, kNumSlots };
+
+struct Workspace {
+  int device = -1;
+  cudaStream_t own = nullptr;
+  cudaStream_t last = nullptr;
+  cudaEvent_t done = nullptr;
+  DevBuf misc, rel_partial, status, in, stream, out, plan, fn, blkpos;
+  uint8_t* h_small = nullptr;  // pinned: out_size (8) + err (4)
+  // ring of event pairs per kernel slot: every launch is timed when timing
+  // is on, and szp_gb300_kernel_time() sums the launches not yet read
+  static constexpr int kRing = 1024;
+  cudaEvent_t ev[kNumSlots][kRing][2];
+  int ev_head[kNumSlots];     // next pair to record
+  int ev_pending[kNumSlots];  // recorded and not yet read
+  int ev_last[kNumSlots];     // most recent completed pair
+  int sm_count = 0;
+
+  int init(int dev) {
+    device = dev;
+    CU(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    CU(misc.ensure(sizeof(DevMisc)));
+    CU(cudaMemset(misc.p, 0, sizeof(DevMisc)));
+    CU(rel_partial.ensure(2 * sizeof(float) * kRelMaxGrid));
+    CU(cudaMallocHost((void**)&h_small, 64));
+    for (int s = 0; s < kNumSlots; s++) {
+      for (int i = 0; i < kRing; i++) {
+        CU(cudaEventCreate(&ev[s][i][0]));
+        CU(cudaEventCreate(&ev[s][i][1]));
+      }
+      ev_head[s] = 0;
+      ev_pending[s] = 0;
+      ev_last[s] = -1;
+    }
+    CU(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+    return SZP_GB300_OK;
+  }
+  DevMisc* dm() const { return misc.as<DevMisc>(); }
+
+  // Calls of one thread may use different streams: order them on the
+  // workspace's look-back words and buffers.
+  cudaStream_t begin(void* user) {
+    cudaStream_t st = user ? (cudaStream_t)user : own;
+    if (last && last != st) cudaStreamWaitEvent(st, done, 0);
+    last = st;
+    return st;
+  }
+  void end(cudaStream_t st) { cudaEventRecord(done, st); }
+
+  void mark(int slot, int which, cudaStream_t st) {
+    if (!g_timing) return;
+    int h = ev_head[slot];
+    cudaEventRecord(ev[slot][h][which], st);
+    if (which == 1) {
+      ev_last[slot] = h;
+      ev_head[slot] = (h + 1) % kRing;
+      if (ev_pending[slot] < kRing) ev_pending[slot]++;
+    }
+  }
+};
+
+thread_local std::vector<Workspace*> t_ws;
+
+int get_ws(Workspace** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(SZP_GB300_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  if ((int)t_ws.size() <= dev) t_ws.resize(dev + 1, nullptr);
+  if (!t_ws[dev]) {
+    Workspace* w = new Workspace();
+    int rc = w->init(dev);
+    if (rc != SZP_GB300_OK) {
+      delete w;
+      return rc;
+    }
+    t_ws[dev] = w;
+  }
+  *out = t_ws[dev];
+  return SZP_GB300_OK;
+}
+
+int status_from_err(uint32_t err) {
+  if (err & kErrCapacity) return fail(SZP_GB300_ECAPACITY, "stream does not fit the output buffer");
+  if (err & kErrLookbackTimeout) return fail(SZP_GB300_ETIMEOUT, "a device look-back wait gave up");
+  if (err & (kErrCorrupt | kErrBlockCount)) return fail(SZP_GB300_ECORRUPT, "malformed stream (flags 0x%x)", err);
+  return SZP_GB300_OK;
+}
+
+Segments make_segments(size_t n, int T, int L) {
+  Segments s;
+  s.n = n;
+  s.T = (uint32_t)T;
+  s.L = (uint32_t)L;
+  s.tsz = n / (uint64_t)T;
+  return s;
+}
+
+uint64_t seg_blocks_host(const Segments& s, uint32_t t, bool fm2) {
+  uint64_t len = s.len(t);
+  if (fm2) return (len + s.L - 1) / s.L;
+  return len > 1 ? (len - 1 + s.L - 1) / s.L : 0;
+}
+
+// tiles of segments 0..T-2 and in total, for tb blocks per tile
+void tile_counts(const Segments& s, bool fm2, uint32_t tb, uint64_t& per_seg, uint64_t& total) {
+  per_seg = 0;
+  if (s.tsz > 0) {
+    uint64_t nb = seg_blocks_host(s, 0, fm2);
+    per_seg = nb ? (nb + tb - 1) / tb : 1;
+  }
+  uint64_t last = 0;
+  if (s.n > 0) {
+    uint64_t nb = seg_blocks_host(s, s.T - 1, fm2);
+    last = nb ? (nb + tb - 1) / tb : 1;
+  }
+  total = (uint64_t)(s.T - 1) * per_seg + last;
+  if (total == 0) total = 1;
+}
+
+size_t max_stream_bytes(size_t n, int L, int T, int fm) {
+  if (L <= 0 || T <= 0) return 0;
+  Segments s = make_segments(n, T, L);
+  bool fm2 = fm == 2;
+  uint64_t per = fm2 ? (L == 1 ? 5 : 4 + block_bytes((uint32_t)L - 1, kMaxBitCount)) : max_block_bytes((uint32_t)L);
+  uint64_t total = 4 + 8ull * (uint64_t)T;
+  for (uint32_t t = 0; t < (uint32_t)T; t++) {
+    uint64_t len = s.len(t);
+    if (!len) continue;
+    uint64_t nb = seg_blocks_host(s, t, fm2);
+    total += (fm2 ? 0 : 4) + nb * per;
+    if (t + 1 < (uint32_t)T && s.tsz > 0) {  // segments 0..T-2 are alike
+      total += (uint64_t)(T - 2 - t) * ((fm2 ? 0 : 4) + nb * per);
+      t = T - 2;
+    }
+  }
+  return (size_t)total;
+}
+
+// ----------------------------------------------------------- compression --
+struct CompressJob {
+  const float* d_x;
+  size_t n;
+  int eb_mode;
+  float eb_abs;
+  double rel;
+  int L, T, fm;
+  uint8_t* d_out;
+  size_t cap;
+  unsigned long long* d_size;  // optional: size copied here too
+};
+
+int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
+  if (j.L <= 0) return fail(SZP_GB300_EINVAL, "blockSize must be positive (got %d)", j.L);
+  if (j.T <= 0) return fail(SZP_GB300_EINVAL, "segment count must be positive");
+  if (j.fm != 1 && j.fm != 2) return fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2 (got %d)", j.fm);
+  if (j.n && !j.d_x) return fail(SZP_GB300_EINVAL, "null input");
+  const uint64_t head = 4 + 8ull * j.T;
+  if (j.cap < head) return fail(SZP_GB300_ECAPACITY, "output buffer smaller than the stream header");
+  const bool fm2 = j.fm == 2;
+  Segments sg = make_segments(j.n, j.T, j.L);
+  uint32_t bpw = 1;
+  uint32_t tb = compress_blocks_per_tile((uint32_t)j.L, bpw);
+  uint64_t per_seg, ntiles;
+  tile_counts(sg, fm2, tb, per_seg, ntiles);
+  if (ntiles >= (1ull << 31) || per_seg >= (1ull << 31))
+    return fail(SZP_GB300_EINVAL, "input too large for one launch");
+  CU(w.status.ensure(ntiles * sizeof(uint64_t)));
+  DevMisc* dm = w.dm();
+  CU(cudaMemsetAsync(&dm->err, 0, sizeof(uint32_t), st));
+
+  CompressArgs a;
+  memset(&a, 0, sizeof a);
+  a.x = j.d_x;
+  a.out = j.d_out;
+  a.cap = j.cap;
+  a.seg = sg;
+  a.eb = j.eb_abs;
+  a.eb_dev = nullptr;
+  a.status = w.status.as<uint64_t>();
+  a.ls = &dm->ls;
+  a.err = &dm->err;
+  a.out_size = &dm->out_size;
+  a.ntiles = (uint32_t)ntiles;
+  a.tiles_per_seg = (uint32_t)per_seg;
+  a.tb = tb;
+  a.bpw = bpw;
+  a.thr = table();
+
+  int launches = 0;
+  if (j.eb_mode == REL) {
+    RelArgs r;
+    r.x = j.d_x;
+    r.n = j.n;
+    r.rel = (float)j.rel;
+    r.partial = w.rel_partial.as<float>();
+    r.counter = &dm->rel_counter;
+    r.eb_out = &dm->eb;
+    uint64_t want = (j.n / 4 + 255) / 256;
+    uint32_t grid = (uint32_t)(want < 1 ? 1 : want);
+    uint32_t lim = (uint32_t)(w.sm_count * 4 < kRelMaxGrid ? w.sm_count * 4 : kRelMaxGrid);
+    if (grid > lim) grid = lim;
+    w.mark(kSlotRel, 0, st);
+    CU(launch_rel_bound(r, grid, st));
+    w.mark(kSlotRel, 1, st);
+    a.eb_dev = &dm->eb;
+    launches++;
+  }
+  size_t smem = compress_smem_bytes((uint32_t)j.L, tb);
+  if (smem > 200 * 1024) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
+  w.mark(kSlotCompress, 0, st);
+  CU(launch_compress(a, fm2, st));
+  w.mark(kSlotCompress, 1, st);
+  launches++;
+  if (j.d_size) CU(cudaMemcpyAsync(j.d_size, &dm->out_size, 8, cudaMemcpyDeviceToDevice, st));
+  count_launches(launches);
+  return SZP_GB300_OK;
+}
+
+// Copies the stream size and error word to pinned memory and waits.
+int finish_sync(Workspace& w, cudaStream_t st, size_t* out_size) {
+  DevMisc* dm = w.dm();
+  CU(cudaMemcpyAsync(w.h_small, &dm->out_size, 8, cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(w.h_small + 8, &dm->err, 4, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  uint64_t sz;
+  uint32_t err;
+  memcpy(&sz, w.h_small, 8);
+  memcpy(&err, w.h_small + 8, 4);
+  t_notices = (err & kErrQuantRange) ? 1 : 0;
+  if (out_size) *out_size = (size_t)sz;
+  return status_from_err(err);
+}
+
+// --------------------------------------------------------- decompression --
+struct DecompressJob {
+  const uint8_t* d_in;
+  size_t len;
+  const uint64_t* d_len;
+  size_t n;
+  int L, T, fm;
+  float* d_y;
+};
+
+int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
+  if (j.L <= 0) return fail(SZP_GB300_EINVAL, "blockSize must be positive (got %d)", j.L);
+  if (j.T <= 0) return fail(SZP_GB300_EINVAL, "segment count must be positive");
+  if (j.fm != 1 && j.fm != 2) return fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2 (got %d)", j.fm);
+  const uint64_t head = 4 + 8ull * j.T;
+  if (j.len < head) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
+  if (j.n && !j.d_y) return fail(SZP_GB300_EINVAL, "null output");
+  const bool fm2 = j.fm == 2;
+  Segments sg = make_segments(j.n, j.T, j.L);
+  const uint32_t maxsz = fm2 ? (j.L == 1 ? 5u : 4 + block_bytes((uint32_t)j.L - 1, kMaxBitCount))
+                             : max_block_bytes((uint32_t)j.L);
+  if (maxsz > 16384) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
+  const uint32_t C = locate_chunk_bytes(maxsz);
+  const uint64_t maxchunks = (j.len + C - 1) / C + (uint64_t)j.T + 1;
+  const uint64_t nlocate = (maxchunks + 3) / 4;
+  uint32_t bpw = 1;
+  uint32_t tb = decode_blocks_per_tile((uint32_t)j.L, bpw);
+  uint64_t per_seg, ntiles;
+  tile_counts(sg, fm2, tb, per_seg, ntiles);
+  uint64_t nblk_total = 0;
+  if (sg.n) {
+    nblk_total = (uint64_t)(sg.T - 1) * (sg.tsz ? seg_blocks_host(sg, 0, fm2) : 0) + seg_blocks_host(sg, sg.T - 1, fm2);
+  }
+  if (ntiles >= (1ull << 31) || maxchunks >= (1ull << 31)) return fail(SZP_GB300_EINVAL, "input too large");
+  const uint64_t stride = maxchunks > ntiles ? maxchunks : ntiles;
+  CU(w.status.ensure(2 * stride * sizeof(uint64_t)));
+  CU(w.fn.ensure(maxchunks * maxsz * sizeof(uint16_t)));
+  CU(w.blkpos.ensure((nblk_total + 1) * sizeof(uint32_t)));
+  const size_t plan_bytes = 64 + 4ull * (j.T + 1) + 16ull * j.T + 64;
+  CU(w.plan.ensure(plan_bytes));
+  DevMisc* dm = w.dm();
+  CU(cudaMemsetAsync(&dm->err, 0, sizeof(uint32_t), st));
+
+  DecArgs a;
+  memset(&a, 0, sizeof a);
+  a.in = j.d_in;
+  a.len = j.len;
+  a.len_dev = j.d_len;
+  a.seg = sg;
+  a.fm2 = fm2;
+  uint8_t* pb = w.plan.as<uint8_t>();
+  a.plan = reinterpret_cast<DecPlan*>(pb);
+  a.reg0 = reinterpret_cast<uint64_t*>(pb + 64);
+  a.reg1 = a.reg0 + j.T;
+  a.chunk_base = reinterpret_cast<uint32_t*>(a.reg1 + j.T);
+  a.chunk = C;
+  a.maxsz = maxsz;
+  a.fn = w.fn.as<uint16_t>();
+  a.status = w.status.as<uint64_t>();
+  a.status_stride = (uint32_t)stride;
+  a.ls = &dm->ls;
+  a.err = &dm->err;
+  a.blkpos = w.blkpos.as<uint32_t>();
+  a.nblk_total = nblk_total;
+  a.y = j.d_y;
+  a.ntiles = (uint32_t)ntiles;
+  a.tiles_per_seg = (uint32_t)per_seg;
+  a.tb = tb;
+  a.bpw = bpw;
+  a.nlocate_ctas = (uint32_t)nlocate;
+
+  w.mark(kSlotSetup, 0, st);
+  CU(launch_dec_setup(a, st));
+  w.mark(kSlotSetup, 1, st);
+  w.mark(kSlotLocate, 0, st);
+  CU(launch_locate(a, st));
+  w.mark(kSlotLocate, 1, st);
+  w.mark(kSlotDecode, 0, st);
+  CU(launch_decode(a, st));
+  w.mark(kSlotDecode, 1, st);
+  count_launches(3);
+  return SZP_GB300_OK;
+}
+
+// Host-side stream length: segment offsets give every segment's start; the
+// last one is walked block by block (the stream does not record its end).
+int host_stream_length(const uint8_t* stream, size_t n, int L, int T, int fm, size_t* len) {
+  if (L <= 0 || T <= 0) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
+  Segments s = make_segments(n, T, L);
+  const bool fm2 = fm == 2;
+  const uint64_t head = 4 + 8ull * T;
+  uint64_t off = 0;
+  memcpy(&off, stream + 4 + 8ull * (T - 1), 8);
+  const uint8_t* p = stream + head + off;
+  uint64_t seglen = s.len(T - 1);
+  if (seglen == 0) {
+    *len = (size_t)(head + off);
+    return SZP_GB300_OK;
+  }
+  uint64_t nb = seg_blocks_host(s, T - 1, fm2);
+  if (!fm2) p += 4;
+  uint64_t lo = s.lo(T - 1), hi = s.hi(T - 1);
+  for (uint64_t b = 0; b < nb; b++) {
+    uint64_t start = fm2 ? lo + b * L + 1 : lo + 1 + b * L;
+    uint64_t end = start + (fm2 ? L - 1 : L);
+    if (end > hi) end = hi;
+    uint32_t m = end > start ? (uint32_t)(end - start) : 0;
+    if (fm2) {
+      p += 4;
+      // the encoder writes a header byte even for a one-element block
+    }
+    uint32_t bc = *p;
+    if (bc > (uint32_t)kMaxBitCount) return fail(SZP_GB300_ECORRUPT, "invalid bit count %u in last segment", bc);
+    p += (m == 0) ? 1 : block_bytes(m, bc);
+  }
+  *len = (size_t)(p - stream);
+  return SZP_GB300_OK;
+}
+
+// ------------------------------------------------- host-buffer pipelines --
+int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double rel, int L, int T, int fm,
+                  uint8_t** out_malloc, uint8_t* out_user, size_t user_cap, size_t* out_size) {
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  cudaStream_t st = w->begin(nullptr);
+  if (n && !data) return fail(SZP_GB300_EINVAL, "null input");
+  const size_t cap = max_stream_bytes(n, L, T, fm);
+  if (!cap) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
+  CU(w->in.ensure(n * sizeof(float) + 16));
+  CU(w->stream.ensure(cap));
+  if (n) CU(cudaMemcpyAsync(w->in.p, data, n * sizeof(float), cudaMemcpyHostToDevice, st));
+  CompressJob j{w->in.as<float>(), n, eb_mode, eb_abs, rel, L, T, fm, w->stream.as<uint8_t>(), cap, nullptr};
+  rc = compress_launch(*w, j, st);
+  if (rc) return rc;
+  size_t sz = 0;
+  rc = finish_sync(*w, st, &sz);
+  w->end(st);
+  if (rc) return rc;
+  uint8_t* dst = out_user;
+  if (!dst) {
+    size_t alloc = sz > 4 + 4 * n ? sz : 4 + 4 * n;  // the reference hands out 4+4n bytes
+    dst = (uint8_t*)malloc(alloc);
+    if (!dst) return fail(SZP_GB300_ENOMEM, "malloc(%zu) failed", alloc);
+  } else if (sz > user_cap) {
+    return fail(SZP_GB300_ECAPACITY, "stream of %zu bytes exceeds the %zu-byte output", sz, user_cap);
+  }
+  cudaError_t e = cudaMemcpyAsync(dst, w->stream.p, sz, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    if (!out_user) free(dst);
+    return fail(SZP_GB300_ECUDA, "copy of the stream failed: %s", cudaGetErrorString(e));
+  }
+  if (out_malloc) *out_malloc = dst;
+  *out_size = sz;
+  return SZP_GB300_OK;
+}
+
+// stream: whole stream (eb first) when eb_override is NaN; otherwise the
+// bytes after eb (the per-type entries) and eb is eb_override.
+int decompress_host(const uint8_t* bytes, size_t len, bool len_known, size_t n, int L, int T, int fm,
+                    bool after_eb, float eb_value, float** out_malloc, float* out_user) {
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!bytes) return fail(SZP_GB300_EINVAL, "null stream");
+  if (L <= 0 || T <= 0) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
+  const uint64_t head = 4 + 8ull * T;
+  // stream as seen from its eb header
+  const uint8_t* full = after_eb ? bytes - 4 : bytes;
+  size_t total = len;
+  if (!len_known || total < head) {
+    // host_stream_length never reads the 4 eb bytes, so `full` may point
+    // before the caller's buffer when only the bytes after eb were given
+    rc = host_stream_length(full, n, L, T, fm, &total);
+    if (rc) return rc;
+  } else {
+    size_t bound = max_stream_bytes(n, L, T, fm);
+    if (total > bound) total = bound;
+  }
+  cudaStream_t st = w->begin(nullptr);
+  CU(w->stream.ensure(total + 16));
+  CU(w->out.ensure(n * sizeof(float) + 16));
+  uint8_t* d_stream = w->stream.as<uint8_t>();
+  if (after_eb) {
+    uint32_t b;
+    memcpy(&b, &eb_value, 4);
+    uint8_t be[4] = {(uint8_t)(b >> 24), (uint8_t)(b >> 16), (uint8_t)(b >> 8), (uint8_t)b};
+    memcpy(w->h_small + 16, be, 4);
+    CU(cudaMemcpyAsync(d_stream, w->h_small + 16, 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_stream + 4, bytes, total - 4, cudaMemcpyHostToDevice, st));
+  } else {
+    CU(cudaMemcpyAsync(d_stream, bytes, total, cudaMemcpyHostToDevice, st));
+  }
+  DecompressJob j{d_stream, total, nullptr, n, L, T, fm, w->out.as<float>()};
+  rc = decompress_launch(*w, j, st);
+  if (rc) return rc;
+  rc = finish_sync(*w, st, nullptr);
+  w->end(st);
+  if (rc) return rc;
+  float* dst = out_user;
+  if (!dst) {
+    dst = (float*)malloc(n ? n * sizeof(float) : 1);
+    if (!dst) return fail(SZP_GB300_ENOMEM, "malloc failed");
+  }
+  if (n) {
+    cudaError_t e = cudaMemcpyAsync(dst, w->out.p, n * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      if (!out_user) free(dst);
+      return fail(SZP_GB300_ECUDA, "copy of the data failed: %s", cudaGetErrorString(e));
+    }
+  }
+  if (out_malloc) *out_malloc = dst;
+  return SZP_GB300_OK;
+}
+
+}  // namespace
+
+// =============================================================== C ABI ====
+extern "C" {
+
+unsigned char* szp_compress(int fastMode, int dataType, void* data, size_t* outSize, int errBoundMode,
+                            double absErrBound, double relBoundRatio, size_t nbEle, int blockSize) {
+  clear_error();
+  if (outSize) *outSize = 0;
+  if (fastMode != SZP_NONRANDOMACCESS && fastMode != SZP_RANDOMACCESS) {
+    fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2");
+    return nullptr;
+  }
+  if (dataType != SZ_FLOAT) {
+    fail(SZP_GB300_EINVAL, "only SZ_FLOAT data is provided");
+    return nullptr;
+  }
+  if (!outSize) {
+    fail(SZP_GB300_EINVAL, "null outSize");
+    return nullptr;
+  }
+  uint8_t* out = nullptr;
+  int T = resolve_segments(0);
+  int rc = compress_host((const float*)data, nbEle, errBoundMode == REL ? REL : ABS, (float)absErrBound,
+                         relBoundRatio, blockSize, T, fastMode, &out, nullptr, 0, outSize);
+  return rc ? nullptr : out;
+}
+
+void* szp_decompress(int fastMode, int dataType, unsigned char* bytes, size_t byteLength, size_t nbEle,
+                     int blockSize) {
+  clear_error();
+  if (dataType != SZ_FLOAT) {
+    fail(SZP_GB300_EINVAL, "only SZ_FLOAT data is provided");
+    return nullptr;
+  }
+  int fm = fastMode == SZP_NONRANDOMACCESS ? 1 : 2;  // the reference treats any other mode as 2
+  int T = resolve_segments(0);
+  float* y = nullptr;
+  int rc = decompress_host(bytes, byteLength, true, nbEle, blockSize, T, fm, false, 0.0f, &y, nullptr);
+  return rc ? nullptr : y;
+}
+
+static unsigned char* fm_compress_alloc(float* x, size_t* outSize, float eb, size_t n, int L, int T, int fm) {
+  clear_error();
+  if (outSize) *outSize = 0;
+  if (!outSize) {
+    fail(SZP_GB300_EINVAL, "null outSize");
+    return nullptr;
+  }
+  uint8_t* out = nullptr;
+  int rc = compress_host(x, n, ABS, eb, 0.0, L, T, fm, &out, nullptr, 0, outSize);
+  return rc ? nullptr : out;
+}
+
+static void fm_compress_arg(unsigned char* output, float* x, size_t* outSize, float eb, size_t n, int L, int T,
+                            int fm) {
+  clear_error();
+  if (!outSize) {
+    fail(SZP_GB300_EINVAL, "null outSize");
+    return;
+  }
+  *outSize = 0;
+  if (!output) {
+    fail(SZP_GB300_EINVAL, "null output");
+    return;
+  }
+  size_t sz = 0;
+  int rc = compress_host(x, n, ABS, eb, 0.0, L, T, fm, nullptr, output, 4 + 4 * n, &sz);
+  if (!rc) *outSize = sz;
+}
+
+unsigned char* szp_float_openmp_threadblock(float* oriData, size_t* outSize, float absErrBound, size_t nbEle,
+                                            int blockSize) {
+  return fm_compress_alloc(oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 1);
+}
+
+void szp_float_openmp_threadblock_arg(unsigned char* output, float* oriData, size_t* outSize, float absErrBound,
+                                      size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 1);
+}
+
+void szp_float_single_thread_arg(unsigned char* output, float* oriData, size_t* outSize, float absErrBound,
+                                 size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, 1, 1);
+}
+
+size_t szp_float_single_thread_arg_record(unsigned char* output, float* oriData, size_t* outSize,
+                                          float absErrBound, size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, 1, 1);
+  return outSize && *outSize ? 4 * nbEle + *outSize : 0;
+}
+
+unsigned char* szp_float_openmp_threadblock_randomaccess(float* oriData, size_t* outSize, float absErrBound,
+                                                         size_t nbEle, int blockSize) {
+  return fm_compress_alloc(oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 2);
+}
+
+void szp_float_openmp_threadblock_randomaccess_arg(unsigned char* output, float* oriData, size_t* outSize,
+                                                   float absErrBound, size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 2);
+}
+
+static float* fm_decompress_alloc(size_t n, float eb, int L, unsigned char* cmp, int T, int fm) {
+  clear_error();
+  float* y = nullptr;
+  int rc = decompress_host(cmp, 0, false, n, L, T, fm, true, eb, &y, nullptr);
+  return rc ? nullptr : y;
+}
+
+static void fm_decompress_arg(float* out, size_t n, float eb, int L, unsigned char* cmp, int T, int fm) {
+  clear_error();
+  if (!out && n) {
+    fail(SZP_GB300_EINVAL, "null output");
+    return;
+  }
+  decompress_host(cmp, 0, false, n, L, T, fm, true, eb, nullptr, out);
+}
+
+float* szp_float_decompress_openmp_threadblock(size_t nbEle, float absErrBound, int blockSize,
+                                               unsigned char* cmpBytes) {
+  return fm_decompress_alloc(nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 1);
+}
+
+void szp_float_decompress_openmp_threadblock_arg(float* newData, size_t nbEle, float absErrBound, int blockSize,
+                                                 unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 1);
+}
+
+void szp_float_decompress_single_thread_arg(float* newData, size_t nbEle, float absErrBound, int blockSize,
+                                            unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, 1, 1);
+}
+
+size_t szp_float_decompress_single_thread_arg_record(float* newData, size_t nbEle, float absErrBound,
+                                                     int blockSize, unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, 1, 1);
+  if (t_status) return 0;
+  size_t len = 0;
+  if (host_stream_length(cmpBytes - 4, nbEle, blockSize, 1, 1, &len)) return 0;
+  return len + 4 * nbEle;
+}
+
+float* szp_float_decompress_openmp_threadblock_randomaccess(size_t nbEle, float absErrBound, int blockSize,
+                                                            unsigned char* cmpBytes) {
+  return fm_decompress_alloc(nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 2);
+}
+
+void szp_float_decompress_openmp_threadblock_randomaccess_arg(float* newData, size_t nbEle, float absErrBound,
+                                                              int blockSize, unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 2);
+}
+
+// ---------------------------------------------------------- extensions --
+void szp_gb300_set_segments(int segments) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_segments = segments > 0 ? segments : 0;
+}
+
+int szp_gb300_get_segments(void) { return resolve_segments(0); }
+
+const char* szp_gb300_last_error(void) { return t_err.c_str(); }
+int szp_gb300_last_status(void) { return t_status; }
+int szp_gb300_last_notices(void) { return t_notices; }
+
+size_t szp_gb300_max_stream_bytes(size_t nbEle, int blockSize, int segments, int fastMode) {
+  return max_stream_bytes(nbEle, blockSize, resolve_segments(segments), fastMode == 2 ? 2 : 1);
+}
+
+int szp_gb300_compress_dev_async(int fastMode, const float* d_data, size_t nbEle, int errBoundMode,
+                                 double absErrBound, double relBoundRatio, int blockSize, int segments,
+                                 unsigned char* d_out, size_t out_capacity, unsigned long long* d_outSize,
+                                 void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_out) return fail(SZP_GB300_EINVAL, "null output");
+  cudaStream_t st = w->begin(stream);
+  CompressJob j{d_data, nbEle, errBoundMode == REL ? REL : ABS, (float)absErrBound, relBoundRatio, blockSize,
+                resolve_segments(segments), fastMode, d_out, out_capacity, d_outSize};
+  rc = compress_launch(*w, j, st);
+  w->end(st);
+  return rc;
+}
+
+int szp_gb300_compress_dev(int fastMode, const float* d_data, size_t nbEle, int errBoundMode, double absErrBound,
+                           double relBoundRatio, int blockSize, int segments, unsigned char* d_out,
+                           size_t out_capacity, size_t* outSize, void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_out) return fail(SZP_GB300_EINVAL, "null output");
+  cudaStream_t st = w->begin(stream);
+  CompressJob j{d_data, nbEle, errBoundMode == REL ? REL : ABS, (float)absErrBound, relBoundRatio, blockSize,
+                resolve_segments(segments), fastMode, d_out, out_capacity, nullptr};
+  rc = compress_launch(*w, j, st);
+  if (rc) return rc;
+  size_t sz = 0;
+  rc = finish_sync(*w, st, &sz);
+  w->end(st);
+  if (outSize) *outSize = sz;
+  return rc;
+}
+
+int szp_gb300_decompress_dev(int fastMode, const unsigned char* d_bytes, size_t byteLength, size_t nbEle,
+                             int blockSize, int segments, float* d_out, void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_bytes) return fail(SZP_GB300_EINVAL, "null stream");
+  cudaStream_t st = w->begin(stream);
+  DecompressJob j{d_bytes, byteLength, nullptr, nbEle, blockSize, resolve_segments(segments), fastMode, d_out};
+  rc = decompress_launch(*w, j, st);
+  w->end(st);
+  return rc;
+}
+
+int szp_gb300_decompress_dev_async(int fastMode, const unsigned char* d_bytes, size_t capacity,
+                                   const unsigned long long* d_byteLength, size_t nbEle, int blockSize,
+                                   int segments, float* d_out, void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_bytes) return fail(SZP_GB300_EINVAL, "null stream");
+  cudaStream_t st = w->begin(stream);
+  DecompressJob j{d_bytes, capacity, reinterpret_cast<const uint64_t*>(d_byteLength), nbEle, blockSize,
+                  resolve_segments(segments), fastMode, d_out};
+  rc = decompress_launch(*w, j, st);
+  w->end(st);
+  return rc;
+}
+
+int szp_gb300_sync_status(void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t)stream : (w->last ? w->last : w->own);
+  return finish_sync(*w, st, nullptr);
+}
+
+void szp_gb300_bitcount_thresholds(uint32_t* thr34) {
+  const BitcountTable& t = table();
+  for (int k = 0; k < 34; k++) thr34[k] = t.thr[k];
+}
+
+int szp_gb300_bitcount_probe(const uint32_t* d_max, uint8_t* d_bc, size_t n, void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  cudaStream_t st = w->begin(stream);
+  CU(launch_bitcount_probe(d_max, d_bc, n, table(), st));
+  count_launches(n ? 1 : 0);
+  w->end(st);
+  return SZP_GB300_OK;
+}
+
+void szp_gb300_set_timing(int enable) { g_timing = enable ? 1 : 0; }
+
+double szp_gb300_kernel_ms(int slot) {
+  Workspace* w;
+  if (get_ws(&w) || slot < 0 || slot >= kNumSlots || w->ev_last[slot] < 0) return -1.0;
+  int h = w->ev_last[slot];
+  float ms = -1.0f;
+  if (cudaEventSynchronize(w->ev[slot][h][1]) != cudaSuccess) return -1.0;
+  if (cudaEventElapsedTime(&ms, w->ev[slot][h][0], w->ev[slot][h][1]) != cudaSuccess) return -1.0;
+  return ms;
+}
+
+double szp_gb300_kernel_time(int slot, int* launches) {
+  if (launches) *launches = 0;
+  Workspace* w;
+  if (get_ws(&w) || slot < 0 || slot >= kNumSlots) return -1.0;
+  int n = w->ev_pending[slot];
+  double total = 0.0;
+  for (int i = 0; i < n; i++) {
+    int h = ((w->ev_head[slot] - n + i) % Workspace::kRing + Workspace::kRing) % Workspace::kRing;
+    float ms = 0.0f;
+    if (cudaEventSynchronize(w->ev[slot][h][1]) != cudaSuccess) return -1.0;
+    if (cudaEventElapsedTime(&ms, w->ev[slot][h][0], w->ev[slot][h][1]) != cudaSuccess) return -1.0;
+    total += ms;
+  }
+  w->ev_pending[slot] = 0;
+  if (launches) *launches = n;
+  return total;
+}
+
+unsigned long long szp_gb300_kernel_launches(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_launches;
+}
+
+}  // extern "C"

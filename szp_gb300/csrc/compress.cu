@@ -1,0 +1,613 @@
+// compress.cu -- SZp fastmode1 / fastmode2 float32 compressors for sm_103a.
+//
+// One launch does the whole stream: every CTA ("tile") owns up to WARPS*BPW
+// consecutive SZp blocks of one segment, quantizes them, reduces each block's
+// max |delta| to its bit count, finds its byte offset with a decoupled
+// look-back over the tiles' byte counts, packs the blocks into shared memory
+// at the destination's alignment, and writes its contiguous span with 16-byte
+// stores.  HBM traffic: 4n bytes read, stream bytes written.
+//
+// Reference semantics followed (SZp/src/szp_float.cc):
+//   quantize  (int)(x * (double)(1.0f/eb))                    :185,209,228
+//   fastmode1 delta carried across blocks of a segment         :226-251
+//   bit count (int)log2f(max)+1                                :253-262
+//   sign bitmap / fixed-length packing   szp_TypeManager.cc:13-94,820-844
+//   fastmode2 per-block seed                                   :812-864
+#include "szp_device.cuh"
+#include "szp_kernels.h"
+
+namespace szp {
+
+// Writes the block's bytes into shared memory at dst (any alignment).
+// Called by a full warp; lane j owns element j.  m = elements (1..32),
+// sign = ballot of negative deltas (valid lanes only), v = |delta| (0 for
+// lanes >= m).
+__device__ __forceinline__ void pack_block32(uint8_t* dst, uint32_t m, uint32_t bc, uint32_t sign, uint32_t v,
+                                             int lane) {
+  if (lane == 0) dst[0] = (uint8_t)bc;
+  if (bc == 0) return;
+  const uint32_t ns = (m + 7) >> 3;
+  // sign bits: element j -> bit 7-(j%8) of byte j/8 (szp_TypeManager.cc:820-844)
+  if ((uint32_t)lane < ns) dst[1 + lane] = (uint8_t)(__brev(sign) >> (24 - 8 * lane));
+  uint8_t* p = dst + 1 + ns;
+  const uint32_t B = bc >> 3, r = bc & 7;
+  if (B) {
+    // byte planes: B little-endian bytes of v>>r per element (szp_TypeManager.cc:36-52)
+    if ((uint32_t)lane < m) {
+      uint32_t hi = v >> r;
+      uint8_t* q = p + lane * B;
+      q[0] = (uint8_t)hi;
+      if (B > 1) q[1] = (uint8_t)(hi >> 8);
+      if (B > 2) q[2] = (uint8_t)(hi >> 16);
+      if (B > 3) q[3] = (uint8_t)(hi >> 24);
+    }
+    p += B * m;
+  }
+  if (r) {
+    // remainder: the low r bits of every element as one MSB-first bit string
+    // (szp_TypeManager.cc:122-434).  Lane k assembles output byte k.
+    const uint32_t nrem = (r * m + 7) >> 3;
+    const uint32_t lo = v & ((1u << r) - 1u);
+    if (r == 1) {
+      uint32_t bits = __ballot_sync(0xffffffffu, lo != 0);
+      if ((uint32_t)lane < nrem) p[lane] = (uint8_t)(__brev(bits) >> (24 - 8 * lane));
+    } else {
+      const uint32_t k = lane;
+      const uint32_t j0 = (8 * k) / r;
+      uint32_t acc = 0;
+#pragma unroll
+      for (int s = 0; s < 4; s++) {
+        uint32_t j = j0 + s;
+        uint32_t val = __shfl_sync(0xffffffffu, lo, j & 31);
+        int start = (int)(j * r) - (int)(8 * k);
+        if (j < 32 && start < 8) {
+          int sh = 8 - start - (int)r;
+          acc |= sh >= 0 ? (val << sh) : (val >> (-sh));
+        }
+      }
+      if (k < nrem) p[k] = (uint8_t)acc;
+    }
+  }
+}
+
+__device__ __forceinline__ void store_u32le(uint8_t* p, uint32_t v) {
+  p[0] = (uint8_t)v;
+  p[1] = (uint8_t)(v >> 8);
+  p[2] = (uint8_t)(v >> 16);
+  p[3] = (uint8_t)(v >> 24);
+}
+
+// Copy `len` bytes staged in shared memory starting at s_out[align] to global
+// dst (where (uintptr_t)dst % 16 == align).  16-byte stores for whole
+// chunks, byte stores at the ragged ends so neighbouring tiles never share a
+// store.
+__device__ __forceinline__ void flush_span(uint8_t* __restrict__ gdst, const uint8_t* __restrict__ s_out,
+                                           uint32_t align, uint32_t len) {
+  if (len == 0) return;
+  uint8_t* gbase = gdst - align;  // 16-byte aligned
+  const uint32_t end = align + len;
+  const uint32_t nchunks = (end + 15) >> 4;
+  for (uint32_t c = threadIdx.x; c < nchunks; c += blockDim.x) {
+    uint32_t b0 = c << 4;
+    if (b0 >= align && b0 + 16 <= end) {
+      *reinterpret_cast<uint4*>(gbase + b0) = *reinterpret_cast<const uint4*>(s_out + b0);
+    } else {
+      uint32_t lo = b0 < align ? align : b0;
+      uint32_t hi = b0 + 16 < end ? b0 + 16 : end;
+      for (uint32_t b = lo; b < hi; b++) gbase[b] = s_out[b];
+    }
+  }
+}
+
+// Tile geometry shared by the compressors.
+struct TileInfo {
+  uint32_t seg;       // segment index
+  uint64_t blk0;      // first block (segment-relative)
+  uint32_t nblk;      // blocks in this tile
+  bool first;         // first tile of its segment (carries the seed)
+  bool has_seg;       // false for the header-only tile of an empty stream
+};
+
+__device__ __forceinline__ TileInfo tile_info(const Segments& sg, uint32_t tile, uint32_t tiles_per_seg,
+                                              uint32_t tb, bool fm2) {
+  TileInfo ti;
+  if (sg.n == 0) {
+    ti.seg = sg.T - 1;
+    ti.blk0 = 0;
+    ti.nblk = 0;
+    ti.first = false;
+    ti.has_seg = false;
+    return ti;
+  }
+  uint32_t t, ts;
+  if (tiles_per_seg) {
+    t = tile / tiles_per_seg;
+    if (t > sg.T - 1) t = sg.T - 1;
+    ts = tile - t * tiles_per_seg;
+  } else {
+    t = sg.T - 1;
+    ts = tile;
+  }
+  uint64_t nb = fm2 ? (sg.len(t) + sg.L - 1) / sg.L : sg.blocks_fm1(t);
+  ti.seg = t;
+  ti.blk0 = (uint64_t)ts * tb;
+  uint64_t rem = nb > ti.blk0 ? nb - ti.blk0 : 0;
+  ti.nblk = (uint32_t)(rem < tb ? rem : tb);
+  ti.first = ts == 0;
+  ti.has_seg = true;
+  return ti;
+}
+
+// Writes eb (big-endian) and, when every segment but the last is empty
+// (n < T), their zero offsets (szp_float.cc:164,280-289).
+__device__ __forceinline__ void write_header_common(uint8_t* out, float eb, const Segments& sg) {
+  uint32_t b = __float_as_uint(eb);
+  for (int i = threadIdx.x; i < 4; i += blockDim.x) out[i] = (uint8_t)(b >> (24 - 8 * i));
+  if (sg.tsz == 0) {
+    uint32_t nz = 8 * (sg.n == 0 ? sg.T : sg.T - 1);
+    for (uint32_t i = threadIdx.x; i < nz; i += blockDim.x) out[4 + i] = 0;
+  }
+}
+
+__device__ __forceinline__ void write_offset(uint8_t* out, uint32_t t, uint64_t off) {
+  uint8_t* p = out + 4 + 8ull * t;
+  for (int i = 0; i < 8; i++) p[i] = (uint8_t)(off >> (8 * i));
+}
+
+// CTA-wide exclusive scan of per-warp byte counts; returns the tile aggregate.
+template <int WARPS>
+__device__ __forceinline__ uint32_t scan_warps(uint32_t* s_w, uint32_t mine, int warp, int lane, uint32_t& excl,
+                                               uint32_t extra_front) {
+  if (lane == 0) s_w[warp] = mine;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t x = lane < WARPS ? s_w[lane] : 0;
+    uint32_t incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane < WARPS) s_w[lane] = incl - x + extra_front;
+    if (lane == 31) s_w[WARPS] = incl + extra_front;
+  }
+  __syncthreads();
+  excl = s_w[warp];
+  return s_w[WARPS];
+}
+
+// ---------------------------------------------------------------------------
+// fastmode1, blockSize 32: one warp per block, one element per lane.
+// ---------------------------------------------------------------------------
+template <int WARPS, int BPW>
+__global__ void __launch_bounds__(WARPS * 32) compress_fm1_l32(CompressArgs a) {
+  constexpr uint32_t TB = WARPS * BPW;
+  extern __shared__ __align__(16) uint8_t s_out[];
+  __shared__ uint32_t s_tk[2];
+  __shared__ uint32_t s_w[WARPS + 1];
+  __shared__ uint64_t s_base;
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t tile, epoch;
+  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
+
+  const Segments sg = a.seg;
+  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
+  const float inv = __fdiv_rn(1.0f, eb);
+  const TileInfo ti = tile_info(sg, tile, a.tiles_per_seg, TB, false);
+  if (tile == 0) write_header_common(a.out, eb, sg);
+
+  const uint64_t lo = sg.lo(ti.seg), hi = sg.hi(ti.seg);
+  uint32_t flags = 0;
+
+  // ---- analysis: q, delta, sign, max, bit count for BPW blocks per warp ----
+  uint32_t vv[BPW], sgn[BPW], bcs[BPW];
+  uint32_t wbytes = 0;
+  const uint64_t wblk = ti.blk0 + (uint64_t)warp * BPW;  // first block of this warp
+  const uint32_t wn = ti.nblk > (uint32_t)warp * BPW ? min((uint32_t)BPW, ti.nblk - warp * BPW) : 0;
+  const uint64_t e0 = lo + 1 + wblk * 32;  // first element of the warp's first block
+  float xv[BPW];
+#pragma unroll
+  for (int k = 0; k < BPW; k++) {
+    uint64_t e = e0 + (uint64_t)k * 32 + lane;
+    xv[k] = ((uint32_t)k < wn && e < hi) ? __ldg(a.x + e) : 0.0f;
+  }
+  int32_t prev = 0;
+  if (wn) prev = quantize(__ldg(a.x + e0 - 1), inv, flags);
+#pragma unroll
+  for (int k = 0; k < BPW; k++) {
+    uint64_t e = e0 + (uint64_t)k * 32 + lane;
+    bool valid = (uint32_t)k < wn && e < hi;
+    int32_t q = quantize(xv[k], inv, flags);
+    int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
+    if (lane == 0) qp = prev;
+    prev = __shfl_sync(0xffffffffu, q, 31);
+    uint32_t d = (uint32_t)q - (uint32_t)qp;  // wrapping, as the compiled reference
+    bool neg = valid && (int32_t)d < 0;
+    uint32_t v = valid ? (neg ? 0u - d : d) : 0u;
+    sgn[k] = __ballot_sync(0xffffffffu, neg);
+    uint32_t mx = __reduce_max_sync(0xffffffffu, v);
+    uint32_t bc = bitcount_from_table(mx, a.thr.thr);
+    vv[k] = v;
+    bcs[k] = bc;
+    if ((uint32_t)k < wn) {
+      uint64_t rem = hi - (e0 + (uint64_t)k * 32);
+      uint32_t m = rem < 32 ? (uint32_t)rem : 32;
+      wbytes += block_bytes(m, bc);
+    }
+  }
+  if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
+
+  // seed of the segment: 4 bytes in front of the tile's first block
+  const bool seed = ti.has_seg && ti.first && hi > lo;
+  uint32_t wexcl;
+  const uint32_t agg = scan_warps<WARPS>(s_w, wbytes, warp, lane, wexcl, seed ? 4u : 0u);
+
+  // ---- decoupled look-back over tile byte counts ----
+  if (warp == 0) {
+    uint64_t excl = 0;
+    if (tile == 0) {
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+    } else {
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+    }
+    if (lane == 0) s_base = excl;
+  }
+  __syncthreads();
+  const uint64_t base = s_base;
+  const uint64_t head = 4 + 8ull * sg.T;
+  const uint64_t gpos = head + base;  // absolute stream position of the tile
+  if (tile == a.ntiles - 1 && threadIdx.x == 0) *a.out_size = gpos + agg;
+  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, base);
+  if (gpos + agg > a.cap) {
+    if (threadIdx.x == 0) atomicOr(a.err, kErrCapacity);
+    return;
+  }
+
+  // ---- pack into shared memory at the destination's 16-byte phase ----
+  const uint32_t align = (uint32_t)(((uintptr_t)a.out + gpos) & 15);
+  uint8_t* s_tile = s_out + align;
+  if (seed && warp == 0) {
+    int32_t sq = quantize(__ldg(a.x + lo), inv, flags);
+    if (lane < 4) s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
+  }
+  uint32_t off = wexcl;
+#pragma unroll
+  for (int k = 0; k < BPW; k++) {
+    if ((uint32_t)k < wn) {
+      uint64_t rem = hi - (e0 + (uint64_t)k * 32);
+      uint32_t m = rem < 32 ? (uint32_t)rem : 32;
+      pack_block32(s_tile + off, m, bcs[k], sgn[k], vv[k], lane);
+      off += block_bytes(m, bcs[k]);
+    }
+  }
+  __syncthreads();
+  flush_span(a.out + gpos, s_out, align, agg);
+}
+
+// ---------------------------------------------------------------------------
+// Any blockSize: one warp per block, the block walked in 32-element pieces.
+// Pieces start on byte boundaries in every section (32 signs = 4 bytes,
+// 32*B bytes, 32*r bits = 4r bytes), so each piece packs like a 32-block.
+// fastmode2 (FM2) gives every block its own seed and L-1 deltas.
+// ---------------------------------------------------------------------------
+template <int WARPS, bool FM2>
+__global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
+  extern __shared__ __align__(16) uint8_t s_out[];
+  __shared__ uint32_t s_tk[2];
+  __shared__ uint32_t s_w[WARPS + 1];
+  __shared__ uint64_t s_base;
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t tile, epoch;
+  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
+
+  const Segments sg = a.seg;
+  const uint32_t L = sg.L;
+  const uint32_t TB = WARPS * a.bpw;
+  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
+  const float inv = __fdiv_rn(1.0f, eb);
+  const TileInfo ti = tile_info(sg, tile, a.tiles_per_seg, TB, FM2);
+  if (tile == 0) write_header_common(a.out, eb, sg);
+  const uint64_t lo = sg.lo(ti.seg), hi = sg.hi(ti.seg);
+  uint32_t flags = 0;
+
+  // block b of the segment: fastmode1 elements [lo+1+bL, ...), previous
+  // element lo+bL; fastmode2 seed at lo+bL and deltas after it.
+  auto block_start = [&](uint64_t b) -> uint64_t { return FM2 ? lo + b * L + 1 : lo + 1 + b * L; };
+  auto block_len = [&](uint64_t b) -> uint32_t {
+    uint64_t s = block_start(b);
+    uint64_t end = s + L;
+    if (FM2) end -= 1;
+    if (end > hi) end = hi;
+    return end > s ? (uint32_t)(end - s) : 0;
+  };
+  const uint32_t per_blk_extra = FM2 ? 4u : 0u;  // fastmode2 seed
+
+  // pass 1: bit counts and sizes
+  uint32_t wbytes = 0;
+  const uint32_t wfirst = warp * a.bpw;
+  for (uint32_t k = 0; k < a.bpw; k++) {
+    uint32_t bi = wfirst + k;
+    if (bi >= ti.nblk) break;
+    uint64_t b = ti.blk0 + bi;
+    uint64_t s = block_start(b);
+    uint32_t m = block_len(b);
+    uint32_t mx = 0;
+    int32_t prev = quantize(__ldg(a.x + s - 1), inv, flags);
+    for (uint32_t p0 = 0; p0 < m; p0 += 32) {
+      uint32_t j = p0 + lane;
+      bool valid = j < m;
+      int32_t q = valid ? quantize(__ldg(a.x + s + j), inv, flags) : 0;
+      int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
+      if (lane == 0) qp = prev;
+      prev = __shfl_sync(0xffffffffu, q, 31);
+      uint32_t d = (uint32_t)q - (uint32_t)qp;
+      uint32_t v = valid ? (((int32_t)d < 0) ? 0u - d : d) : 0u;
+      mx = max(mx, __reduce_max_sync(0xffffffffu, v));
+    }
+    uint32_t bc = bitcount_from_table(mx, a.thr.thr);
+    wbytes += per_blk_extra + (m ? block_bytes(m, bc) : 1u);
+  }
+  if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
+
+  const bool seed = !FM2 && ti.has_seg && ti.first && hi > lo;
+  uint32_t wexcl;
+  const uint32_t agg = scan_warps<WARPS>(s_w, wbytes, warp, lane, wexcl, seed ? 4u : 0u);
+
+  if (warp == 0) {
+    uint64_t excl = 0;
+    if (tile == 0) {
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+    } else {
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+    }
+    if (lane == 0) s_base = excl;
+  }
+  __syncthreads();
+  const uint64_t base = s_base;
+  const uint64_t head = 4 + 8ull * sg.T;
+  const uint64_t gpos = head + base;
+  if (tile == a.ntiles - 1 && threadIdx.x == 0) *a.out_size = gpos + agg;
+  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, base);
+  if (gpos + agg > a.cap) {
+    if (threadIdx.x == 0) atomicOr(a.err, kErrCapacity);
+    return;
+  }
+
+  const uint32_t align = (uint32_t)(((uintptr_t)a.out + gpos) & 15);
+  uint8_t* s_tile = s_out + align;
+  if (seed && warp == 0) {
+    int32_t sq = quantize(__ldg(a.x + lo), inv, flags);
+    if (lane < 4) s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
+  }
+
+  // pass 2: recompute and pack piece by piece
+  uint32_t off = wexcl;
+  for (uint32_t k = 0; k < a.bpw; k++) {
+    uint32_t bi = wfirst + k;
+    if (bi >= ti.nblk) break;
+    uint64_t b = ti.blk0 + bi;
+    uint64_t s = block_start(b);
+    uint32_t m = block_len(b);
+    uint8_t* dst = s_tile + off;
+    if (FM2) {
+      int32_t sq = quantize(__ldg(a.x + s - 1), inv, flags);
+      if (lane < 4) dst[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
+      dst += 4;
+    }
+    // recompute max (cheap, L1-resident) to know the bit count
+    uint32_t mx = 0;
+    {
+      int32_t prev = quantize(__ldg(a.x + s - 1), inv, flags);
+      for (uint32_t p0 = 0; p0 < m; p0 += 32) {
+        uint32_t j = p0 + lane;
+        bool valid = j < m;
+        int32_t q = valid ? quantize(__ldg(a.x + s + j), inv, flags) : 0;
+        int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
+        if (lane == 0) qp = prev;
+        prev = __shfl_sync(0xffffffffu, q, 31);
+        uint32_t d = (uint32_t)q - (uint32_t)qp;
+        uint32_t v = valid ? (((int32_t)d < 0) ? 0u - d : d) : 0u;
+        mx = max(mx, __reduce_max_sync(0xffffffffu, v));
+      }
+    }
+    const uint32_t bc = bitcount_from_table(mx, a.thr.thr);
+    if (lane == 0) dst[0] = (uint8_t)bc;
+    if (m == 0 || bc == 0) {
+      off += per_blk_extra + 1;
+      continue;
+    }
+    const uint32_t ns = (m + 7) >> 3, B = bc >> 3, r = bc & 7;
+    uint8_t* sgnp = dst + 1;
+    uint8_t* bytp = sgnp + ns;
+    uint8_t* remp = bytp + B * m;
+    int32_t prev = quantize(__ldg(a.x + s - 1), inv, flags);
+    for (uint32_t p0 = 0; p0 < m; p0 += 32) {
+      uint32_t j = p0 + lane;
+      bool valid = j < m;
+      uint32_t pm = m - p0 < 32 ? m - p0 : 32;  // elements in this piece
+      int32_t q = valid ? quantize(__ldg(a.x + s + j), inv, flags) : 0;
+      int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
+      if (lane == 0) qp = prev;
+      prev = __shfl_sync(0xffffffffu, q, 31);
+      uint32_t d = (uint32_t)q - (uint32_t)qp;
+      bool neg = valid && (int32_t)d < 0;
+      uint32_t v = valid ? (neg ? 0u - d : d) : 0u;
+      uint32_t sign = __ballot_sync(0xffffffffu, neg);
+      uint32_t pns = (pm + 7) >> 3;
+      if ((uint32_t)lane < pns) sgnp[(p0 >> 3) + lane] = (uint8_t)(__brev(sign) >> (24 - 8 * lane));
+      if (B && valid) {
+        uint32_t h = v >> r;
+        uint8_t* q8 = bytp + (uint64_t)j * B;
+        for (uint32_t t = 0; t < B; t++) q8[t] = (uint8_t)(h >> (8 * t));
+      }
+      if (r) {
+        uint32_t lo_bits = v & ((1u << r) - 1u);
+        uint8_t* rp = remp + (p0 >> 3) * r;  // 32 elements * r bits = 4r bytes per piece
+        uint32_t nrem = (r * pm + 7) >> 3;
+        uint32_t kk = lane;
+        uint32_t j0 = (8 * kk) / r;
+        uint32_t acc = 0;
+        for (int t = 0; t < 8; t++) {  // r == 1 needs 8 contributors
+          uint32_t jj = j0 + t;
+          uint32_t val = __shfl_sync(0xffffffffu, lo_bits, jj & 31);
+          int start = (int)(jj * r) - (int)(8 * kk);
+          if (jj < 32 && start < 8) {
+            int sh = 8 - start - (int)r;
+            acc |= sh >= 0 ? (val << sh) : (val >> (-sh));
+          }
+        }
+        if (kk < nrem) rp[kk] = (uint8_t)acc;
+      }
+    }
+    off += per_blk_extra + block_bytes(m, bc);
+  }
+  __syncthreads();
+  flush_span(a.out + gpos, s_out, align, agg);
+}
+
+// ---------------------------------------------------------------------------
+// REL bound: min/max over x (szp.cc:33-48) finished by the last CTA, which
+// writes eb = range * (float)rel to *eb_out.  Semantics of the reference's
+// serial loop: NaNs are skipped unless x[0] is NaN (then range is NaN);
+// when max == min the same element is both, so range = x - x.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
+  __shared__ float s_mn[8], s_mx[8];
+  __shared__ bool s_last;
+  float mn = INFINITY, mx = -INFINITY;
+  const uint64_t n = a.n;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // scalar head up to 16-byte alignment, vector body, scalar tail
+  uint64_t mis = ((uintptr_t)a.x & 15) >> 2;
+  uint64_t headn = mis ? (4 - mis) : 0;
+  if (headn > n) headn = n;
+  for (uint64_t i = tid; i < headn; i += stride) {
+    float v = a.x[i];
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  const float4* x4 = reinterpret_cast<const float4*>(a.x + headn);
+  const uint64_t n4 = (n - headn) >> 2;
+  for (uint64_t i = tid; i < n4; i += stride) {
+    float4 v = __ldg(x4 + i);
+    mn = fminf(fminf(mn, v.x), fminf(v.y, fminf(v.z, v.w)));
+    mx = fmaxf(fmaxf(mx, v.x), fmaxf(v.y, fmaxf(v.z, v.w)));
+  }
+  for (uint64_t i = headn + n4 * 4 + tid; i < n; i += stride) {
+    float v = a.x[i];
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_mn[warp] = mn;
+    s_mx[warp] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      mn = fminf(mn, s_mn[w]);
+      mx = fmaxf(mx, s_mx[w]);
+    }
+    a.partial[2 * blockIdx.x] = mn;
+    a.partial[2 * blockIdx.x + 1] = mx;
+    __threadfence();
+    uint32_t done = atomicAdd(a.counter, 1u);
+    s_last = done == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  mn = INFINITY;
+  mx = -INFINITY;
+  for (uint32_t b = 0; b < gridDim.x; b++) {
+    mn = fminf(mn, ((volatile float*)a.partial)[2 * b]);
+    mx = fmaxf(mx, ((volatile float*)a.partial)[2 * b + 1]);
+  }
+  *a.counter = 0;  // ready for the next launch
+  float range;
+  if (n == 0) {
+    range = 0.0f;
+  } else if (isnan(a.x[0])) {
+    range = a.x[0];
+  } else if (mx == mn && isfinite(mx)) {
+    range = 0.0f;
+  } else {
+    range = __fsub_rn(mx, mn);
+  }
+  *a.eb_out = __fmul_rn(range, a.rel);
+}
+
+// ---------------------------------------------------------------------------
+// Device self-test of the bit-count rule on arbitrary inputs.
+// ---------------------------------------------------------------------------
+__global__ void bitcount_probe_kernel(const uint32_t* __restrict__ in, uint8_t* __restrict__ out, uint64_t n,
+                                      BitcountTable thr) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (uint8_t)bitcount_from_table(in[i], thr.thr);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+constexpr int kFm1Warps = 8, kFm1Bpw = 8;
+constexpr int kGenWarps = 8;
+
+uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw) {
+  if (L == 32) {
+    bpw = kFm1Bpw;
+    return kFm1Warps * kFm1Bpw;
+  }
+  // keep the staged tile near 16 KB
+  uint32_t mb = max_block_bytes(L) + 4;
+  uint32_t b = (16384u / kGenWarps) / mb;
+  bpw = b < 1 ? 1 : (b > 8 ? 8 : b);
+  return kGenWarps * bpw;
+}
+
+size_t compress_smem_bytes(uint32_t L, uint32_t tb) {
+  return 16 + 4 + (size_t)tb * (max_block_bytes(L) + 4) + 16;
+}
+
+cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st) {
+  size_t smem = compress_smem_bytes(a.seg.L, a.tb);
+  if (!fm2 && a.seg.L == 32) {
+    auto k = compress_fm1_l32<kFm1Warps, kFm1Bpw>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<a.ntiles, kFm1Warps * 32, smem, st>>>(a);
+  } else if (!fm2) {
+    auto k = compress_generic<kGenWarps, false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
+  } else {
+    auto k = compress_generic<kGenWarps, true>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st) {
+  rel_bound_kernel<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bitcount_probe(const uint32_t* in, uint8_t* out, uint64_t n, const BitcountTable& thr,
+                                  cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  bitcount_probe_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n, thr);
+  return cudaGetLastError();
+}
+
+}  // namespace szp

@@ -1,0 +1,190 @@
+// szp_device.cuh -- device-side helpers shared by the SZp fastmode1/2 kernels.
+//
+// Stream format (byte-identical to SZp's, SZp/src/szp_float.cc:148-309):
+//   [eb f32 big-endian][T x u64 segment offsets][segment 0]...[segment T-1]
+//   segment = [i32 seed] {block}*  (fastmode1), blocks start at lo+1 step L
+//   block   = [u8 bc] if bc>0: [sign bits MSB-first ceil(m/8)]
+//             [m x (bc/8) bytes of v>>(bc%8), little-endian]
+//             [low bc%8 bits of each v, one MSB-first bit string]
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace szp {
+
+constexpr int kMaxBitCount = 33;
+
+// Error bits written by kernels into Workspace::err (never a trap).
+enum : uint32_t {
+  kErrLookbackTimeout = 1u << 0,   // a look-back spin hit its iteration limit
+  kErrCapacity = 1u << 1,          // stream larger than the caller's buffer
+  kErrCorrupt = 1u << 2,           // malformed stream (bad bc, walk past end)
+  kErrBlockCount = 1u << 3,        // segment did not hold the expected blocks
+  kErrQuantRange = 1u << 4,        // |x/eb| >= 2^31 or NaN (reference UB; INT_MIN used)
+};
+
+// Bit-count thresholds: thr[k] = smallest m with (int)log2f((float)m)+1 >= k.
+// Filled from the host libm once per process (see api.cu).
+struct BitcountTable {
+  uint32_t thr[36];
+};
+
+// bc = (int)log2f((float)max)+1 (szp_float.cc:261) without calling log2f on the
+// device: the true width k = 32-clz(max) is exact and the reference's value is
+// k or k+1, k+1 exactly when max >= thr[k+1].
+__device__ __forceinline__ int bitcount_from_table(uint32_t max, const uint32_t* __restrict__ thr) {
+  if (max == 0) return 0;
+  int k = 32 - __clz(max);
+  return k + (max >= thr[k + 1] ? 1 : 0);
+}
+
+// Exact q = (int)((double)x * (double)inv) of szp_float.cc:209,228 in FP32.
+// The double product of two floats is exact, so trunc() of it equals trunc()
+// of the round-toward-zero float product whenever |product| < 2^24 (every
+// integer below 2^24 is a float, so RZ never crosses one).  Larger products
+// take the FP64 path; out of range and NaN give INT32_MIN like x86's
+// cvttsd2si, and raise kErrQuantRange.
+__device__ __forceinline__ int32_t quantize_slow(float x, float inv, uint32_t& flags) {
+  double p = __dmul_rn((double)x, (double)inv);
+  if (p > -2147483649.0 && p < 2147483648.0) return __double2int_rz(p);
+  flags |= kErrQuantRange;
+  return INT32_MIN;
+}
+
+__device__ __forceinline__ int32_t quantize(float x, float inv, uint32_t& flags) {
+  float p = __fmul_rz(x, inv);
+  if (fabsf(p) < 16777216.0f) return __float2int_rz(p);
+  return quantize_slow(x, inv, flags);
+}
+
+// Byte size of an encoded block of m elements (1 <= m) with bit count bc.
+__host__ __device__ __forceinline__ uint32_t block_bytes(uint32_t m, uint32_t bc) {
+  if (bc == 0) return 1;
+  uint32_t B = bc >> 3, r = bc & 7;
+  return 1 + ((m + 7) >> 3) + B * m + ((r * m + 7) >> 3);
+}
+
+__host__ __device__ __forceinline__ uint32_t max_block_bytes(uint32_t L) {
+  return block_bytes(L, kMaxBitCount);
+}
+
+// Geometry of the T contiguous segments (szp_float.cc:186,194-199).
+struct Segments {
+  uint64_t n;
+  uint64_t tsz;  // floor(n / T)
+  uint32_t T;
+  uint32_t L;
+  __host__ __device__ __forceinline__ uint64_t lo(uint32_t t) const { return (uint64_t)t * tsz; }
+  __host__ __device__ __forceinline__ uint64_t hi(uint32_t t) const {
+    return t + 1 == T ? n : (uint64_t)(t + 1) * tsz;
+  }
+  __host__ __device__ __forceinline__ uint64_t len(uint32_t t) const { return hi(t) - lo(t); }
+  // fastmode1 blocks of segment t: ceil((len-1)/L) (the seed element excluded)
+  __host__ __device__ __forceinline__ uint64_t blocks_fm1(uint32_t t) const {
+    uint64_t l = len(t);
+    return l > 1 ? (l - 1 + L - 1) / L : 0;
+  }
+};
+
+// 64-bit look-back status word: [epoch:20][flag:2][value:42].
+constexpr int kStatusValueBits = 42;
+constexpr uint64_t kStatusValueMask = (1ull << kStatusValueBits) - 1;
+constexpr uint64_t kFlagAggregate = 1, kFlagInclusive = 2;
+
+__device__ __forceinline__ uint64_t make_status(uint32_t epoch, uint64_t flag, uint64_t value) {
+  return ((uint64_t)(epoch & 0xFFFFF) << 44) | (flag << 42) | (value & kStatusValueMask);
+}
+__device__ __forceinline__ uint32_t status_epoch(uint64_t s) { return (uint32_t)(s >> 44); }
+__device__ __forceinline__ uint64_t status_flag(uint64_t s) { return (s >> 42) & 3; }
+__device__ __forceinline__ uint64_t status_value(uint64_t s) { return s & kStatusValueMask; }
+
+__device__ __forceinline__ uint64_t ld_volatile_u64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Per-launch ordering state.  Tiles are numbered by an atomic ticket so that
+// every predecessor of a tile has started before it (look-back never waits
+// on a CTA that is not resident).  The CTA that draws the last ticket resets
+// the counter and bumps the epoch, so no memset is needed between launches
+// and a captured graph can be replayed.
+struct LaunchState {
+  uint32_t ticket;
+  uint32_t epoch;
+};
+
+// Draw a tile ticket; returns (tile, epoch) broadcast to the CTA.
+__device__ __forceinline__ void draw_ticket(LaunchState* ls, uint32_t ntiles, uint32_t& tile, uint32_t& epoch,
+                                            uint32_t* smem2) {
+  if (threadIdx.x == 0) {
+    uint32_t e = *(volatile uint32_t*)&ls->epoch;
+    __threadfence();
+    uint32_t t = atomicAdd(&ls->ticket, 1u);
+    if (t == ntiles - 1) {
+      // every CTA of this launch has read the epoch before drawing its ticket
+      ls->ticket = 0;
+      __threadfence();
+      atomicAdd(&ls->epoch, 1u);
+    }
+    smem2[0] = t;
+    smem2[1] = e;
+  }
+  __syncthreads();
+  tile = smem2[0];
+  epoch = smem2[1];
+  __syncthreads();
+}
+
+constexpr uint32_t kSpinLimit = 1u << 20;  // look-back spins (~1 s) before giving up
+
+// Decoupled look-back over an additive 42-bit quantity (all tiles share one
+// chain; `stop_at` lets a chain restart at a segment boundary: tiles < stop_at
+// are not consulted).  Called by one full warp; returns the exclusive prefix.
+// On timeout sets kErrLookbackTimeout in *err and returns 0.
+__device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_t tile, uint32_t stop_at,
+                                                 uint32_t epoch, uint32_t* err) {
+  const int lane = threadIdx.x & 31;
+  uint64_t excl = 0;
+  int64_t base = (int64_t)tile - 1;
+  uint32_t spins = 0;
+  while (base >= (int64_t)stop_at) {
+    int64_t idx = base - lane;
+    uint64_t s = 0;
+    bool ready = true;
+    if (idx >= (int64_t)stop_at) {
+      s = ld_acquire_u64(status + idx);
+      ready = status_epoch(s) == (epoch & 0xFFFFF) && status_flag(s) != 0;
+    }
+    // wait until every lane in the window up to the first inclusive is ready
+    uint32_t incl = __ballot_sync(0xffffffffu, idx >= (int64_t)stop_at && ready && status_flag(s) == kFlagInclusive);
+    uint32_t notready = __ballot_sync(0xffffffffu, !ready);
+    // lanes beyond the first inclusive are irrelevant
+    uint32_t upto = incl ? (incl & (0u - incl)) : 0;  // lowest set bit = nearest inclusive
+    uint32_t relevant = upto ? (upto | (upto - 1)) : 0xffffffffu;
+    if (notready & relevant) {
+      if (++spins > kSpinLimit) {
+        if (lane == 0) atomicOr(err, kErrLookbackTimeout);
+        return 0;
+      }
+      __nanosleep(32);
+      continue;
+    }
+    uint64_t v = (idx >= (int64_t)stop_at && ((relevant >> lane) & 1)) ? status_value(s) : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    excl += v;
+    if (upto) break;
+    base -= 32;
+  }
+  return excl;
+}
+
+}  // namespace szp

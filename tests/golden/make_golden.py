@@ -1,0 +1,112 @@
+"""Writes tests/golden/golden.npz: inputs, streams and decompressed outputs
+produced by the REFERENCE library (built from its own sources by
+oracle/Makefile into oracle/_ref/).  Run here, where the reference sources
+exist; the fixtures then travel with the repository.
+
+    python tests/golden/make_golden.py
+
+Each case records x (float32 input), the reference stream, the reference
+decompressed values, and meta (L, T, fastmode, eb mode and bound).  Cases are
+kept small and compressible enough that the reference's own fixed-size
+per-thread buffers (4n/T bytes, SZp/src/szp_float.cc:190) are not overrun.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Port, Reference, reference_compress_arg, reference_decompress_arg  # noqa: E402
+from szp_gb300.workloads import walk, fourier3d, laplace_zero_patches, bitcount_sweep, specials  # noqa: E402
+
+
+def usable(req):
+    """glibc malloc usable size of a request (x86-64 and aarch64)."""
+    return max(24, ((req + 8 + 15) & ~15) - 8)
+
+
+def seg_sizes(stream, T):
+    off = np.frombuffer(stream[4:4 + 8 * T], dtype="<u8").astype(np.int64)
+    ends = np.append(off[1:], len(stream) - 4 - 8 * T)
+    return ends - off
+
+
+def main():
+    ref, port = Reference(), Port()
+    rng = np.random.default_rng(20241203)
+    cases = []
+
+    def add(name, x, L, T, mode, eb_mode, bound):
+        print("case", name, flush=True)
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        # predict the reference's buffer use with the restatement before running it
+        eb_pred = port.rel_bound(x, bound) if eb_mode == 1 else bound
+        pred = port.compress(x, eb_pred, L, T, mode)
+        per_thread = (4 * x.size + T - 1) // T  # malloc request; fortified memcpy checks it
+        if x.size and seg_sizes(pred, T).max() > per_thread:
+            print("skip %s: reference per-thread buffer would overflow" % name)
+            return
+        if eb_mode == 1 and len(pred) > 4 * x.size + 4:
+            print("skip %s: reference output buffer would overflow" % name)
+            return
+        if eb_mode == 1:
+            s = ref.compress(x, L=L, T=T, mode=mode, eb_mode=1, rel=bound)
+        else:
+            s = reference_compress_arg(ref, x, bound, L, T, mode)
+        y = reference_decompress_arg(ref, s, x.size, L, T, mode)
+        cases.append(dict(name=name, x=x, s=np.frombuffer(s, np.uint8).copy(), y=y,
+                          meta=dict(L=L, T=T, mode=mode, eb_mode=eb_mode, bound=bound, n=int(x.size))))
+
+    w = walk(5003, rng)
+    eb = float(np.float32(1e-4 * (w.max() - w.min())))
+    for T in (1, 4, 7):
+        for mode in (1, 2):
+            add("walk_T%d_m%d" % (T, mode), w, 32, T, mode, 0, eb)
+    for L in (1, 2, 7, 8, 16, 33, 64, 128):
+        for mode in (1, 2):
+            add("walk_L%d_m%d" % (L, mode), w[:3001], L, 3, mode, 0, eb)
+    f = fourier3d(16, rng).ravel()
+    for rel in (1e-2, 1e-3, 1e-4):
+        add("fourier_rel%g" % rel, f, 32, 4, 1, 1, rel)
+    add("fourier_rel_m2", f, 32, 2, 2, 1, 1e-3)
+    z = laplace_zero_patches(64, 64, rng).ravel()
+    add("zeros_T1", z, 32, 1, 1, 0, 1e-5)
+    add("zeros_T5", z, 32, 5, 1, 0, 1e-5)
+    add("zeros_m2", z, 32, 3, 2, 0, 1e-5)
+    b = bitcount_sweep(rng)
+    add("bitcounts_T1", b, 32, 1, 1, 0, 1.0)
+    add("bitcounts_T3", b, 32, 3, 1, 0, 1.0)
+    add("bitcounts_m2", b, 32, 2, 2, 0, 1.0)
+    sp = specials(rng)
+    add("specials_T1", sp, 32, 1, 1, 0, 1e-3)
+    add("specials_T2_m2", sp, 32, 2, 2, 0, 1e-3)
+    for n in (1, 2, 3, 31, 32, 33, 34, 64, 65):
+        for T in (1, 2, 5):
+            add("tiny_n%d_T%d" % (n, T), w[:n], 32, T, 1, 0, eb)
+            add("tiny_n%d_T%d_m2" % (n, T), w[:n], 32, T, 2, 0, eb)
+
+    out = {}
+    meta = []
+    for i, c in enumerate(cases):
+        out["x%d" % i] = c["x"]
+        out["s%d" % i] = c["s"]
+        out["y%d" % i] = c["y"]
+        meta.append(dict(c["meta"], name=c["name"]))
+        # the restatement must already agree; a mismatch here is a bug to fix first
+        m = c["meta"]
+        eb_hdr = float(np.frombuffer(c["s"][:4].tobytes()[::-1], np.float32)[0])
+        ps = port.compress(c["x"], eb_hdr, m["L"], m["T"], m["mode"])
+        if ps != c["s"].tobytes():
+            print("WARNING: restatement differs on", c["name"])
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    path = os.path.join(HERE, "golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote %d cases to %s (%d bytes)" % (len(cases), path, os.path.getsize(path)))
+
+
+if __name__ == "__main__":
+    main()
