@@ -202,7 +202,8 @@ def main():
     d_stream = torch.empty(cap, dtype=torch.uint8, device=dev)
     d_y = torch.empty(n, dtype=torch.float32, device=dev)
     d_size = torch.zeros(1, dtype=torch.int64, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     st = stream.cuda_stream
 
     sizes = {}

@@ -144,7 +144,7 @@ int szp_gb300_last_status(void);
 size_t szp_gb300_max_stream_bytes(size_t nbEle, int blockSize, int segments, int fastMode);
 
 /* Device-pointer compressor.  d_data and d_out are device memory; stream is
- * a cudaStream_t (NULL: the library's stream of this thread).  segments <= 0
+ * a cudaStream_t (NULL: the legacy default stream).  segments <= 0
  * uses the default T.  Waits for the stream size, stores it in *outSize and
  * returns a status. */
 int szp_gb300_compress_dev(int fastMode, const float *d_data, size_t nbEle, int errBoundMode, double absErrBound,

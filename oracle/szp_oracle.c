@@ -65,6 +65,30 @@ static inline int32_t quantize(float x, double inv)
     return INT32_MIN;
 }
 
+/* Float results that are NaN follow x86 SSE, the platform the reference's
+ * fixtures were made on: a NaN operand propagates (quieted); an invalid
+ * operation (0*inf, inf-inf) gives the default NaN 0xFFC00000.  aarch64 would
+ * give +0x7FC00000 there, so the restatement states the rule instead of
+ * inheriting the host's. */
+static inline float x86_nan_fix(float r, float a, float b)
+{
+    if (r == r) return r;
+    uint32_t u;
+    if (a != a) memcpy(&u, &a, 4);
+    else if (b != b) memcpy(&u, &b, 4);
+    else u = 0xFFC00000u;
+    u |= 0x00400000u;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+/* (float)q * eb, szpd_float.cc:67,86,112 */
+static inline float dequant(int32_t q, float eb)
+{
+    float f = (float)q;
+    return x86_nan_fix(f * eb, f, eb);
+}
+
 static inline void put_u32le(unsigned char *p, uint32_t v)
 {
     p[0] = (unsigned char)v; p[1] = (unsigned char)(v >> 8);
@@ -300,7 +324,7 @@ static int decode_segment_fm1(const unsigned char *p, const unsigned char *end, 
     if (end - p < 4) return SZO_ERR_STREAM;
     int32_t prior = (int32_t)get_u32le(p);
     p += 4;
-    y[lo] = (float)prior * eb;
+    y[lo] = dequant(prior, eb);
     for (size_t i = lo + 1; i < hi; i += L) {
         size_t m = (i + L > hi) ? hi - i : L;
         size_t nb = get_block(p, end, v, s, m);
@@ -309,7 +333,7 @@ static int decode_segment_fm1(const unsigned char *p, const unsigned char *end, 
         for (size_t j = 0; j < m; j++) {
             uint32_t d = s[j] ? 0u - v[j] : v[j];
             prior = (int32_t)((uint32_t)prior + d);
-            y[i + j] = (float)prior * eb;
+            y[i + j] = dequant(prior, eb);
         }
     }
     return SZO_OK;
@@ -324,7 +348,7 @@ static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, 
         if (end - p < 4) return SZO_ERR_STREAM;
         int32_t prior = (int32_t)get_u32le(p);
         p += 4;
-        y[i] = (float)prior * eb;
+        y[i] = dequant(prior, eb);
         /* a one-element block has no header byte on the decode side, although
          * the encoder wrote a 0 for it (szpd_float.cc:481 vs szp_float.cc:848);
          * it can only be the last block of a segment, so nothing shifts. */
@@ -335,7 +359,7 @@ static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, 
         for (size_t j = 0; j + 1 < m; j++) {
             uint32_t d = s[j] ? 0u - v[j] : v[j];
             prior = (int32_t)((uint32_t)prior + d);
-            y[i + j + 1] = (float)prior * eb;
+            y[i + j + 1] = dequant(prior, eb);
         }
     }
     return SZO_OK;
@@ -389,8 +413,9 @@ float szo_rel_bound(const float *x, size_t n, double rel)
         if (mn > v) mn = v;
         else if (mx < v) mx = v;
     }
-    float range = mx - mn;
-    return range * (float)rel;
+    float range = x86_nan_fix(mx - mn, mx, mn);
+    float r = (float)rel;
+    return x86_nan_fix(range * r, range, r);
 }
 
 /* The 34 bit-count thresholds: thr[k] = smallest m >= 1 with

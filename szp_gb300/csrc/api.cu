@@ -173,9 +173,12 @@ struct Workspace {
   DevMisc* dm() const { return misc.as<DevMisc>(); }
 
   // Calls of one thread may use different streams: order them on the
-  // workspace's look-back words and buffers.
-  cudaStream_t begin(void* user) {
-    cudaStream_t st = user ? (cudaStream_t)user : own;
+  // workspace's look-back words and buffers.  Host-buffer entry points run on
+  // the workspace's own stream; device entry points on the caller's stream
+  // (NULL = the legacy default stream, as everywhere in CUDA).
+  cudaStream_t begin_own() { return begin_on(own); }
+  cudaStream_t begin(void* user) { return begin_on((cudaStream_t)user); }
+  cudaStream_t begin_on(cudaStream_t st) {
     if (last && last != st) cudaStreamWaitEvent(st, done, 0);
     last = st;
     return st;
@@ -491,7 +494,7 @@ int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double
   Workspace* w;
   int rc = get_ws(&w);
   if (rc) return rc;
-  cudaStream_t st = w->begin(nullptr);
+  cudaStream_t st = w->begin_own();
   if (n && !data) return fail(SZP_GB300_EINVAL, "null input");
   const size_t cap = max_stream_bytes(n, L, T, fm);
   if (!cap) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
@@ -546,7 +549,7 @@ int decompress_host(const uint8_t* bytes, size_t len, bool len_known, size_t n, 
     size_t bound = max_stream_bytes(n, L, T, fm);
     if (total > bound) total = bound;
   }
-  cudaStream_t st = w->begin(nullptr);
+  cudaStream_t st = w->begin_own();
   CU(w->stream.ensure(total + 16));
   CU(w->out.ensure(n * sizeof(float) + 16));
   uint8_t* d_stream = w->stream.as<uint8_t>();
@@ -823,8 +826,7 @@ int szp_gb300_sync_status(void* stream) {
   Workspace* w;
   int rc = get_ws(&w);
   if (rc) return rc;
-  cudaStream_t st = stream ? (cudaStream_t)stream : (w->last ? w->last : w->own);
-  return finish_sync(*w, st, nullptr);
+  return finish_sync(*w, (cudaStream_t)stream, nullptr);
 }
 
 void szp_gb300_bitcount_thresholds(uint32_t* thr34) {

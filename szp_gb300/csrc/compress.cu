@@ -540,13 +540,13 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
   if (n == 0) {
     range = 0.0f;
   } else if (isnan(a.x[0])) {
-    range = a.x[0];
+    range = __uint_as_float(__float_as_uint(a.x[0]) | 0x00400000u);
   } else if (mx == mn && isfinite(mx)) {
     range = 0.0f;
   } else {
-    range = __fsub_rn(mx, mn);
+    range = x86_nan_fix(__fsub_rn(mx, mn), mx, mn);
   }
-  *a.eb_out = __fmul_rn(range, a.rel);
+  *a.eb_out = x86_nan_fix(__fmul_rn(range, a.rel), range, a.rel);
 }
 
 // ---------------------------------------------------------------------------

@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(kLocWarps * 32) locate_kernel(DecArgs a) {
     while (found < 0) {
       int64_t idx = k - lane;
       bool inrange = idx >= (int64_t)first;
-      uint64_t s = inrange ? ld_acquire_u64(st_entry + idx) : 0;
+      uint64_t s = inrange ? ld_volatile_u64(st_entry + idx) : 0;
       bool ready = !inrange || (status_epoch(s) == (epoch & 0xFFFFF) && status_flag(s) != 0);
       uint32_t incl = __ballot_sync(0xffffffffu, inrange && ready && status_flag(s) == kFlagInclusive);
       uint32_t notready = __ballot_sync(0xffffffffu, !ready);
@@ -430,7 +430,6 @@ __global__ void __launch_bounds__(kLocWarps * 32) locate_kernel(DecArgs a) {
           timeout = true;
           break;
         }
-        __nanosleep(64);
         continue;
       }
       if (upto) {
@@ -449,6 +448,7 @@ __global__ void __launch_bounds__(kLocWarps * 32) locate_kernel(DecArgs a) {
       if (lane == 0) atomicOr(a.err, kErrLookbackTimeout);
       entry = kExDead;
     } else {
+      if (found + 1 < (int64_t)c) __threadfence();  // order the fn-row reads after the status reads
       uint32_t e = fval;
       for (int64_t m = found + 1; m < (int64_t)c; m++) {
         if (e >= maxsz) break;  // END / DEAD propagate
@@ -572,8 +572,12 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, int lane) {
   return x;
 }
 
-__device__ __forceinline__ float dequant(uint32_t q, float eb) {
-  return __fmul_rn(__int2float_rn((int32_t)q), eb);
+// (float)q * eb (szpd_float.cc:67,86,112).  NaN can only appear when eb is
+// not finite; `special` (warp-uniform) selects the x86 NaN rule then.
+__device__ __forceinline__ float dequant(uint32_t q, float eb, bool special = false) {
+  float f = __int2float_rn((int32_t)q);
+  float r = __fmul_rn(f, eb);
+  return special ? x86_nan_fix(r, f, eb) : r;
 }
 
 template <int WARPS>
@@ -637,6 +641,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_fm1_l32(DecArgs a) {
   const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, false);
   if (!dt.any) return;
   const float eb = a.plan->eb;
+  const bool ebsp = !isfinite(eb);
   const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
   const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
   const uint8_t* __restrict__ in = a.in;
@@ -681,7 +686,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_fm1_l32(DecArgs a) {
       excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
       if (lane == 0) {
         st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
-        a.y[lo] = dequant(excl, eb);
+        a.y[lo] = dequant(excl, eb, ebsp);
       }
     } else {
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
@@ -698,7 +703,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_fm1_l32(DecArgs a) {
       uint64_t b = dt.blk0 + wfirst + k;
       uint64_t s = lo + 1 + b * 32;
       uint32_t m = hi - s < 32 ? (uint32_t)(hi - s) : 32u;
-      if ((uint32_t)lane < m) a.y[s + lane] = dequant(q0 + sc[k], eb);
+      if ((uint32_t)lane < m) a.y[s + lane] = dequant(q0 + sc[k], eb, ebsp);
       q0 += __shfl_sync(0xffffffffu, sc[k], 31);
     }
   }
@@ -721,6 +726,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
   const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, FM2);
   if (!dt.any) return;
   const float eb = a.plan->eb;
+  const bool ebsp = !isfinite(eb);
   const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
   const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
   const uint8_t* __restrict__ in = a.in;
@@ -777,7 +783,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
         excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
         if (lane == 0) {
           st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
-          a.y[lo] = dequant(excl, eb);
+          a.y[lo] = dequant(excl, eb, ebsp);
         }
       } else {
         if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
@@ -805,13 +811,13 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
       const uint8_t* sp = in + hp - 4;
       q0 = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
            ((uint32_t)__ldg(sp + 3) << 24);
-      if (lane == 0) a.y[s - 1] = dequant(q0, eb);
+      if (lane == 0) a.y[s - 1] = dequant(q0, eb, ebsp);
     }
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       uint32_t d = (bc && j < m) ? decode_delta(in + hp, m, bc, j) : 0u;
       uint32_t sc = warp_incl_scan(d, lane);
-      if (j < m) a.y[s + j] = dequant(q0 + sc, eb);
+      if (j < m) a.y[s + j] = dequant(q0 + sc, eb, ebsp);
       q0 += __shfl_sync(0xffffffffu, sc, 31);
     }
   }

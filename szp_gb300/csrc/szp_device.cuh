@@ -57,6 +57,15 @@ __device__ __forceinline__ int32_t quantize(float x, float inv, uint32_t& flags)
   return quantize_slow(x, inv, flags);
 }
 
+// NaN results follow x86 SSE, where the reference's fixtures come from: a NaN
+// operand propagates (quieted), an invalid operation (0*inf, inf-inf) gives
+// the default NaN 0xFFC00000.  The GPU would return 0x7FFFFFFF.
+__device__ __forceinline__ float x86_nan_fix(float r, float a, float b) {
+  if (r == r) return r;
+  uint32_t u = (a != a) ? __float_as_uint(a) : ((b != b) ? __float_as_uint(b) : 0xFFC00000u);
+  return __uint_as_float(u | 0x00400000u);
+}
+
 // Byte size of an encoded block of m elements (1 <= m) with bit count bc.
 __host__ __device__ __forceinline__ uint32_t block_bytes(uint32_t m, uint32_t bc) {
   if (bc == 0) return 1;
@@ -161,7 +170,7 @@ __device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_
     uint64_t s = 0;
     bool ready = true;
     if (idx >= (int64_t)stop_at) {
-      s = ld_acquire_u64(status + idx);
+      s = ld_volatile_u64(status + idx);  // the word carries its value: no acquire needed
       ready = status_epoch(s) == (epoch & 0xFFFFF) && status_flag(s) != 0;
     }
     // wait until every lane in the window up to the first inclusive is ready
@@ -175,7 +184,6 @@ __device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_
         if (lane == 0) atomicOr(err, kErrLookbackTimeout);
         return 0;
       }
-      __nanosleep(32);
       continue;
     }
     uint64_t v = (idx >= (int64_t)stop_at && ((relevant >> lane) & 1)) ? status_value(s) : 0;

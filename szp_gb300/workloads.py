@@ -59,7 +59,7 @@ def laplace_zero_patches(ny, nx, rng, scale=1e-3, zero_frac=0.4, L=32):
 
     while zero_blocks(f) < zero_frac:
         h = int(rng.integers(1, max(2, ny // 4)))
-        w = int(rng.integers(max(L, nx // 16), max(L + 1, nx // 2)))
+        w = min(nx, int(rng.integers(max(L, nx // 16), max(L + 1, nx // 2))))
         y0 = int(rng.integers(0, ny - h + 1))
         x0 = int(rng.integers(0, nx - w + 1))
         f[y0:y0 + h, x0:x0 + w] = 0.0

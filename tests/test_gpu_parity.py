@@ -51,7 +51,7 @@ def test_golden_per_type_entries(szp, golden):
             assert szp.szp_float_openmp_threadblock(c["x"], eb, c["L"]) == c["s"], c["name"]
             if len(c["s"]) <= 4 + 4 * c["n"]:
                 assert szp.szp_float_openmp_threadblock_arg(c["x"], eb, c["L"]) == c["s"], c["name"]
-            if c["T"] == 1:
+            if c["T"] == 1 and len(c["s"]) <= 4 + 4 * c["n"]:
                 assert szp.szp_float_single_thread_arg(c["x"], eb, c["L"]) == c["s"], c["name"]
                 y1 = szp.szp_float_decompress_arg(c["s"], c["n"], c["L"], "single_thread_arg")
                 assert np.array_equal(bits(y1), bits(c["y"])), c["name"]
@@ -89,7 +89,8 @@ def test_random_parity_vs_oracle(szp, port):
         mode = int(rng.choice([1, 1, 2]))
         x = _fields(rng, n)
         finite = x[np.isfinite(x)]
-        rng_v = float(finite.max() - finite.min()) if finite.size else 1.0
+        with np.errstate(over="ignore"):
+            rng_v = float(finite.max() - finite.min()) if finite.size else 1.0  # may be inf: eb = inf
         eb = float(np.float32(max(rng_v, 1e-6) * 10 ** rng.uniform(-7, -1)))
         szp.set_segments(T)
         s = szp.szp_compress(x, szp.ABS, eb, 0.0, L, mode)
