@@ -129,6 +129,7 @@ struct DevMisc {
   uint64_t out_size;
   float eb;
   float pad;
+  uint32_t verify[2];  // verify_kernel: failures, CTAs done (reset by its last CTA)
 };
 constexpr int kRelMaxGrid = 1024;
 
@@ -139,7 +140,7 @@ struct Workspace {
   cudaStream_t own = nullptr;
   cudaStream_t last = nullptr;
   cudaEvent_t done = nullptr;
-  DevBuf misc, rel_partial, status, in, stream, out, plan, fn, blkpos;
+  DevBuf misc, rel_partial, status, in, stream, out, plan, walks, blkpos;
   uint8_t* h_small = nullptr;  // pinned: out_size (8) + err (4)
   // ring of event pairs per kernel slot: every launch is timed when timing
   // is on, and szp_gb300_kernel_time() sums the launches not yet read
@@ -393,7 +394,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   if (maxsz > 16384) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
   const uint32_t C = locate_chunk_bytes(maxsz);
   const uint64_t maxchunks = (j.len + C - 1) / C + (uint64_t)j.T + 1;
-  const uint64_t nlocate = (maxchunks + 3) / 4;
+  const uint64_t nchunk_ctas = (maxchunks + 255) / 256;
   uint32_t bpw = 1;
   uint32_t tb = decode_blocks_per_tile((uint32_t)j.L, bpw);
   uint64_t per_seg, ntiles;
@@ -403,9 +404,9 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
     nblk_total = (uint64_t)(sg.T - 1) * (sg.tsz ? seg_blocks_host(sg, 0, fm2) : 0) + seg_blocks_host(sg, sg.T - 1, fm2);
   }
   if (ntiles >= (1ull << 31) || maxchunks >= (1ull << 31)) return fail(SZP_GB300_EINVAL, "input too large");
-  const uint64_t stride = maxchunks > ntiles ? maxchunks : ntiles;
-  CU(w.status.ensure(2 * stride * sizeof(uint64_t)));
-  CU(w.fn.ensure(maxchunks * maxsz * sizeof(uint16_t)));
+  const uint64_t nstatus = ntiles > nchunk_ctas ? ntiles : nchunk_ctas;
+  CU(w.status.ensure(nstatus * sizeof(uint64_t)));
+  CU(w.walks.ensure(maxchunks * (2 * sizeof(uint4) + sizeof(uint32_t))));
   CU(w.blkpos.ensure((nblk_total + 1) * sizeof(uint32_t)));
   const size_t plan_bytes = 64 + 4ull * (j.T + 1) + 16ull * j.T + 64;
   CU(w.plan.ensure(plan_bytes));
@@ -425,10 +426,14 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.reg1 = a.reg0 + j.T;
   a.chunk_base = reinterpret_cast<uint32_t*>(a.reg1 + j.T);
   a.chunk = C;
+  a.overlap = locate_overlap_bytes(maxsz);
   a.maxsz = maxsz;
-  a.fn = w.fn.as<uint16_t>();
+  a.walks = w.walks.as<uint4>();
+  a.final_walks = a.walks + maxchunks;
+  a.fails = reinterpret_cast<uint32_t*>(a.final_walks + maxchunks);
+  a.counters = dm->verify;
+  a.max_chunks = (uint32_t)maxchunks;
   a.status = w.status.as<uint64_t>();
-  a.status_stride = (uint32_t)stride;
   a.ls = &dm->ls;
   a.err = &dm->err;
   a.blkpos = w.blkpos.as<uint32_t>();
@@ -438,7 +443,8 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.tiles_per_seg = (uint32_t)per_seg;
   a.tb = tb;
   a.bpw = bpw;
-  a.nlocate_ctas = (uint32_t)nlocate;
+  a.nchunk_ctas = (uint32_t)nchunk_ctas;
+  if (decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) return fail(SZP_GB300_EINVAL, "blockSize too large");
 
   w.mark(kSlotSetup, 0, st);
   CU(launch_dec_setup(a, st));
@@ -449,7 +455,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   w.mark(kSlotDecode, 0, st);
   CU(launch_decode(a, st));
   w.mark(kSlotDecode, 1, st);
-  count_launches(3);
+  count_launches(5);
   return SZP_GB300_OK;
 }
 

@@ -15,6 +15,7 @@
 //   fastmode2 per-block seed                                   :812-864
 #include "szp_device.cuh"
 #include "szp_kernels.h"
+#include "szp_tma.cuh"
 
 namespace szp {
 
@@ -177,73 +178,157 @@ __device__ __forceinline__ uint32_t scan_warps(uint32_t* s_w, uint32_t mine, int
 }
 
 // ---------------------------------------------------------------------------
-// fastmode1, blockSize 32: one warp per block, one element per lane.
+// fastmode1, blockSize L = 8*LPB (8..256): LPB lanes per block, 8 elements
+// per lane.  Eight elements fill whole bytes in every section of a block
+// (one sign byte, 8*B bytes of byte planes, r bytes of remainder bits), so
+// each lane packs its part of a block without talking to other lanes; only
+// the block max (LPB-lane reduction) and the byte offsets (warp scan, CTA
+// scan, decoupled look-back) are shared.  A warp handles ROUNDS groups of
+// 32/LPB consecutive blocks; a 256-thread CTA a tile of 8*ROUNDS*32/LPB blocks.
 // ---------------------------------------------------------------------------
-template <int WARPS, int BPW>
-__global__ void __launch_bounds__(WARPS * 32) compress_fm1_l32(CompressArgs a) {
-  constexpr uint32_t TB = WARPS * BPW;
+
+// Loads x[s .. s+8) (lane-local, ml valid elements) into v[]; mis = (s mod 4)
+// of the float address, identical for every lane of the tile.
+__device__ __forceinline__ void load8(const float* __restrict__ x, uint64_t s, uint32_t ml, uint32_t mis,
+                                      uint64_t n, float v[8]) {
+  const float* p = x + s;
+  if (ml == 8 && s >= 4 && s + 12 <= n) {
+    const float4* q = reinterpret_cast<const float4*>(p - mis);
+    float4 A = __ldg(q), B = __ldg(q + 1);
+    if (mis == 0) {
+      v[0] = A.x; v[1] = A.y; v[2] = A.z; v[3] = A.w; v[4] = B.x; v[5] = B.y; v[6] = B.z; v[7] = B.w;
+    } else {
+      float4 C = __ldg(q + 2);
+      if (mis == 1) {
+        v[0] = A.y; v[1] = A.z; v[2] = A.w; v[3] = B.x; v[4] = B.y; v[5] = B.z; v[6] = B.w; v[7] = C.x;
+      } else if (mis == 2) {
+        v[0] = A.z; v[1] = A.w; v[2] = B.x; v[3] = B.y; v[4] = B.z; v[5] = B.w; v[6] = C.x; v[7] = C.y;
+      } else {
+        v[0] = A.w; v[1] = B.x; v[2] = B.y; v[3] = B.z; v[4] = B.w; v[5] = C.x; v[6] = C.y; v[7] = C.z;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = (uint32_t)j < ml ? __ldg(p + j) : 0.0f;
+  }
+}
+
+// Stages a tile's bytes (shared memory s_out[align .. align+len)) to global
+// dst (dst % 16 == align): bulk copy for the 16-byte-aligned middle, byte
+// stores for the ragged ends.  Every thread of the CTA calls it.
+__device__ __forceinline__ void flush_span_bulk(uint8_t* __restrict__ gdst, uint8_t* __restrict__ s_out,
+                                                uint32_t align, uint32_t len) {
+  fence_async_smem();
+  __syncthreads();
+  if (len == 0) return;
+  uint8_t* g0 = gdst - align;
+  const uint32_t end = align + len;
+  const uint32_t i0 = (align + 15) & ~15u;
+  const uint32_t i1 = end & ~15u;
+  if (i1 > i0) {
+    if (threadIdx.x == 0) {
+      bulk_store(g0 + i0, s_out + i0, i1 - i0);
+      bulk_commit();
+    }
+    for (uint32_t b = align + threadIdx.x; b < i0; b += blockDim.x) g0[b] = s_out[b];
+    for (uint32_t b = i1 + threadIdx.x; b < end; b += blockDim.x) g0[b] = s_out[b];
+    if (threadIdx.x == 0) bulk_wait_read();
+  } else {
+    for (uint32_t b = align + threadIdx.x; b < end; b += blockDim.x) g0[b] = s_out[b];
+  }
+}
+
+template <int LPB, int ROUNDS>
+__global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
+  constexpr int WARPS = 8;
+  constexpr uint32_t L = 8 * LPB;
+  constexpr int BPR = 32 / LPB;
+  constexpr uint32_t TB = WARPS * ROUNDS * BPR;
   extern __shared__ __align__(16) uint8_t s_out[];
   __shared__ uint32_t s_tk[2];
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint64_t s_base;
+  __shared__ uint32_t s_thr[36];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane % LPB, grp = lane / LPB;
+  if (threadIdx.x < 36) s_thr[threadIdx.x] = a.thr.thr[threadIdx.x];
   uint32_t tile, epoch;
-  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
+  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);  // its barriers publish s_thr
 
   const Segments sg = a.seg;
   const float eb = a.eb_dev ? *a.eb_dev : a.eb;
   const float inv = __fdiv_rn(1.0f, eb);
   const TileInfo ti = tile_info(sg, tile, a.tiles_per_seg, TB, false);
   if (tile == 0) write_header_common(a.out, eb, sg);
-
   const uint64_t lo = sg.lo(ti.seg), hi = sg.hi(ti.seg);
+  const uint64_t n = sg.n;
   uint32_t flags = 0;
 
-  // ---- analysis: q, delta, sign, max, bit count for BPW blocks per warp ----
-  uint32_t vv[BPW], sgn[BPW], bcs[BPW];
+  const uint32_t wfirst = (uint32_t)warp * ROUNDS * BPR;  // first block of the warp, tile-relative
+  const uint32_t mis = (uint32_t)(((uintptr_t)(a.x + lo + 1)) >> 2) & 3u;
+
+  uint32_t vv[ROUNDS][8];
+  uint32_t sgnb[ROUNDS], bcs[ROUNDS], roff[ROUNDS];
   uint32_t wbytes = 0;
-  const uint64_t wblk = ti.blk0 + (uint64_t)warp * BPW;  // first block of this warp
-  const uint32_t wn = ti.nblk > (uint32_t)warp * BPW ? min((uint32_t)BPW, ti.nblk - warp * BPW) : 0;
-  const uint64_t e0 = lo + 1 + wblk * 32;  // first element of the warp's first block
-  float xv[BPW];
+  int32_t carry = 0;
+  if (wfirst < ti.nblk && lane == 0) carry = quantize(__ldg(a.x + lo + (ti.blk0 + wfirst) * L), inv, flags);
+
 #pragma unroll
-  for (int k = 0; k < BPW; k++) {
-    uint64_t e = e0 + (uint64_t)k * 32 + lane;
-    xv[k] = ((uint32_t)k < wn && e < hi) ? __ldg(a.x + e) : 0.0f;
-  }
-  int32_t prev = 0;
-  if (wn) prev = quantize(__ldg(a.x + e0 - 1), inv, flags);
+  for (int r = 0; r < ROUNDS; r++) {
+    const uint32_t bt = wfirst + r * BPR + grp;  // tile-relative block
+    const uint64_t b = ti.blk0 + bt;
+    const uint64_t bs = lo + 1 + b * L;  // first element of the block
+    const uint32_t m = bt < ti.nblk ? (uint32_t)min((uint64_t)L, hi - bs) : 0u;
+    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+    float xv[8];
+    load8(a.x, bs + 8 * sub, ml, mis, n, xv);
+    int32_t q[8];
 #pragma unroll
-  for (int k = 0; k < BPW; k++) {
-    uint64_t e = e0 + (uint64_t)k * 32 + lane;
-    bool valid = (uint32_t)k < wn && e < hi;
-    int32_t q = quantize(xv[k], inv, flags);
-    int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
-    if (lane == 0) qp = prev;
-    prev = __shfl_sync(0xffffffffu, q, 31);
-    uint32_t d = (uint32_t)q - (uint32_t)qp;  // wrapping, as the compiled reference
-    bool neg = valid && (int32_t)d < 0;
-    uint32_t v = valid ? (neg ? 0u - d : d) : 0u;
-    sgn[k] = __ballot_sync(0xffffffffu, neg);
-    uint32_t mx = __reduce_max_sync(0xffffffffu, v);
-    uint32_t bc = bitcount_from_table(mx, a.thr.thr);
-    vv[k] = v;
-    bcs[k] = bc;
-    if ((uint32_t)k < wn) {
-      uint64_t rem = hi - (e0 + (uint64_t)k * 32);
-      uint32_t m = rem < 32 ? (uint32_t)rem : 32;
-      wbytes += block_bytes(m, bc);
+    for (int j = 0; j < 8; j++) q[j] = quantize(xv[j], inv, flags);
+    int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
+    if (lane == 0) prev = carry;
+    carry = __shfl_sync(0xffffffffu, q[7], 31);
+    uint32_t sb = 0, lmax = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      uint32_t d = (uint32_t)q[j] - (uint32_t)prev;  // wrapping, as the compiled reference
+      prev = q[j];
+      bool valid = (uint32_t)j < ml;
+      bool neg = valid && (int32_t)d < 0;
+      uint32_t v = valid ? (neg ? 0u - d : d) : 0u;
+      sb |= (neg ? 1u : 0u) << (7 - j);
+      lmax = max(lmax, v);
+      vv[r][j] = v;
     }
+#pragma unroll
+    for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    uint32_t bc = 0;
+    if (lmax) {
+      int k = 32 - __clz(lmax);
+      bc = k + (k >= 21 && lmax >= s_thr[k + 1] ? 1 : 0);
+    }
+    sgnb[r] = sb;
+    bcs[r] = bc;
+    const uint32_t size = m ? block_bytes(m, bc) : 0u;
+    // byte offsets of the blocks of this round: scan over group leaders
+    uint32_t val = sub == 0 ? size : 0u;
+    uint32_t incl = val;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t gex = __shfl_sync(0xffffffffu, incl - val, grp * LPB);
+    roff[r] = wbytes + gex;
+    wbytes += __shfl_sync(0xffffffffu, incl, 31);
   }
   if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
 
-  // seed of the segment: 4 bytes in front of the tile's first block
   const bool seed = ti.has_seg && ti.first && hi > lo;
   uint32_t wexcl;
   const uint32_t agg = scan_warps<WARPS>(s_w, wbytes, warp, lane, wexcl, seed ? 4u : 0u);
 
-  // ---- decoupled look-back over tile byte counts ----
   if (warp == 0) {
     uint64_t excl = 0;
     if (tile == 0) {
@@ -256,11 +341,9 @@ __global__ void __launch_bounds__(WARPS * 32) compress_fm1_l32(CompressArgs a) {
     if (lane == 0) s_base = excl;
   }
   __syncthreads();
-  const uint64_t base = s_base;
-  const uint64_t head = 4 + 8ull * sg.T;
-  const uint64_t gpos = head + base;  // absolute stream position of the tile
+  const uint64_t gpos = 4 + 8ull * sg.T + s_base;  // absolute stream position of the tile
   if (tile == a.ntiles - 1 && threadIdx.x == 0) *a.out_size = gpos + agg;
-  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, base);
+  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, s_base);
   if (gpos + agg > a.cap) {
     if (threadIdx.x == 0) atomicOr(a.err, kErrCapacity);
     return;
@@ -269,22 +352,52 @@ __global__ void __launch_bounds__(WARPS * 32) compress_fm1_l32(CompressArgs a) {
   // ---- pack into shared memory at the destination's 16-byte phase ----
   const uint32_t align = (uint32_t)(((uintptr_t)a.out + gpos) & 15);
   uint8_t* s_tile = s_out + align;
-  if (seed && warp == 0) {
-    int32_t sq = quantize(__ldg(a.x + lo), inv, flags);
-    if (lane < 4) s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
+  if (seed && warp == 0 && lane < 4) {
+    uint32_t f2 = 0;
+    int32_t sq = quantize(__ldg(a.x + lo), inv, f2);
+    s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
   }
-  uint32_t off = wexcl;
+  const uint32_t front = (seed ? 4u : 0u) + wexcl;
 #pragma unroll
-  for (int k = 0; k < BPW; k++) {
-    if ((uint32_t)k < wn) {
-      uint64_t rem = hi - (e0 + (uint64_t)k * 32);
-      uint32_t m = rem < 32 ? (uint32_t)rem : 32;
-      pack_block32(s_tile + off, m, bcs[k], sgn[k], vv[k], lane);
-      off += block_bytes(m, bcs[k]);
+  for (int r = 0; r < ROUNDS; r++) {
+    const uint32_t bt = wfirst + r * BPR + grp;
+    if (bt >= ti.nblk) continue;
+    const uint64_t bs = lo + 1 + (ti.blk0 + bt) * L;
+    const uint32_t m = (uint32_t)min((uint64_t)L, hi - bs);
+    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+    const uint32_t bc = bcs[r];
+    uint8_t* dst = s_tile + front + roff[r];
+    if (sub == 0) dst[0] = (uint8_t)bc;
+    if (bc == 0 || ml == 0) continue;
+    const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
+    dst[1 + sub] = (uint8_t)sgnb[r];  // sign bits, szp_TypeManager.cc:820-844
+    if (B) {  // byte planes, szp_TypeManager.cc:36-52
+      uint8_t* q8 = dst + 1 + ns + 8 * B * sub;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        if ((uint32_t)j < ml) {
+          uint32_t h = vv[r][j] >> rr;
+          q8[j * B] = (uint8_t)h;
+          if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
+          if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
+          if (B > 3) q8[j * B + 3] = (uint8_t)(h >> 24);
+        }
+      }
+    }
+    if (rr) {  // remainder bits, MSB first, szp_TypeManager.cc:122-434
+      const uint32_t mask = (1u << rr) - 1u;
+      uint64_t acc = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc = (acc << rr) | (uint64_t)((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
+      uint8_t* rp = dst + 1 + ns + B * m + rr * sub;
+      const uint32_t nb = (ml * rr + 7) >> 3;
+      const uint32_t top = 8 * rr - 8;
+#pragma unroll
+      for (uint32_t k = 0; k < 7; k++)
+        if (k < nb) rp[k] = (uint8_t)(acc >> (top - 8 * k));
     }
   }
-  __syncthreads();
-  flush_span(a.out + gpos, s_out, align, agg);
+  flush_span_bulk(a.out + gpos, s_out, align, agg);
 }
 
 // ---------------------------------------------------------------------------
@@ -561,13 +674,27 @@ __global__ void bitcount_probe_kernel(const uint32_t* __restrict__ in, uint8_t* 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-constexpr int kFm1Warps = 8, kFm1Bpw = 8;
 constexpr int kGenWarps = 8;
 
+// lanes per block for the lane-group kernel, 0 if L needs the generic one
+static int lanes_per_block(uint32_t L) {
+  switch (L) {
+    case 8: return 1;
+    case 16: return 2;
+    case 32: return 4;
+    case 64: return 8;
+    case 128: return 16;
+    case 256: return 32;
+    default: return 0;
+  }
+}
+constexpr int kRounds = 4;
+
 uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw) {
-  if (L == 32) {
-    bpw = kFm1Bpw;
-    return kFm1Warps * kFm1Bpw;
+  int lpb = lanes_per_block(L);
+  if (lpb) {
+    bpw = kRounds * (32 / lpb);
+    return 8 * bpw;
   }
   // keep the staged tile near 16 KB
   uint32_t mb = max_block_bytes(L) + 4;
@@ -577,22 +704,36 @@ uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw) {
 }
 
 size_t compress_smem_bytes(uint32_t L, uint32_t tb) {
-  return 16 + 4 + (size_t)tb * (max_block_bytes(L) + 4) + 16;
+  return 16 + 4 + (size_t)tb * (max_block_bytes(L) + 4) + 32;
+}
+
+template <int LPB>
+static cudaError_t launch_lanes(const CompressArgs& a, size_t smem, cudaStream_t st) {
+  auto k = compress_fm1_lanes<LPB, kRounds>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.ntiles, 256, smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st) {
   size_t smem = compress_smem_bytes(a.seg.L, a.tb);
-  if (!fm2 && a.seg.L == 32) {
-    auto k = compress_fm1_l32<kFm1Warps, kFm1Bpw>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<a.ntiles, kFm1Warps * 32, smem, st>>>(a);
-  } else if (!fm2) {
+  if (!fm2) {
+    switch (lanes_per_block(a.seg.L)) {
+      case 1: return launch_lanes<1>(a, smem, st);
+      case 2: return launch_lanes<2>(a, smem, st);
+      case 4: return launch_lanes<4>(a, smem, st);
+      case 8: return launch_lanes<8>(a, smem, st);
+      case 16: return launch_lanes<16>(a, smem, st);
+      case 32: return launch_lanes<32>(a, smem, st);
+      default: break;
+    }
     auto k = compress_generic<kGenWarps, false>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
   } else {
     auto k = compress_generic<kGenWarps, true>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
   }
   return cudaGetLastError();

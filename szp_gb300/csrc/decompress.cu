@@ -1,37 +1,39 @@
 // decompress.cu -- SZp fastmode1 / fastmode2 float32 decompressors for sm_103a.
 //
 // The stream keeps no block index: a block's position depends on the bit
-// counts of all blocks before it in its segment (szpd_float.cc:76-118).  Three
-// launches recover it in parallel:
+// counts of all blocks before it in its segment (szpd_float.cc:76-118).  Four
+// launches recover the positions and decode:
 //
-//  1. dec_setup   one CTA reads eb and the T segment offsets, validates them
-//                 and cuts every segment's block region into fixed chunks.
-//  2. locate      one warp per chunk.  It walks the chunk from every entry
-//                 offset a block could start at (0 .. largest block - 1),
-//                 merging walks that meet (claims in shared memory) so the
-//                 work is roughly one walk.  The result is the chunk's exit
-//                 function entry -> first position past the chunk.  When all
-//                 live entries agree (the usual case, walks re-synchronise),
-//                 the chunk's exit is known at once; otherwise successors
-//                 compose functions in a look-back.  With its entry known the
-//                 chunk counts its blocks, a second look-back turns counts
-//                 into block indices, and every block's header offset is
-//                 written to blkpos.
-//  3. decode      one CTA per run of blocks: unpack sign bits and fixed-length
-//                 fields, prefix-add deltas (fastmode1: decoupled look-back
-//                 over the tiles of a segment), dequantize (float)q*eb.
+//  1. dec_setup   one CTA reads eb and the T segment offsets, validates them and
+//                 cuts every segment's block region into fixed chunks.
+//  2. walk        one thread per chunk walks the chain of block headers.  A
+//                 chunk other than a segment's first does not know where its
+//                 first header is, so it starts `overlap` bytes early at the
+//                 first position whose chain stays valid: chains started on
+//                 payload bytes die within a step or two (a header byte must be
+//                 <= 33) or land on a true header and from then on follow the
+//                 true chain.  The chunk records its first header, its exit
+//                 (first header past it) and its header count.
+//  3. verify      chunk c is right when its first header equals chunk c-1's
+//                 exit (induction from each segment's first chunk, which starts
+//                 exactly).  Checks are independent; the last CTA re-walks, in
+//                 order, the rare chunks that fail, from their true entries.
+//  4. positions   a decoupled look-back over header counts gives every chunk
+//                 its first block index; each chunk re-walks and writes the
+//                 header offset of each of its blocks.
+//  5. decode      per tile of blocks: the tile's stream span is staged in shared
+//                 memory by a bulk copy; LPB lanes per block unpack 8 elements
+//                 each (sign byte, byte planes, remainder bits are byte-aligned
+//                 per 8 elements), prefix-add (fastmode1: warp/CTA scans and a
+//                 look-back over the tiles of a segment) and dequantize.
 #include "szp_device.cuh"
 #include "szp_kernels.h"
+#include "szp_tma.cuh"
 
 namespace szp {
 
-constexpr uint16_t kExEnd = 0xFFFE;    // walk left the segment
-constexpr uint16_t kExDead = 0xFFFF;   // walk met an invalid header
-constexpr uint16_t kExMerged = 0xFFFD;
-constexpr uint16_t kExLive = 0xFFFC;
-constexpr uint16_t kFree = 0xFFFF;
-constexpr int kLocWarps = 4;
-constexpr uint32_t kPreMax = 64;
+constexpr uint32_t kPosEnd = 0xFFFFFFFEu;   // the walk left the segment region
+constexpr uint32_t kPosDead = 0xFFFFFFFFu;  // the walk met an invalid header
 
 // Size of a full block whose bit-count byte is b; 0 if b is not a valid
 // header.  fastmode2 blocks carry a 4-byte seed and L-1 deltas.
@@ -47,41 +49,12 @@ __host__ __device__ __forceinline__ uint32_t max_walk_block(uint32_t L, bool fm2
 }
 
 uint32_t locate_chunk_bytes(uint32_t maxsz) {
-  uint32_t c = 2048;
+  uint32_t c = 1024;
   while (c < 2 * maxsz) c *= 2;
   return c;
 }
 
-// per-warp shared memory layout of the locate kernel
-struct LocLayout {
-  uint32_t bytes_off, claim_off, pos_off, res_off, tgt_off, l0_off, l1_off, lead_off, pre_off, per_warp;
-  __host__ __device__ LocLayout(uint32_t C, uint32_t maxsz) {
-    uint32_t o = 0;
-    bytes_off = o;
-    o += (C + maxsz + 32 + 15) & ~15u;
-    claim_off = o;
-    o += 2 * C;
-    pos_off = o;
-    o += 2 * maxsz;
-    res_off = o;
-    o += 2 * maxsz;
-    tgt_off = o;
-    o += 2 * maxsz;
-    l0_off = o;
-    o += 2 * maxsz;
-    l1_off = o;
-    o += 2 * maxsz;
-    lead_off = o;
-    o += 2 * C;
-    pre_off = o;
-    o += 2 * kPreMax;
-    per_warp = (o + 15) & ~15u;
-  }
-};
-
-size_t locate_smem_bytes(uint32_t chunk, uint32_t maxsz) {
-  return (size_t)LocLayout(chunk, maxsz).per_warp * kLocWarps;
-}
+uint32_t locate_overlap_bytes(uint32_t maxsz) { return maxsz < 128 ? 256u : 2 * maxsz; }
 
 __device__ __forceinline__ uint64_t load_u64le(const uint8_t* p) {
   uint64_t v = 0;
@@ -185,350 +158,281 @@ __device__ __forceinline__ uint64_t seg_blocks(const Segments& sg, uint32_t t, b
 }
 
 // ---------------------------------------------------------------------------
-// 2. locate block headers
+// 2-4. locate block headers
 // ---------------------------------------------------------------------------
-template <bool FM2>
-__global__ void __launch_bounds__(kLocWarps * 32) locate_kernel(DecArgs a) {
-  extern __shared__ __align__(16) uint8_t smem[];
-  __shared__ uint32_t s_tk[2];
-  uint32_t tk, epoch;
-  draw_ticket(a.ls, a.nlocate_ctas, tk, epoch, s_tk);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const Segments sg = a.seg;
-  const uint32_t T = sg.T, L = sg.L, C = a.chunk, maxsz = a.maxsz;
-  const uint32_t c = tk * kLocWarps + warp;
-  const uint32_t nch = a.chunk_base[T];
-  if (c >= nch) return;  // no CTA-wide barrier below this point
 
-  // segment of chunk c: largest t with chunk_base[t] <= c
+// Segment of chunk c: largest t with chunk_base[t] <= c.
+__device__ __forceinline__ uint32_t chunk_segment(const uint32_t* __restrict__ cb, uint32_t T, uint32_t c) {
   uint32_t lo_t = 0, hi_t = T - 1;
   while (lo_t < hi_t) {
     uint32_t mid = (lo_t + hi_t + 1) >> 1;
-    if (a.chunk_base[mid] <= c) lo_t = mid; else hi_t = mid - 1;
+    if (cb[mid] <= c) lo_t = mid; else hi_t = mid - 1;
   }
-  const uint32_t t = lo_t;
-  const uint32_t first = a.chunk_base[t];
-  const uint32_t ci = c - first;
-  const uint64_t R0 = a.reg0[t], R1 = a.reg1[t];
-  const uint64_t c0 = R0 + (uint64_t)ci * C;
-  const uint64_t rest = R1 - c0;
-  const uint32_t clen = (uint32_t)(rest < C ? rest : C);
-  const uint32_t end_rel = (uint32_t)(rest < (uint64_t)clen + maxsz + 8 ? rest : (uint64_t)clen + maxsz + 8);
-  const uint32_t nload = end_rel;  // never read past the segment region
+  return lo_t;
+}
 
-  const LocLayout lay(C, maxsz);
-  uint8_t* base = smem + warp * lay.per_warp;
-  uint8_t* sb = base + lay.bytes_off;
-  uint16_t* claim = reinterpret_cast<uint16_t*>(base + lay.claim_off);
-  uint16_t* pos_s = reinterpret_cast<uint16_t*>(base + lay.pos_off);
-  uint16_t* res_s = reinterpret_cast<uint16_t*>(base + lay.res_off);
-  uint16_t* tgt_s = reinterpret_cast<uint16_t*>(base + lay.tgt_off);
-  uint16_t* list0 = reinterpret_cast<uint16_t*>(base + lay.l0_off);
-  uint16_t* list1 = reinterpret_cast<uint16_t*>(base + lay.l1_off);
-  uint16_t* lead = reinterpret_cast<uint16_t*>(base + lay.lead_off);
-  uint16_t* pre = reinterpret_cast<uint16_t*>(base + lay.pre_off);
+// Byte size of the block whose first byte is at region offset p, or 0 when
+// its bit-count byte is invalid or lies past the region (length rlen).
+__device__ __forceinline__ uint32_t step_size(const uint8_t* __restrict__ base, uint32_t p, uint32_t rlen,
+                                              uint32_t L, bool fm2) {
+  uint32_t hp = fm2 ? p + 4 : p;
+  if (hp >= rlen) return 0;
+  return full_block_size(__ldg(base + hp), L, fm2);
+}
 
-  // stage the chunk (and the longest block that may start in it)
-  {
-    const uint8_t* src = a.in + c0;
-    uint32_t mis = (uint32_t)((uintptr_t)src & 15);
-    uint32_t headb = mis ? 16 - mis : 0;
-    if (headb > nload) headb = nload;
-    for (uint32_t i = lane; i < headb; i += 32) sb[i] = src[i];
-    uint32_t nvec = (nload - headb) >> 4;
-    const uint4* s4 = reinterpret_cast<const uint4*>(src + headb);
-    for (uint32_t i = lane; i < nvec; i += 32) {
-      uint4 v = __ldg(s4 + i);
-      uint8_t* d = sb + headb + 16 * i;
-      const uint8_t* vb = reinterpret_cast<const uint8_t*>(&v);
-#pragma unroll
-      for (int k = 0; k < 16; k++) d[k] = vb[k];
+// Walks from p through [.., cE): returns the header count, sets *exit to the
+// first header position >= cE (kPosEnd when it is past the region) or
+// kPosDead.
+__device__ __forceinline__ uint32_t walk_from(const uint8_t* __restrict__ base, uint32_t p, uint32_t cE,
+                                              uint32_t rlen, uint32_t L, bool fm2, uint32_t* exit) {
+  uint32_t k = 0;
+  while (p < cE) {
+    uint32_t sz = step_size(base, p, rlen, L, fm2);
+    if (!sz) {
+      *exit = kPosDead;
+      return k;
     }
-    for (uint32_t i = headb + 16 * nvec + lane; i < nload; i += 32) sb[i] = src[i];
-    for (uint32_t i = lane; i < clen; i += 32) claim[i] = kFree;
+    k++;
+    p += sz;
   }
-  __syncwarp();
+  *exit = p >= rlen ? kPosEnd : p;
+  return k;
+}
 
-  // header byte of a block at p (p < clen); 0 size means invalid
-  auto step = [&](uint32_t p) -> uint32_t {
-    uint32_t hp = FM2 ? p + 4 : p;
-    if (hp >= nload) return 0;
-    return full_block_size(sb[hp], L, FM2);
-  };
+struct ChunkGeom {
+  uint32_t t, ci, cS, cE, rlen;
+  const uint8_t* base;
+};
 
-  // ---- walks from every entry, merged through claims ----
-  const uint32_t E = maxsz;
-  uint32_t cnt = 0;
-  for (uint32_t e = lane; e < E; e += 32) {
-    if (e >= clen) {
-      res_s[e] = kExEnd;  // only the short last chunk: past its end is past the segment
-    } else {
-      res_s[e] = kExLive;
-      pos_s[e] = (uint16_t)e;
-    }
-  }
-  {
-    uint32_t live = E < clen ? E : clen;
-    for (uint32_t e = lane; e < live; e += 32) list0[e] = (uint16_t)e;
-    cnt = live;
-  }
-  __syncwarp();
-  uint16_t* cur = list0;
-  uint16_t* nxt = list1;
-  int leader = -1;
-  while (cnt > 0) {
-    if (cnt == 1) {
-      leader = cur[0];
-      break;
-    }
-    uint32_t newcnt = 0;
-    for (uint32_t b0 = 0; b0 < cnt; b0 += 32) {
-      uint32_t i = b0 + lane;
-      bool live = false;
-      uint16_t id = 0;
-      if (i < cnt) {
-        id = cur[i];
-        uint32_t p = pos_s[id];
-        uint16_t old = atomicCAS(claim + p, kFree, id);
-        if (old != kFree) {
-          res_s[id] = kExMerged;
-          tgt_s[id] = old;
-        } else {
-          uint32_t sz = step(p);
-          if (!sz) {
-            res_s[id] = kExDead;
-          } else {
-            uint32_t np = p + sz;
-            if (np >= end_rel) res_s[id] = kExEnd;
-            else if (np >= clen) res_s[id] = (uint16_t)(np - clen);
-            else {
-              pos_s[id] = (uint16_t)np;
-              live = true;
-            }
-          }
-        }
-      }
-      uint32_t bal = __ballot_sync(0xffffffffu, live);
-      if (live) nxt[newcnt + __popc(bal & ((1u << lane) - 1u))] = id;
-      newcnt += __popc(bal);
-    }
-    __syncwarp();
-    uint16_t* tmp = cur;
-    cur = nxt;
-    nxt = tmp;
-    cnt = newcnt;
-  }
-  // one walk left: follow it without atomics, recording its headers.  Its
-  // recorded headers can be spliced onto the true path unless it ended by
-  // merging into an earlier walk (whose later headers are not recorded).
-  uint32_t nlead = 0;
-  bool can_splice = false;
-  if (leader >= 0) {
-    uint32_t ok = 0;
-    if (lane == 0) {
-      uint32_t p = pos_s[leader];
-      uint32_t k = 0;
-      uint16_t r = kExDead;
-      while (true) {
-        uint16_t cl = claim[p];
-        if (cl != kFree) {
-          r = kExMerged;
-          tgt_s[leader] = cl;
-          break;
-        }
-        uint32_t sz = step(p);
-        if (!sz) {
-          r = kExDead;
-          break;
-        }
-        claim[p] = (uint16_t)(0x8000u | k);
-        lead[k++] = (uint16_t)p;
-        uint32_t np = p + sz;
-        if (np >= end_rel) {
-          r = kExEnd;
-          break;
-        }
-        if (np >= clen) {
-          r = (uint16_t)(np - clen);
-          break;
-        }
-        p = np;
-      }
-      res_s[leader] = r;
-      nlead = k;
-      ok = r != kExMerged;
-    }
-    nlead = __shfl_sync(0xffffffffu, nlead, 0);
-    can_splice = __shfl_sync(0xffffffffu, ok, 0) != 0;
-  }
-  __syncwarp();
-  // resolve merged walks to their final exits (claims only point backwards)
-  uint32_t fmin = 0xFFFFu, fmax = 0;
-  for (uint32_t e = lane; e < E; e += 32) {
-    uint32_t j = e;
-    uint16_t r = res_s[j];
-    for (uint32_t guard = 0; r == kExMerged && guard < E + 1; guard++) {
-      uint16_t tg = tgt_s[j];
-      j = tg & 0x7FFFu;  // list-phase claims hold walk ids
-      if (j >= E) {
-        r = kExDead;
-        break;
-      }
-      r = res_s[j];
-    }
-    if (r == kExMerged || r == kExLive) r = kExDead;
-    // other lanes following a chain through e read either the merged marker
-    // (and then the unchanged target) or this final value: both agree
-    res_s[e] = r;
-    if (r != kExDead) {
-      fmin = min(fmin, (uint32_t)r);
-      fmax = max(fmax, (uint32_t)r);
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    fmin = min(fmin, __shfl_xor_sync(0xffffffffu, fmin, o));
-    fmax = max(fmax, __shfl_xor_sync(0xffffffffu, fmax, o));
-  }
-  __syncwarp();
-  const bool constant = fmin == fmax;  // all live entries leave at one place
-  const uint16_t cexit = constant ? (uint16_t)fmin : kExDead;
+__device__ __forceinline__ ChunkGeom chunk_geom(const DecArgs& a, uint32_t c) {
+  ChunkGeom g;
+  g.t = chunk_segment(a.chunk_base, a.seg.T, c);
+  g.ci = c - a.chunk_base[g.t];
+  const uint64_t R0 = a.reg0[g.t], R1 = a.reg1[g.t];
+  g.rlen = (uint32_t)(R1 - R0);
+  g.cS = g.ci * a.chunk;
+  g.cE = min(g.cS + a.chunk, g.rlen);
+  g.base = a.in + R0;
+  return g;
+}
 
-  uint64_t* st_entry = a.status;
-  uint64_t* st_count = a.status + a.status_stride;
-
-  // ---- publish exit function, find own entry ----
-  if (!constant) {
-    for (uint32_t e = lane; e < E; e += 32) a.fn[(uint64_t)c * maxsz + e] = res_s[e];
-    __threadfence();
-    __syncwarp();
-  }
-  uint32_t entry;
-  if (ci == 0) {
-    entry = 0;
-    if (lane == 0) st_release_u64(st_entry + c, make_status(epoch, kFlagInclusive, res_s[0]));
+// 2. speculative walk of every chunk
+template <bool FM2>
+__global__ void __launch_bounds__(256) walk_kernel(DecArgs a) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.plan->bad || c >= a.chunk_base[a.seg.T]) return;
+  const ChunkGeom g = chunk_geom(a, c);
+  const uint32_t L = a.seg.L;
+  uint32_t h, x, k;
+  if (g.ci == 0) {
+    h = 0;  // a segment's block region starts with a header
+    k = walk_from(g.base, 0, g.cE, g.rlen, L, FM2, &x);
   } else {
-    if (lane == 0) {
-      if (constant) st_release_u64(st_entry + c, make_status(epoch, kFlagInclusive, cexit));
-      else st_release_u64(st_entry + c, make_status(epoch, kFlagAggregate, 0));
-    }
-    // nearest predecessor whose exit is known
-    int64_t k = (int64_t)c - 1;
-    int64_t found = -1;
-    uint32_t fval = 0, spins = 0;
-    bool timeout = false;
-    while (found < 0) {
-      int64_t idx = k - lane;
-      bool inrange = idx >= (int64_t)first;
-      uint64_t s = inrange ? ld_volatile_u64(st_entry + idx) : 0;
-      bool ready = !inrange || (status_epoch(s) == (epoch & 0xFFFFF) && status_flag(s) != 0);
-      uint32_t incl = __ballot_sync(0xffffffffu, inrange && ready && status_flag(s) == kFlagInclusive);
-      uint32_t notready = __ballot_sync(0xffffffffu, !ready);
-      uint32_t upto = incl & (0u - incl);
-      uint32_t relevant = upto ? (upto | (upto - 1)) : 0xffffffffu;
-      if (notready & relevant) {
-        if (++spins > kSpinLimit) {
-          timeout = true;
+    // find a chain that survives from the overlap window through the chunk
+    const uint32_t w0 = g.cS > a.overlap ? g.cS - a.overlap : 0;
+    uint32_t anchor = w0, budget = 8 * (a.chunk + a.overlap);
+    h = kPosDead;
+    x = kPosDead;
+    k = 0;
+    while (anchor < g.cE && budget) {
+      uint32_t p = anchor;
+      bool alive = true;
+      while (p < g.cS && budget) {
+        budget--;
+        uint32_t sz = step_size(g.base, p, g.rlen, L, FM2);
+        if (!sz) {
+          alive = false;
           break;
         }
+        p += sz;
+      }
+      if (!alive) {
+        anchor++;
         continue;
       }
-      if (upto) {
-        int fl = __ffs(upto) - 1;
-        found = k - fl;
-        fval = (uint32_t)__shfl_sync(0xffffffffu, (uint32_t)status_value(s), fl);
-      } else {
-        k -= 32;  // the segment's first chunk is always inclusive, so this ends
-        if (k < (int64_t)first) {
-          timeout = true;  // unreachable unless the status words are corrupt
-          break;
-        }
+      uint32_t ex;
+      uint32_t kk = walk_from(g.base, p, g.cE, g.rlen, L, FM2, &ex);
+      budget = budget > kk ? budget - kk : 0;
+      if (ex == kPosDead) {
+        anchor = anchor < g.cS ? anchor + 1 : p + 1;  // a false chain: try the next start
+        continue;
       }
-    }
-    if (timeout) {
-      if (lane == 0) atomicOr(a.err, kErrLookbackTimeout);
-      entry = kExDead;
-    } else {
-      if (found + 1 < (int64_t)c) __threadfence();  // order the fn-row reads after the status reads
-      uint32_t e = fval;
-      for (int64_t m = found + 1; m < (int64_t)c; m++) {
-        if (e >= maxsz) break;  // END / DEAD propagate
-        e = a.fn[(uint64_t)m * maxsz + e];
-      }
-      entry = e;
-    }
-    if (!constant && lane == 0) {
-      uint16_t ex = entry < maxsz ? res_s[entry] : (uint16_t)entry;
-      st_release_u64(st_entry + c, make_status(epoch, kFlagInclusive, ex));
+      h = p >= g.rlen ? kPosEnd : p;
+      x = ex;
+      k = kk;
+      break;
     }
   }
+  a.walks[c] = make_uint4(h, x, k, 0);
+}
 
-  // ---- headers on the true path through this chunk ----
-  uint32_t npre = 0, splice = 0xFFFFFFFFu, count = 0;
-  bool overflow = false;
-  if (lane == 0 && entry < clen) {
-    uint32_t p = entry;
-    while (p < clen) {
-      uint16_t cl = claim[p];
-      if (can_splice && (cl & 0x8000u) && cl != kFree) {
-        splice = cl & 0x7FFFu;
+__device__ __forceinline__ uint4 ld_volatile_u4(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.volatile.global.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p)
+               : "memory");
+  return v;
+}
+
+// Walks chunk c exactly from entry e (serial repair path).
+__device__ __forceinline__ uint4 exact_walk(const DecArgs& a, const ChunkGeom& g, uint32_t e, bool fm2) {
+  if (e == kPosEnd || e == kPosDead) return make_uint4(e, e, 0, 0);
+  uint32_t x;
+  uint32_t k = walk_from(g.base, e, g.cE, g.rlen, a.seg.L, fm2, &x);
+  return make_uint4(e, x, k, 0);
+}
+
+// 3. verification; the last CTA repairs failed chunks in order.
+template <bool FM2>
+__global__ void __launch_bounds__(256) verify_kernel(DecArgs a) {
+  __shared__ bool s_last;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nch = a.plan->bad ? 0 : a.chunk_base[a.seg.T];
+  if (c < nch) {
+    const ChunkGeom g = chunk_geom(a, c);
+    uint4 w = a.walks[c];
+    bool ok = true;
+    if (g.ci > 0) {
+      const uint32_t px = a.walks[c - 1].y;
+      if (px == kPosEnd) {
+        w = make_uint4(kPosEnd, kPosEnd, 0, 0);  // inside the segment's last block
+      } else {
+        ok = px == w.x;
+      }
+    }
+    a.final_walks[c] = w;
+    if (!ok) {
+      uint32_t i = atomicAdd(&a.counters[0], 1u);
+      if (i < a.max_chunks) a.fails[i] = c;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&a.counters[1], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  const uint32_t nf = min(*(volatile uint32_t*)&a.counters[0], a.max_chunks);
+  a.counters[0] = 0;
+  a.counters[1] = 0;
+  if (nf == 0) return;
+  if (nf > 2048) {
+    // many failures (garbage past the data, or adversarial input): one
+    // ordered pass over every chunk
+    for (uint32_t m = 1; m < nch; m++) {
+      const ChunkGeom g = chunk_geom(a, m);
+      if (g.ci == 0) continue;
+      const uint32_t e = ld_volatile_u4(a.final_walks + m - 1).y;
+      if (e == kPosEnd || e == kPosDead) {
+        a.final_walks[m] = make_uint4(e, e, 0, 0);
+        continue;
+      }
+      if (ld_volatile_u4(a.final_walks + m).x != e) a.final_walks[m] = exact_walk(a, g, e, FM2);
+    }
+    __threadfence();
+    return;
+  }
+  // order the failures (usually a handful)
+  uint32_t* f = a.fails;
+  for (uint32_t i = 1; i < nf; i++) {
+    uint32_t v = f[i], j = i;
+    while (j > 0 && f[j - 1] > v) {
+      f[j] = f[j - 1];
+      j--;
+    }
+    f[j] = v;
+  }
+  uint32_t done_upto = 0;  // chunks below this are final
+  for (uint32_t i = 0; i < nf; i++) {
+    uint32_t m = f[i];
+    if (m < done_upto) continue;
+    ChunkGeom g = chunk_geom(a, m);
+    const uint32_t seg_end = a.chunk_base[g.t + 1];
+    while (true) {
+      const uint32_t e = ld_volatile_u4(a.final_walks + m - 1).y;
+      if (e == kPosEnd || e == kPosDead) {
+        // past the segment's last block (or a dead chain: the block count
+        // check reports it): nothing more in this segment
+        for (uint32_t r = m; r < seg_end; r++) a.final_walks[r] = make_uint4(e, e, 0, 0);
+        done_upto = seg_end;
         break;
       }
-      uint32_t sz = step(p);
-      if (!sz) break;
-      if (npre < kPreMax) pre[npre] = (uint16_t)p;
-      else overflow = true;
-      npre++;
-      p += sz;
+      uint4 w = exact_walk(a, g, e, FM2);
+      a.final_walks[m] = w;
+      done_upto = m + 1;
+      if (m + 1 >= seg_end) break;
+      uint4 nx = ld_volatile_u4(a.final_walks + m + 1);
+      if (w.y != kPosEnd && w.y != kPosDead && nx.x == w.y) break;  // the successor verifies
+      m++;
+      g = chunk_geom(a, m);
     }
-    count = npre + (splice != 0xFFFFFFFFu ? nlead - splice : 0);
   }
-  count = __shfl_sync(0xffffffffu, count, 0);
-  npre = __shfl_sync(0xffffffffu, npre, 0);
-  splice = __shfl_sync(0xffffffffu, splice, 0);
-  overflow = __shfl_sync(0xffffffffu, overflow ? 1 : 0, 0) != 0;
+  __threadfence();
+}
 
-  // ---- block index of the first header: look-back over counts ----
-  uint64_t g0 = 0;
-  if (ci == 0) {
-    if (lane == 0) st_release_u64(st_count + c, make_status(epoch, kFlagInclusive, count));
-  } else {
-    if (lane == 0) st_release_u64(st_count + c, make_status(epoch, kFlagAggregate, count));
-    g0 = lookback_sum(st_count, c, first, epoch, a.err);
-    if (lane == 0) st_release_u64(st_count + c, make_status(epoch, kFlagInclusive, g0 + count));
+// 4. block indices (look-back over header counts) and header offsets.
+template <bool FM2>
+__global__ void __launch_bounds__(256) positions_kernel(DecArgs a) {
+  __shared__ uint32_t s_tk[2];
+  __shared__ uint32_t s_w[9];
+  __shared__ uint64_t s_base;
+  uint32_t tile, epoch;
+  draw_ticket(a.ls, a.nchunk_ctas, tile, epoch, s_tk);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t c = tile * 256 + threadIdx.x;
+  const uint32_t nch = a.plan->bad ? 0 : a.chunk_base[a.seg.T];
+  uint4 w = make_uint4(kPosEnd, kPosEnd, 0, 0);
+  if (c < nch) w = a.final_walks[c];
+  const uint32_t k = w.z;
+  // CTA scan of counts
+  uint32_t incl = k;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
   }
-  const uint64_t nb = seg_blocks(sg, t, FM2);
-  const uint64_t gb = seg_block_base(sg, t, FM2);
-  const uint32_t rel0 = (uint32_t)(c0 - R0);
-  if (!overflow) {
-    for (uint32_t i = lane; i < count; i += 32) {
-      uint64_t g = g0 + i;
-      if (g >= nb) break;
-      uint32_t p = i < npre ? pre[i] : lead[splice + (i - npre)];
-      a.blkpos[gb + g] = rel0 + p;
+  if (lane == 31) s_w[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t v = lane < 8 ? s_w[lane] : 0u;
+    uint32_t vi = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, vi, o);
+      if (lane >= o) vi += y;
     }
-  } else if (lane == 0) {
-    // long unmerged prefix (rare): walk again, writing as we go
-    uint32_t p = entry;
-    uint64_t g = g0;
-    while (p < clen && g < g0 + npre) {
-      uint16_t cl = claim[p];
-      if (can_splice && (cl & 0x8000u) && cl != kFree) break;
-      uint32_t sz = step(p);
+    if (lane < 8) s_w[lane] = vi - v;
+    uint32_t agg = __shfl_sync(0xffffffffu, vi, 7);
+    uint64_t excl = 0;
+    if (tile == 0) {
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+    } else {
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+    }
+    if (lane == 0) s_base = excl;
+  }
+  __syncthreads();
+  if (c >= nch) return;
+  const uint64_t g0 = s_base + s_w[warp] + (incl - k);  // global index of the chunk's first header
+  const ChunkGeom g = chunk_geom(a, c);
+  const Segments& sg = a.seg;
+  const uint64_t gb = seg_block_base(sg, g.t, FM2), nb = seg_blocks(sg, g.t, FM2);
+  if (k && w.x < g.rlen) {
+    uint32_t p = w.x;
+    for (uint32_t i = 0; i < k; i++) {
+      uint64_t gi = g0 + i;
+      if (gi >= gb && gi < gb + nb) a.blkpos[gi] = p;
+      uint32_t sz = step_size(g.base, p, g.rlen, sg.L, FM2);
       if (!sz) break;
-      if (g < nb) a.blkpos[gb + g] = rel0 + p;
-      g++;
       p += sz;
-    }
-    for (uint32_t i = npre; i < count; i++) {
-      uint64_t gg = g0 + i;
-      if (gg < nb) a.blkpos[gb + gg] = rel0 + lead[splice + (i - npre)];
     }
   }
   // the last chunk of a segment checks the block total
-  if (lane == 0 && c + 1 == a.chunk_base[t + 1]) {
-    uint64_t total = g0 + count;
-    bool last_seg = t + 1 == T;
-    if (total < nb || (!last_seg && total != nb)) atomicOr(a.err, kErrBlockCount);
+  if (c + 1 == a.chunk_base[g.t + 1]) {
+    const uint64_t end = g0 + k;
+    const bool last_seg = g.t + 1 == sg.T;
+    if (end < gb + nb || (!last_seg && end != gb + nb)) atomicOr(a.err, kErrBlockCount);
   }
 }
 
@@ -626,17 +530,43 @@ __device__ __forceinline__ DecTile dec_tile(const Segments& sg, uint32_t tile, u
   return d;
 }
 
-// fastmode1, blockSize 32: one warp per block, one element per lane.
-template <int WARPS, int BPW>
-__global__ void __launch_bounds__(WARPS * 32) decode_fm1_l32(DecArgs a) {
+// Stores 8 consecutive floats at y[s..) (ml valid); mis = s mod 4 of the
+// float address (same for every lane of the tile).
+__device__ __forceinline__ void store8(float* __restrict__ y, uint64_t s, uint32_t ml, uint32_t mis,
+                                       const float v[8]) {
+  float* p = y + s;
+  if (ml == 8 && mis == 0) {
+    reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+  } else if (ml == 8 && mis == 2) {
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) reinterpret_cast<float2*>(p)[j / 2] = make_float2(v[j], v[j + 1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if ((uint32_t)j < ml) p[j] = v[j];
+  }
+}
+
+// fastmode1, blockSize L = 8*LPB: LPB lanes per block, 8 elements per lane
+// (the byte layout of 8 elements is self-contained, see compress.cu).
+template <int LPB, int ROUNDS>
+__global__ void __launch_bounds__(256) decode_fm1_lanes(DecArgs a) {
+  constexpr int WARPS = 8;
+  constexpr uint32_t L = 8 * LPB;
+  constexpr int BPR = 32 / LPB;
+  constexpr uint32_t TB = WARPS * ROUNDS * BPR;
+  extern __shared__ __align__(16) uint8_t s_span[];
   __shared__ uint32_t s_tk[2];
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint32_t s_base;
-  constexpr uint32_t TB = WARPS * BPW;
+  __shared__ uint32_t s_geo[2];  // span start (region offset), span length
+  __shared__ __align__(8) uint64_t s_bar;
   uint32_t tile, epoch;
   draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
   if (a.plan->bad) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane % LPB, grp = lane / LPB;
   const Segments sg = a.seg;
   const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, false);
   if (!dt.any) return;
@@ -645,45 +575,133 @@ __global__ void __launch_bounds__(WARPS * 32) decode_fm1_l32(DecArgs a) {
   const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
   const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
   const uint8_t* __restrict__ in = a.in;
-  const uint64_t gb = seg_block_base(sg, dt.seg, false);
+  const uint32_t* __restrict__ bp = a.blkpos + seg_block_base(sg, dt.seg, false) + dt.blk0;
 
-  const uint32_t wfirst = warp * BPW;
-  const uint32_t wn = dt.nblk > wfirst ? min((uint32_t)BPW, dt.nblk - wfirst) : 0;
-  uint32_t mypos = 0;
-  if ((uint32_t)lane < wn) mypos = __ldg(a.blkpos + gb + dt.blk0 + wfirst + lane);
-  uint32_t sc[BPW], tot = 0, wtot = 0;
+  // ---- stage the tile's stream span in shared memory ----
+  const uint32_t maxsz = a.maxsz;
+  const uint32_t rlen = (uint32_t)(R1 - R0);
+  uint32_t align = 0;
+  if (threadIdx.x == 0) {
+    uint32_t s0 = 0, s1 = 0;
+    if (dt.nblk) {
+      s0 = min(__ldg(bp), rlen);
+      s1 = (uint32_t)min((uint64_t)rlen, (uint64_t)__ldg(bp + dt.nblk - 1) + maxsz);
+      if (s1 < s0) s1 = s0;
+    }
+    s_geo[0] = s0;
+    s_geo[1] = min(s1 - s0, TB * maxsz);  // bounds a corrupt index to the buffer
+    mbar_init(&s_bar, 1);
+  }
+  __syncthreads();
+  const uint32_t span0 = s_geo[0], spanlen = s_geo[1];
+  const uint8_t* gspan = in + R0 + span0;
+  align = (uint32_t)((uintptr_t)gspan & 15);
+  {
+    const uint32_t end = align + spanlen;
+    const uint32_t i0 = (align + 15) & ~15u, i1 = end & ~15u;
+    const uint8_t* g0 = gspan - align;
+    bool bulk = i1 > i0;
+    if (threadIdx.x == 0 && bulk) {
+      mbar_arrive_expect_tx(&s_bar, i1 - i0);
+      bulk_load(s_span + i0, g0 + i0, i1 - i0, &s_bar);
+    }
+    if (bulk) {
+      for (uint32_t b = align + threadIdx.x; b < i0; b += blockDim.x) s_span[b] = __ldg(g0 + b);
+      for (uint32_t b = i1 + threadIdx.x; b < end; b += blockDim.x) s_span[b] = __ldg(g0 + b);
+    } else {
+      for (uint32_t b = align + threadIdx.x; b < end; b += blockDim.x) s_span[b] = __ldg(g0 + b);
+    }
+    bool ok = !bulk || mbar_wait_bounded(&s_bar, 0, 1u << 22);
+    if (!ok) {
+      atomicOr(a.err, kErrLookbackTimeout);
+      mbar_wait_bounded(&s_bar, 0, 1u << 22);  // let the copy land before the CTA leaves
+    }
+    __syncthreads();
+  }
+  const uint8_t* sp = s_span + align;  // span byte i at sp[i]
+
+  // ---- unpack deltas and prefix-add inside each lane ----
+  const uint32_t wfirst = (uint32_t)warp * ROUNDS * BPR;
+  uint32_t pre[ROUNDS][8];
+  uint32_t lex[ROUNDS], rbase[ROUNDS];
+  uint32_t wtot = 0;
   bool corrupt = false;
 #pragma unroll
-  for (int k = 0; k < BPW; k++) {
-    sc[k] = 0;
-    if ((uint32_t)k < wn) {
-      uint64_t b = dt.blk0 + wfirst + k;
-      uint64_t s = lo + 1 + b * 32;
-      uint32_t m = hi - s < 32 ? (uint32_t)(hi - s) : 32u;
-      uint64_t hp = R0 + __shfl_sync(0xffffffffu, mypos, k);
-      uint32_t bc = hp < R1 ? __ldg(in + hp) : 255u;
-      uint32_t d = 0;
-      if (bc > 33 || hp + block_bytes(m, bc) > R1) {
+  for (int r = 0; r < ROUNDS; r++) {
+    const uint32_t bt = wfirst + r * BPR + grp;
+    const uint64_t bs = lo + 1 + (dt.blk0 + bt) * L;
+    const uint32_t m = bt < dt.nblk ? (uint32_t)min((uint64_t)L, hi - bs) : 0u;
+    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+    uint32_t d[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) d[j] = 0;
+    if (m) {
+      const uint32_t off = __ldg(bp + bt) - span0;
+      uint32_t bc = off < spanlen ? sp[off] : 255u;
+      if (bc > 33 || off + block_bytes(m, bc) > spanlen) {
         corrupt = true;
-      } else if (bc) {
-        if ((uint32_t)lane < m) d = decode_delta(in + hp, m, bc, lane);
+        bc = 0;
       }
-      sc[k] = warp_incl_scan(d, lane);
-      wtot += __shfl_sync(0xffffffffu, sc[k], 31);
+      if (bc && ml) {
+        const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
+        const uint32_t sb = sp[off + 1 + sub];
+        uint32_t hv[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) hv[j] = 0;
+        if (B) {
+          const uint8_t* q8 = sp + off + 1 + ns + 8 * B * sub;
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            if ((uint32_t)j < ml) {
+              uint32_t h = q8[j * B];
+              if (B > 1) h |= (uint32_t)q8[j * B + 1] << 8;
+              if (B > 2) h |= (uint32_t)q8[j * B + 2] << 16;
+              if (B > 3) h |= (uint32_t)q8[j * B + 3] << 24;
+              hv[j] = h << rr;
+            }
+          }
+        }
+        if (rr) {
+          const uint8_t* rp = sp + off + 1 + ns + B * m + rr * sub;
+          const uint32_t nb = (ml * rr + 7) >> 3;
+          uint64_t acc = 0;
+#pragma unroll
+          for (uint32_t k = 0; k < 7; k++) acc = (acc << 8) | (uint64_t)(k < nb ? rp[k] : 0u);
+          // 56-bit window: field j occupies bits [56 - rr*(j+1), 56 - rr*j)
+          const uint32_t mask = (1u << rr) - 1u;
+#pragma unroll
+          for (int j = 0; j < 8; j++) hv[j] |= (uint32_t)(acc >> (56 - rr * (j + 1))) & mask;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          uint32_t v = (uint32_t)j < ml ? hv[j] : 0u;
+          d[j] = ((sb >> (7 - j)) & 1u) ? 0u - v : v;
+        }
+      }
     }
+    uint32_t run = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      run += d[j];
+      pre[r][j] = run;
+    }
+    const uint32_t incl = warp_incl_scan(run, lane);
+    lex[r] = incl - run;
+    rbase[r] = wtot;
+    wtot += __shfl_sync(0xffffffffu, incl, 31);
   }
-  if (corrupt && lane == 0) atomicOr(a.err, kErrCorrupt);
-  (void)tot;
+  if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
 
+  // ---- q chain of the segment: CTA scan + look-back from the seed ----
   uint32_t wexcl;
   const uint32_t agg = scan_warps_u32<WARPS>(s_w, wtot, warp, lane, wexcl);
-  // q chain of the segment: first tile starts from the seed
   const uint32_t first_tile = a.tiles_per_seg ? dt.seg * a.tiles_per_seg : 0;
   if (warp == 0) {
     uint32_t excl;
     if (dt.first) {
-      const uint8_t* sp = in + R0 - 4;
-      excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
+      const uint8_t* seedp = in + R0 - 4;
+      excl = (uint32_t)seedp[0] | ((uint32_t)seedp[1] << 8) | ((uint32_t)seedp[2] << 16) |
+             ((uint32_t)seedp[3] << 24);
       if (lane == 0) {
         st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
         a.y[lo] = dequant(excl, eb, ebsp);
@@ -696,16 +714,21 @@ __global__ void __launch_bounds__(WARPS * 32) decode_fm1_l32(DecArgs a) {
     if (lane == 0) s_base = excl;
   }
   __syncthreads();
-  uint32_t q0 = s_base + wexcl;
+  const uint32_t qw = s_base + wexcl;
+  const uint32_t mis = (uint32_t)(((uintptr_t)(a.y + lo + 1)) >> 2) & 3u;
 #pragma unroll
-  for (int k = 0; k < BPW; k++) {
-    if ((uint32_t)k < wn) {
-      uint64_t b = dt.blk0 + wfirst + k;
-      uint64_t s = lo + 1 + b * 32;
-      uint32_t m = hi - s < 32 ? (uint32_t)(hi - s) : 32u;
-      if ((uint32_t)lane < m) a.y[s + lane] = dequant(q0 + sc[k], eb, ebsp);
-      q0 += __shfl_sync(0xffffffffu, sc[k], 31);
-    }
+  for (int r = 0; r < ROUNDS; r++) {
+    const uint32_t bt = wfirst + r * BPR + grp;
+    if (bt >= dt.nblk) continue;
+    const uint64_t bs = lo + 1 + (dt.blk0 + bt) * L;
+    const uint32_t m = (uint32_t)min((uint64_t)L, hi - bs);
+    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+    if (!ml) continue;
+    const uint32_t q0 = qw + rbase[r] + lex[r];
+    float v[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = dequant(q0 + pre[r][j], eb, ebsp);
+    store8(a.y, bs + 8 * sub, ml, mis, v);
   }
 }
 
@@ -824,16 +847,35 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
   if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
 }
 
-constexpr int kDecWarps = 8, kDecBpw = 8;
+constexpr int kDecWarps = 8;
+constexpr int kDecRounds = 4;
+
+static int dec_lanes_per_block(uint32_t L) {
+  switch (L) {
+    case 8: return 1;
+    case 16: return 2;
+    case 32: return 4;
+    case 64: return 8;
+    case 128: return 16;
+    case 256: return 32;
+    default: return 0;
+  }
+}
 
 uint32_t decode_blocks_per_tile(uint32_t L, uint32_t& bpw) {
-  if (L == 32) {
-    bpw = kDecBpw;
-    return kDecWarps * kDecBpw;
+  int lpb = dec_lanes_per_block(L);
+  if (lpb) {
+    bpw = kDecRounds * (32 / lpb);
+    return kDecWarps * bpw;
   }
   uint32_t b = 2048u / (L < 32 ? 32u : L);
   bpw = b < 1 ? 1 : (b > 8 ? 8 : b);
   return kDecWarps * bpw;
+}
+
+size_t decode_smem_bytes(uint32_t L, uint32_t tb, bool fm2) {
+  if (fm2 || !dec_lanes_per_block(L)) return 0;
+  return (size_t)tb * max_block_bytes(L) + 64;
 }
 
 cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st) {
@@ -842,27 +884,44 @@ cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st) {
-  size_t smem = locate_smem_bytes(a.chunk, a.maxsz);
+  if (a.nchunk_ctas == 0) return cudaSuccess;
   if (a.fm2) {
-    auto k = locate_kernel<true>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<a.nlocate_ctas, kLocWarps * 32, smem, st>>>(a);
+    walk_kernel<true><<<a.nchunk_ctas, 256, 0, st>>>(a);
+    verify_kernel<true><<<a.nchunk_ctas, 256, 0, st>>>(a);
+    positions_kernel<true><<<a.nchunk_ctas, 256, 0, st>>>(a);
   } else {
-    auto k = locate_kernel<false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k<<<a.nlocate_ctas, kLocWarps * 32, smem, st>>>(a);
+    walk_kernel<false><<<a.nchunk_ctas, 256, 0, st>>>(a);
+    verify_kernel<false><<<a.nchunk_ctas, 256, 0, st>>>(a);
+    positions_kernel<false><<<a.nchunk_ctas, 256, 0, st>>>(a);
   }
+  return cudaGetLastError();
+}
+
+template <int LPB>
+static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
+  auto k = decode_fm1_lanes<LPB, kDecRounds>;
+  size_t smem = decode_smem_bytes(a.seg.L, a.tb, false);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.ntiles, 256, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {
   if (a.fm2) {
     decode_generic<kDecWarps, true><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
-  } else if (a.seg.L == 32) {
-    decode_fm1_l32<kDecWarps, kDecBpw><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
-  } else {
-    decode_generic<kDecWarps, false><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
+    return cudaGetLastError();
   }
+  switch (dec_lanes_per_block(a.seg.L)) {
+    case 1: return launch_dec_lanes<1>(a, st);
+    case 2: return launch_dec_lanes<2>(a, st);
+    case 4: return launch_dec_lanes<4>(a, st);
+    case 8: return launch_dec_lanes<8>(a, st);
+    case 16: return launch_dec_lanes<16>(a, st);
+    case 32: return launch_dec_lanes<32>(a, st);
+    default: break;
+  }
+  decode_generic<kDecWarps, false><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
   return cudaGetLastError();
 }
 
