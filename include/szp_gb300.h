@@ -198,6 +198,15 @@ double szp_gb300_kernel_ms(int slot);
  * last call (up to 1024), and their number in *launches. */
 double szp_gb300_kernel_time(int slot, int *launches);
 
+/* Bytes a decompression CTA walks before its region to find the header
+ * chain (-1: default).  Smaller values make the speculative walks fail more
+ * often and exercise the repair paths; streams decode the same. */
+void szp_gb300_set_locate_overlap(int bytes);
+
+/* Chunks whose speculative header walk the last decompression of this
+ * thread had to repair in order (statistics; -1 on error). */
+int szp_gb300_last_repairs(void);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long szp_gb300_kernel_launches(void);
 

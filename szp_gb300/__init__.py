@@ -68,9 +68,11 @@ _sig("szp_gb300_sync_status", ctypes.c_int, [_vp])
 _sig("szp_gb300_bitcount_thresholds", None, [_vp])
 _sig("szp_gb300_bitcount_probe", ctypes.c_int, [_vp, _vp, _sz, _vp])
 _sig("szp_gb300_set_timing", None, [ctypes.c_int])
+_sig("szp_gb300_set_locate_overlap", None, [ctypes.c_int])
 _sig("szp_gb300_kernel_ms", ctypes.c_double, [ctypes.c_int])
 _sig("szp_gb300_kernel_time", ctypes.c_double, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)])
 _sig("szp_gb300_kernel_launches", ctypes.c_ulonglong, [])
+_sig("szp_gb300_last_repairs", ctypes.c_int, [])
 
 _libc = ctypes.CDLL(None)
 _libc.free.argtypes = [_vp]
@@ -283,6 +285,11 @@ def bitcount_thresholds():
     return thr
 
 
+def set_locate_overlap(nbytes):
+    """Bytes walked before a decompression chunk (-1 = default); for tests."""
+    _lib.szp_gb300_set_locate_overlap(int(nbytes))
+
+
 def set_timing(on):
     _lib.szp_gb300_set_timing(1 if on else 0)
 
@@ -299,6 +306,10 @@ def kernel_time(slot):
 
 
 SLOT_REL, SLOT_COMPRESS, SLOT_SETUP, SLOT_LOCATE, SLOT_DECODE = range(5)
+
+
+def last_repairs():
+    return _lib.szp_gb300_last_repairs()
 
 
 def kernel_launches():

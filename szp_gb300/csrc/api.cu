@@ -85,6 +85,7 @@ const BitcountTable& table() {
 std::mutex g_mu;
 int g_segments = 0;
 int g_timing = 0;
+int g_overlap = -1;  // locate overlap override (tests of the repair paths)
 unsigned long long g_launches = 0;
 
 int resolve_segments(int requested) {
@@ -129,7 +130,7 @@ struct DevMisc {
   uint64_t out_size;
   float eb;
   float pad;
-  uint32_t verify[2];  // verify_kernel: failures, CTAs done (reset by its last CTA)
+  uint32_t verify[4];  // [0] locate repairs of the last launch
 };
 constexpr int kRelMaxGrid = 1024;
 
@@ -393,8 +394,8 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
                              : max_block_bytes((uint32_t)j.L);
   if (maxsz > 16384) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
   const uint32_t C = locate_chunk_bytes(maxsz);
-  const uint64_t maxchunks = (j.len + C - 1) / C + (uint64_t)j.T + 1;
-  const uint64_t nchunk_ctas = (maxchunks + 255) / 256;
+  const uint32_t SC = locate_super_bytes(maxsz);
+  const uint64_t nlocate = (j.len + SC - 1) / SC + (uint64_t)j.T + 1;
   uint32_t bpw = 1;
   uint32_t tb = decode_blocks_per_tile((uint32_t)j.L, bpw);
   uint64_t per_seg, ntiles;
@@ -403,10 +404,10 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   if (sg.n) {
     nblk_total = (uint64_t)(sg.T - 1) * (sg.tsz ? seg_blocks_host(sg, 0, fm2) : 0) + seg_blocks_host(sg, sg.T - 1, fm2);
   }
-  if (ntiles >= (1ull << 31) || maxchunks >= (1ull << 31)) return fail(SZP_GB300_EINVAL, "input too large");
-  const uint64_t nstatus = ntiles > nchunk_ctas ? ntiles : nchunk_ctas;
+  if (ntiles >= (1ull << 31) || nlocate >= (1ull << 31)) return fail(SZP_GB300_EINVAL, "input too large");
+  const uint64_t nstatus = ntiles > nlocate ? ntiles : nlocate;
   CU(w.status.ensure(nstatus * sizeof(uint64_t)));
-  CU(w.walks.ensure(maxchunks * (2 * sizeof(uint4) + sizeof(uint32_t))));
+  CU(w.walks.ensure(nlocate * sizeof(uint2)));
   CU(w.blkpos.ensure((nblk_total + 1) * sizeof(uint32_t)));
   const size_t plan_bytes = 64 + 4ull * (j.T + 1) + 16ull * j.T + 64;
   CU(w.plan.ensure(plan_bytes));
@@ -426,13 +427,11 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.reg1 = a.reg0 + j.T;
   a.chunk_base = reinterpret_cast<uint32_t*>(a.reg1 + j.T);
   a.chunk = C;
-  a.overlap = locate_overlap_bytes(maxsz);
+  a.super_chunk = SC;
+  a.overlap = g_overlap >= 0 ? (uint32_t)g_overlap : locate_overlap_bytes(maxsz);
   a.maxsz = maxsz;
-  a.walks = w.walks.as<uint4>();
-  a.final_walks = a.walks + maxchunks;
-  a.fails = reinterpret_cast<uint32_t*>(a.final_walks + maxchunks);
+  a.aux = w.walks.as<uint2>();
   a.counters = dm->verify;
-  a.max_chunks = (uint32_t)maxchunks;
   a.status = w.status.as<uint64_t>();
   a.ls = &dm->ls;
   a.err = &dm->err;
@@ -443,8 +442,11 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.tiles_per_seg = (uint32_t)per_seg;
   a.tb = tb;
   a.bpw = bpw;
-  a.nchunk_ctas = (uint32_t)nchunk_ctas;
-  if (decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) return fail(SZP_GB300_EINVAL, "blockSize too large");
+  a.nlocate_ctas = (uint32_t)nlocate;
+  if (decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024 ||
+      locate_smem_bytes(SC, a.overlap, maxsz) > 200 * 1024)
+    return fail(SZP_GB300_EINVAL, "blockSize too large");
+  CU(cudaMemsetAsync(dm->verify, 0, sizeof(uint32_t), st));
 
   w.mark(kSlotSetup, 0, st);
   CU(launch_dec_setup(a, st));
@@ -455,7 +457,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   w.mark(kSlotDecode, 0, st);
   CU(launch_decode(a, st));
   w.mark(kSlotDecode, 1, st);
-  count_launches(5);
+  count_launches(3);
   return SZP_GB300_OK;
 }
 
@@ -854,6 +856,8 @@ int szp_gb300_bitcount_probe(const uint32_t* d_max, uint8_t* d_bc, size_t n, voi
 
 void szp_gb300_set_timing(int enable) { g_timing = enable ? 1 : 0; }
 
+void szp_gb300_set_locate_overlap(int bytes) { g_overlap = bytes; }
+
 double szp_gb300_kernel_ms(int slot) {
   Workspace* w;
   if (get_ws(&w) || slot < 0 || slot >= kNumSlots || w->ev_last[slot] < 0) return -1.0;
@@ -880,6 +884,14 @@ double szp_gb300_kernel_time(int slot, int* launches) {
   w->ev_pending[slot] = 0;
   if (launches) *launches = n;
   return total;
+}
+
+int szp_gb300_last_repairs(void) {
+  Workspace* w;
+  if (get_ws(&w)) return -1;
+  uint32_t v = 0;
+  if (cudaMemcpy(&v, &w->dm()->verify[0], 4, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return (int)v;
 }
 
 unsigned long long szp_gb300_kernel_launches(void) {

@@ -249,6 +249,7 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint64_t s_base;
   __shared__ uint32_t s_thr[36];
+  __shared__ uint64_t s_red[2 * WARPS + 2];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane % LPB, grp = lane / LPB;
@@ -329,16 +330,16 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
   uint32_t wexcl;
   const uint32_t agg = scan_warps<WARPS>(s_w, wbytes, warp, lane, wexcl, seed ? 4u : 0u);
 
-  if (warp == 0) {
+  {
     uint64_t excl = 0;
     if (tile == 0) {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
     } else {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
-      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      excl = lookback_sum_cta(a.status, tile, 0, epoch, a.err, s_red);
+      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
-    if (lane == 0) s_base = excl;
+    if (threadIdx.x == 0) s_base = excl;
   }
   __syncthreads();
   const uint64_t gpos = 4 + 8ull * sg.T + s_base;  // absolute stream position of the tile
@@ -357,7 +358,7 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
     int32_t sq = quantize(__ldg(a.x + lo), inv, f2);
     s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
   }
-  const uint32_t front = (seed ? 4u : 0u) + wexcl;
+  const uint32_t front = wexcl;  // includes the 4 seed bytes of a segment's first tile
 #pragma unroll
   for (int r = 0; r < ROUNDS; r++) {
     const uint32_t bt = wfirst + r * BPR + grp;

@@ -6,22 +6,22 @@
 //
 //  1. dec_setup   one CTA reads eb and the T segment offsets, validates them and
 //                 cuts every segment's block region into fixed chunks.
-//  2. walk        one thread per chunk walks the chain of block headers.  A
-//                 chunk other than a segment's first does not know where its
-//                 first header is, so it starts `overlap` bytes early at the
-//                 first position whose chain stays valid: chains started on
-//                 payload bytes die within a step or two (a header byte must be
-//                 <= 33) or land on a true header and from then on follow the
-//                 true chain.  The chunk records its first header, its exit
-//                 (first header past it) and its header count.
-//  3. verify      chunk c is right when its first header equals chunk c-1's
-//                 exit (induction from each segment's first chunk, which starts
-//                 exactly).  Checks are independent; the last CTA re-walks, in
-//                 order, the rare chunks that fail, from their true entries.
-//  4. positions   a decoupled look-back over header counts gives every chunk
-//                 its first block index; each chunk re-walks and writes the
-//                 header offset of each of its blocks.
-//  5. decode      per tile of blocks: the tile's stream span is staged in shared
+//  2. locate      one CTA per super-chunk (threads x chunk bytes) of a segment:
+//                 the bytes (plus an overlap before them) are staged in shared
+//                 memory by a bulk copy and every thread walks the chain of
+//                 block headers through its chunk.  Only a segment's first
+//                 chunk knows where its first header is; the others start early
+//                 (in the overlap) at the first position whose chain stays
+//                 valid: chains started on payload bytes die within a step or
+//                 two (a header byte must be <= 33) or land on a true header and
+//                 follow the true chain from then on.  A chunk is right when its
+//                 first header is its predecessor's exit; wrong chunks (rare)
+//                 are re-walked in order.  Across CTAs a decoupled look-back
+//                 sums header counts and checks the same chain property on the
+//                 (entry, exit) pairs the predecessors published; a CTA whose
+//                 entry proves wrong re-walks from the true one.  Each chunk then
+//                 writes the header offset of each of its blocks.
+//  3. decode      per tile of blocks: the tile's stream span is staged in shared
 //                 memory by a bulk copy; LPB lanes per block unpack 8 elements
 //                 each (sign byte, byte planes, remainder bits are byte-aligned
 //                 per 8 elements), prefix-add (fastmode1: warp/CTA scans and a
@@ -48,13 +48,22 @@ __host__ __device__ __forceinline__ uint32_t max_walk_block(uint32_t L, bool fm2
   return fm2 ? (L == 1 ? 5u : 4 + block_bytes(L - 1, kMaxBitCount)) : block_bytes(L, kMaxBitCount);
 }
 
+constexpr int kLocThreads = 128;
+
 uint32_t locate_chunk_bytes(uint32_t maxsz) {
-  uint32_t c = 1024;
+  uint32_t c = 512;
   while (c < 2 * maxsz) c *= 2;
   return c;
 }
-
-uint32_t locate_overlap_bytes(uint32_t maxsz) { return maxsz < 128 ? 256u : 2 * maxsz; }
+uint32_t locate_super_bytes(uint32_t maxsz) { return locate_chunk_bytes(maxsz) * kLocThreads; }
+uint32_t locate_overlap_bytes(uint32_t maxsz) {
+  uint32_t w = 2048;
+  while (w < 8 * maxsz) w *= 2;
+  return w;
+}
+size_t locate_smem_bytes(uint32_t super_chunk, uint32_t overlap, uint32_t maxsz) {
+  return (size_t)overlap + super_chunk + maxsz + 64;
+}
 
 __device__ __forceinline__ uint64_t load_u64le(const uint8_t* p) {
   uint64_t v = 0;
@@ -117,7 +126,7 @@ __global__ void dec_setup_kernel(DecArgs a) {
             r1 = end < bound ? end : bound;
             if (nblk > 0 && r1 <= r0) bad = true;
             if (r1 - r0 >= (1ull << 32)) bad = true;  // block offsets are 32-bit
-            nch = (uint32_t)((r1 - r0 + a.chunk - 1) / a.chunk);
+            nch = (uint32_t)((r1 - r0 + a.super_chunk - 1) / a.super_chunk);
           }
         }
       }
@@ -158,10 +167,11 @@ __device__ __forceinline__ uint64_t seg_blocks(const Segments& sg, uint32_t t, b
 }
 
 // ---------------------------------------------------------------------------
-// 2-4. locate block headers
+// 2. locate block headers
 // ---------------------------------------------------------------------------
+constexpr uint64_t kFlagRepair = 3;  // status: the CTA is re-walking; not ready
 
-// Segment of chunk c: largest t with chunk_base[t] <= c.
+// CTA (super-chunk) of ticket c: largest t with chunk_base[t] <= c.
 __device__ __forceinline__ uint32_t chunk_segment(const uint32_t* __restrict__ cb, uint32_t T, uint32_t c) {
   uint32_t lo_t = 0, hi_t = T - 1;
   while (lo_t < hi_t) {
@@ -171,268 +181,350 @@ __device__ __forceinline__ uint32_t chunk_segment(const uint32_t* __restrict__ c
   return lo_t;
 }
 
-// Byte size of the block whose first byte is at region offset p, or 0 when
-// its bit-count byte is invalid or lies past the region (length rlen).
-__device__ __forceinline__ uint32_t step_size(const uint8_t* __restrict__ base, uint32_t p, uint32_t rlen,
-                                              uint32_t L, bool fm2) {
-  uint32_t hp = fm2 ? p + 4 : p;
-  if (hp >= rlen) return 0;
-  return full_block_size(__ldg(base + hp), L, fm2);
-}
-
-// Walks from p through [.., cE): returns the header count, sets *exit to the
-// first header position >= cE (kPosEnd when it is past the region) or
-// kPosDead.
-__device__ __forceinline__ uint32_t walk_from(const uint8_t* __restrict__ base, uint32_t p, uint32_t cE,
-                                              uint32_t rlen, uint32_t L, bool fm2, uint32_t* exit) {
-  uint32_t k = 0;
-  while (p < cE) {
-    uint32_t sz = step_size(base, p, rlen, L, fm2);
-    if (!sz) {
-      *exit = kPosDead;
-      return k;
-    }
-    k++;
-    p += sz;
+// A header chain walked in the shared-memory copy of a segment's region:
+// region offset p is at sb[p - base0]; bytes exist below `avail`.
+struct SmemChain {
+  const uint8_t* sb;
+  uint32_t base0, avail, rlen, L;
+  bool fm2;
+  // block size at p, 0 when its bit-count byte is invalid or not staged
+  __device__ __forceinline__ uint32_t step(uint32_t p) const {
+    uint32_t hp = fm2 ? p + 4 : p;
+    if (hp >= avail) return 0;
+    return full_block_size(sb[hp - base0], L, fm2);
   }
-  *exit = p >= rlen ? kPosEnd : p;
-  return k;
-}
-
-struct ChunkGeom {
-  uint32_t t, ci, cS, cE, rlen;
-  const uint8_t* base;
+  // walk from p to cE: header count, exit (kPosEnd past the region, kPosDead)
+  __device__ __forceinline__ uint32_t walk(uint32_t p, uint32_t cE, uint32_t* exit) const {
+    uint32_t k = 0;
+    while (p < cE) {
+      uint32_t sz = step(p);
+      if (!sz) {
+        *exit = kPosDead;
+        return k;
+      }
+      k++;
+      p += sz;
+    }
+    *exit = p >= rlen ? kPosEnd : p;
+    return k;
+  }
 };
 
-__device__ __forceinline__ ChunkGeom chunk_geom(const DecArgs& a, uint32_t c) {
-  ChunkGeom g;
-  g.t = chunk_segment(a.chunk_base, a.seg.T, c);
-  g.ci = c - a.chunk_base[g.t];
-  const uint64_t R0 = a.reg0[g.t], R1 = a.reg1[g.t];
-  g.rlen = (uint32_t)(R1 - R0);
-  g.cS = g.ci * a.chunk;
-  g.cE = min(g.cS + a.chunk, g.rlen);
-  g.base = a.in + R0;
-  return g;
-}
-
-// 2. speculative walk of every chunk
-template <bool FM2>
-__global__ void __launch_bounds__(256) walk_kernel(DecArgs a) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a.plan->bad || c >= a.chunk_base[a.seg.T]) return;
-  const ChunkGeom g = chunk_geom(a, c);
-  const uint32_t L = a.seg.L;
-  uint32_t h, x, k;
-  if (g.ci == 0) {
-    h = 0;  // a segment's block region starts with a header
-    k = walk_from(g.base, 0, g.cE, g.rlen, L, FM2, &x);
-  } else {
-    // find a chain that survives from the overlap window through the chunk
-    const uint32_t w0 = g.cS > a.overlap ? g.cS - a.overlap : 0;
-    uint32_t anchor = w0, budget = 8 * (a.chunk + a.overlap);
-    h = kPosDead;
-    x = kPosDead;
-    k = 0;
-    while (anchor < g.cE && budget) {
-      uint32_t p = anchor;
-      bool alive = true;
-      while (p < g.cS && budget) {
-        budget--;
-        uint32_t sz = step_size(g.base, p, g.rlen, L, FM2);
-        if (!sz) {
-          alive = false;
-          break;
-        }
-        p += sz;
-      }
-      if (!alive) {
-        anchor++;
-        continue;
-      }
-      uint32_t ex;
-      uint32_t kk = walk_from(g.base, p, g.cE, g.rlen, L, FM2, &ex);
-      budget = budget > kk ? budget - kk : 0;
-      if (ex == kPosDead) {
-        anchor = anchor < g.cS ? anchor + 1 : p + 1;  // a false chain: try the next start
-        continue;
-      }
-      h = p >= g.rlen ? kPosEnd : p;
-      x = ex;
-      k = kk;
-      break;
-    }
-  }
-  a.walks[c] = make_uint4(h, x, k, 0);
-}
-
-__device__ __forceinline__ uint4 ld_volatile_u4(const uint4* p) {
-  uint4 v;
-  asm volatile("ld.volatile.global.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p)
-               : "memory");
+__device__ __forceinline__ uint2 ld_volatile_u2(const uint2* p) {
+  uint2 v;
+  asm volatile("ld.volatile.global.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
   return v;
 }
 
-// Walks chunk c exactly from entry e (serial repair path).
-__device__ __forceinline__ uint4 exact_walk(const DecArgs& a, const ChunkGeom& g, uint32_t e, bool fm2) {
-  if (e == kPosEnd || e == kPosDead) return make_uint4(e, e, 0, 0);
-  uint32_t x;
-  uint32_t k = walk_from(g.base, e, g.cE, g.rlen, a.seg.L, fm2, &x);
-  return make_uint4(e, x, k, 0);
+// Re-walks, in order, every chunk from `from` on whose first header is not
+// the exit of the chunk before it (e = exit before chunk `from`); thread-serial.
+__device__ __forceinline__ void rewalk_from(const SmemChain& ch, uint32_t* h, uint32_t* x, uint32_t* k,
+                                            uint32_t from, uint32_t e, uint32_t nactive, uint32_t scS,
+                                            uint32_t scE, uint32_t C) {
+  for (uint32_t i = from; i < nactive; i++) {
+    if (e == kPosEnd || e == kPosDead) {
+      h[i] = e;
+      x[i] = e;
+      k[i] = 0;
+      continue;
+    }
+    if (h[i] != e) {
+      const uint32_t cE = min(scS + (i + 1) * C, scE);
+      h[i] = e;
+      uint32_t ex;
+      k[i] = ch.walk(e, cE, &ex);
+      x[i] = ex;
+    }
+    e = x[i];
+  }
 }
 
-// 3. verification; the last CTA repairs failed chunks in order.
 template <bool FM2>
-__global__ void __launch_bounds__(256) verify_kernel(DecArgs a) {
-  __shared__ bool s_last;
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t nch = a.plan->bad ? 0 : a.chunk_base[a.seg.T];
-  if (c < nch) {
-    const ChunkGeom g = chunk_geom(a, c);
-    uint4 w = a.walks[c];
-    bool ok = true;
-    if (g.ci > 0) {
-      const uint32_t px = a.walks[c - 1].y;
-      if (px == kPosEnd) {
-        w = make_uint4(kPosEnd, kPosEnd, 0, 0);  // inside the segment's last block
-      } else {
-        ok = px == w.x;
-      }
+__global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
+  constexpr int NT = kLocThreads;
+  extern __shared__ __align__(16) uint8_t s_bytes[];
+  __shared__ uint32_t s_tk[2];
+  __shared__ uint32_t s_h[NT], s_x[NT], s_k[NT];
+  __shared__ uint2 s_aux[NT];
+  __shared__ uint64_t s_val[NT];
+  __shared__ uint32_t s_misc[8];
+  __shared__ __align__(8) uint64_t s_bar;
+  uint32_t tile, epoch;
+  draw_ticket(a.ls, a.nlocate_ctas, tile, epoch, s_tk);
+  const uint32_t nct = a.plan->bad ? 0 : a.chunk_base[a.seg.T];
+  if (tile >= nct) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const Segments& sg = a.seg;
+  const uint32_t t = chunk_segment(a.chunk_base, sg.T, tile);
+  const uint32_t first = a.chunk_base[t];
+  const uint32_t j = tile - first;
+  const uint64_t R0 = a.reg0[t];
+  const uint32_t rlen = (uint32_t)(a.reg1[t] - R0);
+  const uint32_t C = a.chunk, SC = a.super_chunk, W0 = a.overlap;
+  const uint32_t scS = j * SC, scE = min(scS + SC, rlen);
+
+  // ---- stage [scS - W0, scE + maxsz) of the region ----
+  const uint32_t st0 = scS > W0 ? scS - W0 : 0u;
+  const uint32_t st1 = (uint32_t)min((uint64_t)rlen, (uint64_t)scE + a.maxsz + 8);
+  const uint8_t* g = a.in + R0 + st0;
+  const uint32_t align = (uint32_t)((uintptr_t)g & 15);
+  {
+    if (tid == 0) mbar_init(&s_bar, 1);
+    __syncthreads();
+    const uint32_t end = align + (st1 - st0);
+    const uint32_t i0 = (align + 15) & ~15u, i1 = end & ~15u;
+    const uint8_t* g0 = g - align;
+    const bool bulk = i1 > i0;
+    if (tid == 0 && bulk) {
+      mbar_arrive_expect_tx(&s_bar, i1 - i0);
+      bulk_load(s_bytes + i0, g0 + i0, i1 - i0, &s_bar);
     }
-    a.final_walks[c] = w;
-    if (!ok) {
-      uint32_t i = atomicAdd(&a.counters[0], 1u);
-      if (i < a.max_chunks) a.fails[i] = c;
+    if (bulk) {
+      for (uint32_t b = align + tid; b < i0; b += NT) s_bytes[b] = __ldg(g0 + b);
+      for (uint32_t b = i1 + tid; b < end; b += NT) s_bytes[b] = __ldg(g0 + b);
+    } else {
+      for (uint32_t b = align + tid; b < end; b += NT) s_bytes[b] = __ldg(g0 + b);
     }
+    if (bulk && !mbar_wait_bounded(&s_bar, 0, 1u << 22)) {
+      atomicOr(a.err, kErrLookbackTimeout);
+      mbar_wait_bounded(&s_bar, 0, 1u << 22);
+    }
+    __syncthreads();
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(&a.counters[1], 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!s_last || threadIdx.x != 0) return;
-  __threadfence();
-  const uint32_t nf = min(*(volatile uint32_t*)&a.counters[0], a.max_chunks);
-  a.counters[0] = 0;
-  a.counters[1] = 0;
-  if (nf == 0) return;
-  if (nf > 2048) {
-    // many failures (garbage past the data, or adversarial input): one
-    // ordered pass over every chunk
-    for (uint32_t m = 1; m < nch; m++) {
-      const ChunkGeom g = chunk_geom(a, m);
-      if (g.ci == 0) continue;
-      const uint32_t e = ld_volatile_u4(a.final_walks + m - 1).y;
-      if (e == kPosEnd || e == kPosDead) {
-        a.final_walks[m] = make_uint4(e, e, 0, 0);
-        continue;
-      }
-      if (ld_volatile_u4(a.final_walks + m).x != e) a.final_walks[m] = exact_walk(a, g, e, FM2);
-    }
-    __threadfence();
-    return;
-  }
-  // order the failures (usually a handful)
-  uint32_t* f = a.fails;
-  for (uint32_t i = 1; i < nf; i++) {
-    uint32_t v = f[i], j = i;
-    while (j > 0 && f[j - 1] > v) {
-      f[j] = f[j - 1];
-      j--;
-    }
-    f[j] = v;
-  }
-  uint32_t done_upto = 0;  // chunks below this are final
-  for (uint32_t i = 0; i < nf; i++) {
-    uint32_t m = f[i];
-    if (m < done_upto) continue;
-    ChunkGeom g = chunk_geom(a, m);
-    const uint32_t seg_end = a.chunk_base[g.t + 1];
-    while (true) {
-      const uint32_t e = ld_volatile_u4(a.final_walks + m - 1).y;
-      if (e == kPosEnd || e == kPosDead) {
-        // past the segment's last block (or a dead chain: the block count
-        // check reports it): nothing more in this segment
-        for (uint32_t r = m; r < seg_end; r++) a.final_walks[r] = make_uint4(e, e, 0, 0);
-        done_upto = seg_end;
+  SmemChain ch;
+  ch.sb = s_bytes + align;
+  ch.base0 = st0;
+  ch.avail = st1;
+  ch.rlen = rlen;
+  ch.L = sg.L;
+  ch.fm2 = FM2;
+
+  // ---- speculative walk of each thread's chunk ----
+  const uint32_t nactive = (scE - scS + C - 1) / C;
+  const uint32_t cS = scS + tid * C, cE = min(cS + C, scE);
+  uint32_t h = kPosEnd, x = kPosEnd, k = 0;
+  if ((uint32_t)tid < nactive) {
+    if (j == 0 && tid == 0) {
+      h = 0;  // a segment's block region starts with a header
+      k = ch.walk(0, cE, &x);
+    } else {
+      // the first chunk of a CTA is checked across CTAs (costly to repair), the
+      // others against their neighbour here (cheap): shorter overlap for those
+      const uint32_t W = tid == 0 ? W0 : min(W0, max(512u, 4 * a.maxsz));
+      const uint32_t w0 = cS > st0 + W ? cS - W : st0;
+      uint32_t anchor = w0, budget = 4 * (W + C);
+      h = kPosDead;
+      x = kPosDead;
+      while (anchor < cE && budget) {
+        uint32_t p = anchor;
+        bool alive = true;
+        while (p < cS && budget) {
+          budget--;
+          uint32_t sz = ch.step(p);
+          if (!sz) {
+            alive = false;
+            break;
+          }
+          p += sz;
+        }
+        if (!alive) {
+          anchor++;
+          continue;
+        }
+        uint32_t ex;
+        uint32_t kk = ch.walk(p, cE, &ex);
+        budget = budget > kk ? budget - kk : 0u;
+        if (ex == kPosDead) {
+          anchor++;
+          continue;
+        }
+        h = p >= rlen ? kPosEnd : p;
+        x = ex;
+        k = kk;
         break;
       }
-      uint4 w = exact_walk(a, g, e, FM2);
-      a.final_walks[m] = w;
-      done_upto = m + 1;
-      if (m + 1 >= seg_end) break;
-      uint4 nx = ld_volatile_u4(a.final_walks + m + 1);
-      if (w.y != kPosEnd && w.y != kPosDead && nx.x == w.y) break;  // the successor verifies
-      m++;
-      g = chunk_geom(a, m);
     }
   }
-  __threadfence();
-}
+  s_h[tid] = h;
+  s_x[tid] = x;
+  s_k[tid] = k;
+  __syncthreads();
+  // ---- chunk boundaries inside the CTA ----
+  bool bad = false;
+  if (tid > 0 && (uint32_t)tid < nactive) {
+    const uint32_t px = s_x[tid - 1];
+    bad = (px == kPosEnd) ? (h != kPosEnd || k != 0) : (px != h);
+  }
+  const uint32_t repairs = __syncthreads_count(bad);
+  if (repairs) {
+    if (tid == 0) {
+      rewalk_from(ch, s_h, s_x, s_k, 1, s_x[0], nactive, scS, scE, C);
+      atomicAdd(&a.counters[0], repairs);
+    }
+    __syncthreads();
+  }
 
-// 4. block indices (look-back over header counts) and header offsets.
-template <bool FM2>
-__global__ void __launch_bounds__(256) positions_kernel(DecArgs a) {
-  __shared__ uint32_t s_tk[2];
-  __shared__ uint32_t s_w[9];
-  __shared__ uint64_t s_base;
-  uint32_t tile, epoch;
-  draw_ticket(a.ls, a.nchunk_ctas, tile, epoch, s_tk);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t c = tile * 256 + threadIdx.x;
-  const uint32_t nch = a.plan->bad ? 0 : a.chunk_base[a.seg.T];
-  uint4 w = make_uint4(kPosEnd, kPosEnd, 0, 0);
-  if (c < nch) w = a.final_walks[c];
-  const uint32_t k = w.z;
-  // CTA scan of counts
-  uint32_t incl = k;
+  // ---- look-back over header counts, verifying entries ----
+  uint32_t K = 0;
+  for (int i = 0; i < NT; i++) K += s_k[i];  // shared reads, same in every thread
+  uint32_t h0 = s_h[0], xl = s_x[nactive - 1];
+  uint64_t prefix = 0;
+  if (j == 0) {
+    if (tid == 0) {
+      a.aux[tile] = make_uint2(h0, xl);
+      __threadfence();
+      st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, K));
+    }
+  } else {
+    if (tid == 0) {
+      a.aux[tile] = make_uint2(h0, xl);
+      __threadfence();
+      st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, K));
+    }
+    uint32_t spins = 0;
+    while (true) {
+      // window: thread i reads tile-1-i (seqlock read of status + aux)
+      int64_t base = (int64_t)tile - 1;
+      uint64_t acc = 0;
+      uint32_t need_x = h0;       // exit the next-older tile must have
+      uint32_t pred_x = kPosDead;  // exit of the tile just before this one
+      int verdict = 0;             // 1 done, 2 retry, 3 repair self
+      bool self_ok = true;
+      while (true) {
+        const int64_t idx = base - tid;
+        bool inr = idx >= (int64_t)first;
+        uint64_t s1 = 0, s2 = 0;
+        uint2 ax = make_uint2(0, 0);
+        bool ready = true, incl = false;
+        if (inr) {
+          s1 = ld_volatile_u64(a.status + idx);
+          __threadfence();
+          ax = ld_volatile_u2(a.aux + idx);
+          __threadfence();
+          s2 = ld_volatile_u64(a.status + idx);
+          const uint64_t f = status_flag(s1);
+          ready = s1 == s2 && status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
+          incl = ready && f == kFlagInclusive;
+        }
+        s_aux[tid] = ax;
+        s_val[tid] = inr ? status_value(s1) : 0;
+        const int nearest = __syncthreads_or(incl) ? 1 : 0;
+        // nearest inclusive and readiness of everything before it
+        uint32_t jstar = NT;
+        if (nearest) {
+          const uint32_t bi = __ballot_sync(0xffffffffu, incl);
+          if (lane == 0) s_misc[warp] = bi ? (uint32_t)(warp * 32 + __ffs(bi) - 1) : (uint32_t)NT;
+          __syncthreads();
+          for (int w = 0; w < NT / 32; w++) jstar = min(jstar, s_misc[w]);
+          __syncthreads();
+        }
+        const bool relevant = inr && (uint32_t)tid <= jstar;
+        if (__syncthreads_or(relevant && !ready)) {
+          verdict = 2;
+          break;
+        }
+        // chain checks: the entry of thread i's tile must be the exit of the
+        // next older tile (thread i+1); the inclusive tile is already verified
+        bool broken = false;
+        if (relevant && (uint32_t)tid < jstar && tid + 1 < NT && idx - 1 >= (int64_t)first) {
+          const uint32_t e = ax.x, ox = s_aux[tid + 1].y;
+          broken = (ox == kPosEnd) ? (e != kPosEnd) : (e != ox);
+        }
+        if (__syncthreads_or(broken)) {
+          verdict = 2;  // an older tile's entry is wrong: it will repair itself
+          break;
+        }
+        if (base == (int64_t)tile - 1) {
+          // our own entry against the nearest predecessor's exit
+          const uint32_t px = s_aux[0].y;
+          self_ok = (px == kPosEnd) ? (h0 == kPosEnd && K == 0) : (px == h0);
+          pred_x = px;
+        } else {
+          // window boundary: the nearest of this window must exit where the
+          // farthest of the previous window entered
+          const uint32_t px = s_aux[0].y;
+          if (!((px == kPosEnd) ? (need_x == kPosEnd) : (px == need_x))) {
+            verdict = 2;
+            break;
+          }
+        }
+        // sum the counts of the relevant window entries
+        uint64_t v = relevant ? s_val[tid] : 0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) s_misc[4 + warp] = (uint32_t)v;  // per-warp partials (< 2^32)
+        __syncthreads();
+        uint64_t tot = 0;
+        for (int w = 0; w < NT / 32; w++) tot += s_misc[4 + w];
+        const uint32_t far_h = s_aux[NT - 1].x;
+        __syncthreads();
+        acc += tot;
+        if (jstar < (uint32_t)NT || base - NT < (int64_t)first) {
+          verdict = self_ok ? 1 : 3;
+          break;
+        }
+        need_x = far_h;
+        base -= NT;
+      }
+      if (verdict == 2) {
+        if (++spins > kSpinLimit) {
+          if (tid == 0) atomicOr(a.err, kErrLookbackTimeout);
+          break;
+        }
+        continue;
+      }
+      if (verdict == 3) {
+        // our speculative entry was wrong: re-walk from the verified exit
+        if (tid == 0) {
+          st_release_u64(a.status + tile, make_status(epoch, kFlagRepair, 0));
+          __threadfence();
+          s_h[0] = pred_x == kPosDead ? kPosEnd : kPosDead;  // differs from the entry: chunk 0 is re-walked
+          rewalk_from(ch, s_h, s_x, s_k, 0, pred_x, nactive, scS, scE, C);
+          atomicAdd(&a.counters[0], 1u);
+        }
+        __syncthreads();
+        K = 0;
+        for (int i = 0; i < NT; i++) K += s_k[i];
+        h0 = s_h[0];
+        xl = s_x[nactive - 1];
+        if (tid == 0) {
+          a.aux[tile] = make_uint2(h0, xl);
+          __threadfence();
+        }
+      }
+      prefix = acc;
+      if (tid == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, prefix + K));
+      break;
+    }
+  }
+  // ---- header offsets of every block of every chunk ----
+  uint32_t kx = s_k[tid];
+  uint32_t incl_k = kx;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl_k, o);
+    if (lane >= o) incl_k += y;
   }
-  if (lane == 31) s_w[warp] = incl;
+  if (lane == 31) s_misc[warp] = incl_k;
   __syncthreads();
-  if (warp == 0) {
-    uint32_t v = lane < 8 ? s_w[lane] : 0u;
-    uint32_t vi = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, vi, o);
-      if (lane >= o) vi += y;
-    }
-    if (lane < 8) s_w[lane] = vi - v;
-    uint32_t agg = __shfl_sync(0xffffffffu, vi, 7);
-    uint64_t excl = 0;
-    if (tile == 0) {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
-    } else {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
-      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
-    }
-    if (lane == 0) s_base = excl;
-  }
-  __syncthreads();
-  if (c >= nch) return;
-  const uint64_t g0 = s_base + s_w[warp] + (incl - k);  // global index of the chunk's first header
-  const ChunkGeom g = chunk_geom(a, c);
-  const Segments& sg = a.seg;
-  const uint64_t gb = seg_block_base(sg, g.t, FM2), nb = seg_blocks(sg, g.t, FM2);
-  if (k && w.x < g.rlen) {
-    uint32_t p = w.x;
-    for (uint32_t i = 0; i < k; i++) {
-      uint64_t gi = g0 + i;
-      if (gi >= gb && gi < gb + nb) a.blkpos[gi] = p;
-      uint32_t sz = step_size(g.base, p, g.rlen, sg.L, FM2);
+  uint32_t wex = 0;
+  for (int w = 0; w < warp; w++) wex += s_misc[w];
+  const uint64_t g0 = prefix + wex + (incl_k - kx);
+  const uint64_t gb = seg_block_base(sg, t, FM2), nb = seg_blocks(sg, t, FM2);
+  uint32_t p = s_h[tid];
+  if (kx && p < rlen) {
+    for (uint32_t i = 0; i < kx; i++) {
+      const uint64_t gi = g0 + i;
+      if (gi < nb) a.blkpos[gb + gi] = p;
+      const uint32_t sz = ch.step(p);
       if (!sz) break;
       p += sz;
     }
   }
-  // the last chunk of a segment checks the block total
-  if (c + 1 == a.chunk_base[g.t + 1]) {
-    const uint64_t end = g0 + k;
-    const bool last_seg = g.t + 1 == sg.T;
-    if (end < gb + nb || (!last_seg && end != gb + nb)) atomicOr(a.err, kErrBlockCount);
+  // the last CTA of a segment checks the block total
+  if (tid == 0 && tile + 1 == a.chunk_base[t + 1]) {
+    const uint64_t total = prefix + K;
+    const bool last_seg = t + 1 == sg.T;
+    if (total < nb || (!last_seg && total != nb)) atomicOr(a.err, kErrBlockCount);
   }
 }
 
@@ -562,6 +654,7 @@ __global__ void __launch_bounds__(256) decode_fm1_lanes(DecArgs a) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_geo[2];  // span start (region offset), span length
   __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint64_t s_red[2 * WARPS + 2];
   uint32_t tile, epoch;
   draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
   if (a.plan->bad) return;
@@ -696,22 +789,23 @@ __global__ void __launch_bounds__(256) decode_fm1_lanes(DecArgs a) {
   uint32_t wexcl;
   const uint32_t agg = scan_warps_u32<WARPS>(s_w, wtot, warp, lane, wexcl);
   const uint32_t first_tile = a.tiles_per_seg ? dt.seg * a.tiles_per_seg : 0;
-  if (warp == 0) {
+  {
     uint32_t excl;
     if (dt.first) {
       const uint8_t* seedp = in + R0 - 4;
       excl = (uint32_t)seedp[0] | ((uint32_t)seedp[1] << 8) | ((uint32_t)seedp[2] << 16) |
              ((uint32_t)seedp[3] << 24);
-      if (lane == 0) {
+      if (threadIdx.x == 0) {
         st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
         a.y[lo] = dequant(excl, eb, ebsp);
       }
     } else {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
-      excl = (uint32_t)lookback_sum(a.status, tile, first_tile, epoch, a.err);
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
+      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      excl = (uint32_t)lookback_sum_cta(a.status, tile, first_tile, epoch, a.err, s_red);
+      if (threadIdx.x == 0)
+        st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
     }
-    if (lane == 0) s_base = excl;
+    if (threadIdx.x == 0) s_base = excl;
   }
   __syncthreads();
   const uint32_t qw = s_base + wexcl;
@@ -884,15 +978,18 @@ cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st) {
-  if (a.nchunk_ctas == 0) return cudaSuccess;
+  if (a.nlocate_ctas == 0) return cudaSuccess;
+  const size_t smem = locate_smem_bytes(a.super_chunk, a.overlap, a.maxsz);
   if (a.fm2) {
-    walk_kernel<true><<<a.nchunk_ctas, 256, 0, st>>>(a);
-    verify_kernel<true><<<a.nchunk_ctas, 256, 0, st>>>(a);
-    positions_kernel<true><<<a.nchunk_ctas, 256, 0, st>>>(a);
+    auto k = locate_kernel<true>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<a.nlocate_ctas, kLocThreads, smem, st>>>(a);
   } else {
-    walk_kernel<false><<<a.nchunk_ctas, 256, 0, st>>>(a);
-    verify_kernel<false><<<a.nchunk_ctas, 256, 0, st>>>(a);
-    positions_kernel<false><<<a.nchunk_ctas, 256, 0, st>>>(a);
+    auto k = locate_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<a.nlocate_ctas, kLocThreads, smem, st>>>(a);
   }
   return cudaGetLastError();
 }

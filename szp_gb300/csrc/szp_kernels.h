@@ -54,14 +54,12 @@ struct DecArgs {
   uint32_t* chunk_base;  // [T+1]
   uint64_t* reg0;        // [T] absolute start of each segment's block region
   uint64_t* reg1;        // [T] absolute end of it (exclusive)
-  uint32_t chunk;        // bytes per locate chunk
-  uint32_t overlap;      // bytes walked before a chunk to synchronise
+  uint32_t chunk;        // bytes per locate thread
+  uint32_t super_chunk;  // bytes per locate CTA (chunk * threads)
+  uint32_t overlap;      // bytes walked before a CTA's region to find the header chain
   uint32_t maxsz;        // largest block (including a fastmode2 seed)
-  uint4* walks;          // per chunk: first header, exit, header count (region-relative)
-  uint4* final_walks;    // the same after verification and repair
-  uint32_t* fails;       // chunks whose speculative walk did not verify
-  uint32_t* counters;    // [0] fails, [1] CTAs done
-  uint32_t max_chunks;   // capacity of walks / fails
+  uint2* aux;            // per locate CTA: (entry, exit) of its header chain
+  uint32_t* counters;    // [0] repairs of the last launch
   uint64_t* status;      // look-back words
   LaunchState* ls;
   uint32_t* err;
@@ -72,7 +70,7 @@ struct DecArgs {
   uint32_t tiles_per_seg;
   uint32_t tb;
   uint32_t bpw;
-  uint32_t nchunk_ctas;  // CTAs of the per-chunk kernels (256 chunks each)
+  uint32_t nlocate_ctas; // CTAs of the locate kernel (upper bound)
 };
 
 uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw);
@@ -85,7 +83,9 @@ cudaError_t launch_bitcount_probe(const uint32_t* in, uint8_t* out, uint64_t n, 
 // decompression
 uint32_t decode_blocks_per_tile(uint32_t L, uint32_t& bpw);
 uint32_t locate_chunk_bytes(uint32_t maxsz);
+uint32_t locate_super_bytes(uint32_t maxsz);
 uint32_t locate_overlap_bytes(uint32_t maxsz);
+size_t locate_smem_bytes(uint32_t super_chunk, uint32_t overlap, uint32_t maxsz);
 size_t decode_smem_bytes(uint32_t L, uint32_t tb, bool fm2);
 cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st);

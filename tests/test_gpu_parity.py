@@ -222,3 +222,22 @@ def test_bad_arguments(szp):
         szp.szp_compress(x, szp.ABS, 1e-3, 0.0, 32, 3)
     with pytest.raises(szp.SzpError):
         szp.szp_compress(x, szp.ABS, 1e-3, 0.0, 32, 1, data_type=szp.SZ_DOUBLE)
+
+
+@pytest.mark.parametrize("overlap", [0, 3, 40])
+def test_locate_repair_path(szp, port, overlap):
+    """Short overlaps make speculative chunk walks miss the header chain; the
+    in-order repair must still recover every block."""
+    from szp_gb300.workloads import walk, laplace_zero_patches
+    rng = np.random.default_rng(81 + overlap)
+    szp.set_locate_overlap(overlap)
+    try:
+        for T, n, L in ((1, 400_000, 32), (5, 1_000_000, 32), (3, 300_000, 64), (2, 200_000, 8)):
+            x = walk(n, rng) if T != 5 else laplace_zero_patches(1000, 1000, rng).ravel()
+            eb = float(np.float32(1e-5 * (x.max() - x.min()) + 1e-7))
+            s = port.compress(x, eb, L, T, 1)
+            szp.set_segments(T)
+            y = szp.szp_decompress(s, n, L, 1)
+            assert np.array_equal(bits(y), bits(port.decompress(s, n, L, T, 1))), (overlap, T, n, L)
+    finally:
+        szp.set_locate_overlap(-1)
