@@ -17,7 +17,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/szp_gb300.h"
+#include "szp_gb300.h"
 #include "szp_kernels.h"
 
 using namespace szp;

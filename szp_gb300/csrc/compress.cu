@@ -238,6 +238,33 @@ __device__ __forceinline__ void flush_span_bulk(uint8_t* __restrict__ gdst, uint
   }
 }
 
+// Exact path for the elements whose |x/eb| >= 2^24 (or NaN/inf); kept out
+// of line so the common path issues no FP64 instructions.
+__device__ __noinline__ void quantize8_slow(const float* xv, float inv, int32_t* q, uint32_t* flags) {
+  uint32_t f = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    float p = __fmul_rz(xv[j], inv);
+    if (!(fabsf(p) < 16777216.0f)) q[j] = quantize_slow(xv[j], inv, f);
+  }
+  *flags |= f;
+}
+
+// q = trunc(x/eb) for 8 values (see quantize()); slow lanes fixed by a
+// warp-uniform branch.
+__device__ __forceinline__ void quantize8(const float* xv, float inv, int32_t* q, uint32_t& flags) {
+  bool slow = false;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    float p = __fmul_rz(xv[j], inv);
+    q[j] = __float2int_rz(p);
+    slow |= !(fabsf(p) < 16777216.0f);
+  }
+  if (__any_sync(0xffffffffu, slow)) {
+    if (slow) quantize8_slow(xv, inv, q, &flags);
+  }
+}
+
 template <int LPB, int ROUNDS>
 __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
   constexpr int WARPS = 8;
@@ -249,7 +276,6 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint64_t s_base;
   __shared__ uint32_t s_thr[36];
-  __shared__ uint64_t s_red[2 * WARPS + 2];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane % LPB, grp = lane / LPB;
@@ -285,22 +311,33 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
     float xv[8];
     load8(a.x, bs + 8 * sub, ml, mis, n, xv);
     int32_t q[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) q[j] = quantize(xv[j], inv, flags);
+    quantize8(xv, inv, q, flags);
     int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
     if (lane == 0) prev = carry;
     carry = __shfl_sync(0xffffffffu, q[7], 31);
     uint32_t sb = 0, lmax = 0;
+    if (__all_sync(0xffffffffu, ml == 8)) {
+      // every lane holds 8 elements: no masking
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      uint32_t d = (uint32_t)q[j] - (uint32_t)prev;  // wrapping, as the compiled reference
-      prev = q[j];
-      bool valid = (uint32_t)j < ml;
-      bool neg = valid && (int32_t)d < 0;
-      uint32_t v = valid ? (neg ? 0u - d : d) : 0u;
-      sb |= (neg ? 1u : 0u) << (7 - j);
-      lmax = max(lmax, v);
-      vv[r][j] = v;
+      for (int j = 0; j < 8; j++) {
+        int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
+        prev = q[j];
+        uint32_t v = (uint32_t)abs(d);  // |INT_MIN| wraps to 2^31 like the reference's -diff
+        sb = (sb << 1) + ((uint32_t)d >> 31);  // sign bits MSB first
+        lmax = max(lmax, v);
+        vv[r][j] = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);
+        prev = q[j];
+        bool valid = (uint32_t)j < ml;
+        uint32_t v = valid ? (uint32_t)abs(d) : 0u;
+        sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
+        lmax = max(lmax, v);
+        vv[r][j] = v;
+      }
     }
 #pragma unroll
     for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
@@ -330,16 +367,16 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
   uint32_t wexcl;
   const uint32_t agg = scan_warps<WARPS>(s_w, wbytes, warp, lane, wexcl, seed ? 4u : 0u);
 
-  {
+  if (warp == 0) {
     uint64_t excl = 0;
     if (tile == 0) {
-      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
     } else {
-      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
-      excl = lookback_sum_cta(a.status, tile, 0, epoch, a.err, s_red);
-      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
-    if (threadIdx.x == 0) s_base = excl;
+    if (lane == 0) s_base = excl;
   }
   __syncthreads();
   const uint64_t gpos = 4 + 8ull * sg.T + s_base;  // absolute stream position of the tile

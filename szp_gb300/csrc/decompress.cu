@@ -50,15 +50,14 @@ __host__ __device__ __forceinline__ uint32_t max_walk_block(uint32_t L, bool fm2
 
 constexpr int kLocThreads = 128;
 
-uint32_t locate_chunk_bytes(uint32_t maxsz) {
-  uint32_t c = 512;
-  while (c < 2 * maxsz) c *= 2;
-  return c;
-}
+// A chunk may hold no header at all (a block larger than the chunk), so the
+// chunk size does not depend on the block size; the overlap that lets a
+// speculative walk synchronise spans at least 8 of the largest blocks.
+uint32_t locate_chunk_bytes(uint32_t) { return 512; }
 uint32_t locate_super_bytes(uint32_t maxsz) { return locate_chunk_bytes(maxsz) * kLocThreads; }
 uint32_t locate_overlap_bytes(uint32_t maxsz) {
   uint32_t w = 2048;
-  while (w < 8 * maxsz) w *= 2;
+  while (w < 8 * maxsz && w < 65536) w *= 2;
   return w;
 }
 size_t locate_smem_bytes(uint32_t super_chunk, uint32_t overlap, uint32_t maxsz) {
