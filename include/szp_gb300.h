@@ -172,6 +172,22 @@ int szp_gb300_decompress_dev_async(int fastMode, const unsigned char *d_bytes, s
                                    const unsigned long long *d_byteLength, size_t nbEle, int blockSize,
                                    int segments, float *d_out, void *stream);
 
+/* Fastmode1 compressor that allocates nothing; no counterpart in the
+ * reference.  For callers that cannot allocate device memory when they
+ * compress (all GPU memory handed to their own pool, or a serving loop that
+ * must not pay cudaMalloc's device-wide synchronisation): they pass device
+ * buffers d_data and d_out, and the kernels' working memory is a static
+ * device array of this library (about 136 KB per GPU that loads it, held until
+ * the process exits).  At most 16384 tiles of 256 blocks (134,217,728 floats
+ * at blockSize 32); larger inputs are rejected with SZP_GB300_EINVAL.  The
+ * first call on a device looks up the array's device address (set-up).  All
+ * calls share the array: calls that overlap on the GPU race.  Waits for the
+ * result; *outSize gets the stream size (also when it exceeds out_capacity,
+ * which returns SZP_GB300_ECAPACITY).  The stream equals szp_gb300_compress_dev's. */
+int szp_gb300_compress_dev_noalloc(const float *d_data, size_t nbEle, int errBoundMode, double absErrBound,
+                                   double relBoundRatio, int blockSize, int segments, unsigned char *d_out,
+                                   size_t out_capacity, size_t *outSize, void *stream);
+
 /* Waits for stream and returns the status of the device-side checks of the
  * calling thread's last calls (capacity, corrupt stream, timeouts). */
 int szp_gb300_sync_status(void *stream);

@@ -65,6 +65,8 @@ _sig("szp_gb300_decompress_dev", ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, cty
 _sig("szp_gb300_decompress_dev_async", ctypes.c_int, [ctypes.c_int, _vp, _sz, _vp, _sz, ctypes.c_int,
                                                       ctypes.c_int, _vp, _vp])
 _sig("szp_gb300_sync_status", ctypes.c_int, [_vp])
+_sig("szp_gb300_compress_dev_noalloc", ctypes.c_int, [_vp, _sz, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                      ctypes.c_int, ctypes.c_int, _vp, _sz, _szp, _vp])
 _sig("szp_gb300_bitcount_thresholds", None, [_vp])
 _sig("szp_gb300_bitcount_probe", ctypes.c_int, [_vp, _vp, _sz, _vp])
 _sig("szp_gb300_set_timing", None, [ctypes.c_int])
@@ -273,6 +275,19 @@ def decompress_dev_async(d_stream, capacity, d_len, n, d_out, block_size=32, seg
                                              stream or None)
     if rc != 0:
         raise SzpError(rc, "decompress_dev_async failed: %s" % last_error())
+
+
+def compress_dev_noalloc(d_data, n, d_out, capacity, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0,
+                         block_size=32, segments=0, stream=0):
+    """Allocation-free fastmode1 compressor (static device working memory);
+    returns the stream size.  For callers that cannot allocate device memory
+    while compressing."""
+    size = ctypes.c_size_t(0)
+    rc = _lib.szp_gb300_compress_dev_noalloc(d_data, n, err_bound_mode, abs_err_bound, rel_bound_ratio, block_size,
+                                             segments, d_out, capacity, ctypes.byref(size), stream or None)
+    if rc != 0:
+        raise SzpError(rc, "compress_dev_noalloc failed: %s" % last_error())
+    return size.value
 
 
 def sync_status(stream=0):

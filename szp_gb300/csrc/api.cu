@@ -596,6 +596,21 @@ int decompress_host(const uint8_t* bytes, size_t len, bool len_known, size_t n, 
 
 }  // namespace
 
+// Host helpers shared with noalloc.cu (no allocation in any of them).
+namespace szp {
+const BitcountTable& host_bitcount_table() { return table(); }
+int host_resolve_segments(int requested) { return resolve_segments(requested); }
+void host_compress_tiles(size_t n, int T, int L, uint64_t& tiles_per_seg, uint64_t& ntiles, uint32_t& tb,
+                         uint32_t& bpw) {
+  tb = compress_blocks_per_tile((uint32_t)L, bpw);
+  Segments sg = make_segments(n, T, L);
+  tile_counts(sg, false, tb, tiles_per_seg, ntiles);
+}
+int host_fail(int status, const char* msg) { return fail(status, "%s", msg); }
+void host_clear_error() { clear_error(); }
+void host_count_launches(int k) { count_launches(k); }
+}  // namespace szp
+
 // =============================================================== C ABI ====
 extern "C" {
 

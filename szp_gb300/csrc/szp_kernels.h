@@ -91,4 +91,13 @@ cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st);
 
+// host helpers (api.cu)
+const BitcountTable& host_bitcount_table();
+int host_resolve_segments(int requested);
+void host_compress_tiles(size_t n, int T, int L, uint64_t& tiles_per_seg, uint64_t& ntiles, uint32_t& tb,
+                         uint32_t& bpw);
+int host_fail(int status, const char* msg);
+void host_clear_error();
+void host_count_launches(int k);
+
 }  // namespace szp
