@@ -324,6 +324,8 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   a.tiles_per_seg = (uint32_t)per_seg;
   a.tb = tb;
   a.bpw = bpw;
+  a.nb_reg = sg.tsz ? seg_blocks_host(sg, 0, fm2) : 0;
+  a.nb_last = seg_blocks_host(sg, sg.T - 1, fm2);
   a.thr = table();
 
   int launches = 0;
@@ -605,6 +607,11 @@ void host_compress_tiles(size_t n, int T, int L, uint64_t& tiles_per_seg, uint64
   tb = compress_blocks_per_tile((uint32_t)L, bpw);
   Segments sg = make_segments(n, T, L);
   tile_counts(sg, false, tb, tiles_per_seg, ntiles);
+}
+void host_segment_blocks(size_t n, int T, int L, uint64_t& nb_reg, uint64_t& nb_last) {
+  Segments sg = make_segments(n, T, L);
+  nb_reg = sg.tsz ? seg_blocks_host(sg, 0, false) : 0;
+  nb_last = seg_blocks_host(sg, sg.T - 1, false);
 }
 int host_fail(int status, const char* msg) { return fail(status, "%s", msg); }
 void host_clear_error() { clear_error(); }

@@ -187,32 +187,6 @@ __device__ __forceinline__ uint32_t scan_warps(uint32_t* s_w, uint32_t mine, int
 // 32/LPB consecutive blocks; a 256-thread CTA a tile of 8*ROUNDS*32/LPB blocks.
 // ---------------------------------------------------------------------------
 
-// Loads x[s .. s+8) (lane-local, ml valid elements) into v[]; mis = (s mod 4)
-// of the float address, identical for every lane of the tile.
-__device__ __forceinline__ void load8(const float* __restrict__ x, uint64_t s, uint32_t ml, uint32_t mis,
-                                      uint64_t n, float v[8]) {
-  const float* p = x + s;
-  if (ml == 8 && s >= 4 && s + 12 <= n) {
-    const float4* q = reinterpret_cast<const float4*>(p - mis);
-    float4 A = __ldg(q), B = __ldg(q + 1);
-    if (mis == 0) {
-      v[0] = A.x; v[1] = A.y; v[2] = A.z; v[3] = A.w; v[4] = B.x; v[5] = B.y; v[6] = B.z; v[7] = B.w;
-    } else {
-      float4 C = __ldg(q + 2);
-      if (mis == 1) {
-        v[0] = A.y; v[1] = A.z; v[2] = A.w; v[3] = B.x; v[4] = B.y; v[5] = B.z; v[6] = B.w; v[7] = C.x;
-      } else if (mis == 2) {
-        v[0] = A.z; v[1] = A.w; v[2] = B.x; v[3] = B.y; v[4] = B.z; v[5] = B.w; v[6] = C.x; v[7] = C.y;
-      } else {
-        v[0] = A.w; v[1] = B.x; v[2] = B.y; v[3] = B.z; v[4] = B.w; v[5] = C.x; v[6] = C.y; v[7] = C.z;
-      }
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 8; j++) v[j] = (uint32_t)j < ml ? __ldg(p + j) : 0.0f;
-  }
-}
-
 // Stages a tile's bytes (shared memory s_out[align .. align+len)) to global
 // dst (dst % 16 == align): bulk copy for the 16-byte-aligned middle, byte
 // stores for the ragged ends.  Every thread of the CTA calls it.
@@ -265,109 +239,209 @@ __device__ __forceinline__ void quantize8(const float* xv, float inv, int32_t* q
   }
 }
 
-template <int LPB, int ROUNDS>
-__global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
-  constexpr int WARPS = 8;
+// Exclusive scan of n (<= 4*blockDim) values in shared memory by the whole
+// CTA (256 threads); returns the total.  s_part needs 8 words.
+__device__ __forceinline__ uint32_t cta_scan_excl(uint32_t* v, uint32_t n, uint32_t* s_part) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t i0 = threadIdx.x * per;
+  uint32_t loc[4], sum = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    loc[k] = ((uint32_t)k < per && i0 + k < n) ? v[i0 + k] : 0u;
+    sum += loc[k];
+  }
+  uint32_t incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_part[warp] = incl;
+  __syncthreads();
+  uint32_t wex = 0, tot = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+    uint32_t pw = s_part[w];
+    if (w < warp) wex += pw;
+    tot += pw;
+  }
+  uint32_t run = wex + incl - sum;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if ((uint32_t)k < per && i0 + k < n) v[i0 + k] = run;
+    run += loc[k];
+  }
+  __syncthreads();
+  return tot;
+}
+
+// Tile geometry, computed once by thread 0.
+struct TileGeo {
+  uint64_t lo, hi;  // segment element range
+  uint64_t e0;      // first element of the tile's first block
+  uint32_t seg, nblk, nel;  // blocks, elements of those blocks
+  uint32_t first;   // first tile of its segment
+  uint32_t d;       // shared-memory float index of element e0-1
+  int32_t seed;     // q(x[lo]) for a segment's first tile
+  uint32_t has_seg;
+};
+
+template <int LPB>
+__global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ CompressArgs a) {
+  constexpr int WARPS = 8, ROUNDS = 4;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
   constexpr uint32_t TB = WARPS * ROUNDS * BPR;
-  extern __shared__ __align__(16) uint8_t s_out[];
+  extern __shared__ __align__(16) uint8_t s_buf[];  // input window, then the staged output
   __shared__ uint32_t s_tk[2];
-  __shared__ uint32_t s_w[WARPS + 1];
-  __shared__ uint64_t s_base;
+  __shared__ uint32_t s_off[TB];
+  __shared__ uint8_t s_bc[TB];
+  __shared__ uint32_t s_part[8];
   __shared__ uint32_t s_thr[36];
+  __shared__ uint32_t s_stash[ROUNDS * 8 * 32];
+  __shared__ uint64_t s_base;
+  __shared__ TileGeo s_g;
+  __shared__ __align__(8) uint64_t s_bar;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane % LPB, grp = lane / LPB;
   if (threadIdx.x < 36) s_thr[threadIdx.x] = a.thr.thr[threadIdx.x];
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
   uint32_t tile, epoch;
-  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);  // its barriers publish s_thr
+  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);  // its barriers publish s_thr and s_bar
 
-  const Segments sg = a.seg;
+  const Segments& sg = a.seg;
   const float eb = a.eb_dev ? *a.eb_dev : a.eb;
   const float inv = __fdiv_rn(1.0f, eb);
-  const TileInfo ti = tile_info(sg, tile, a.tiles_per_seg, TB, false);
+  float* sx = reinterpret_cast<float*>(s_buf);
   if (tile == 0) write_header_common(a.out, eb, sg);
-  const uint64_t lo = sg.lo(ti.seg), hi = sg.hi(ti.seg);
-  const uint64_t n = sg.n;
+
+  // ---- thread 0: geometry, then one bulk copy of the tile's input window ----
+  if (threadIdx.x == 0) {
+    TileGeo g;
+    g.has_seg = sg.n > 0;
+    uint32_t t = sg.T - 1, ts = tile;
+    if (a.tiles_per_seg) {
+      t = tile / a.tiles_per_seg;
+      if (t > sg.T - 1) t = sg.T - 1;
+      ts = tile - t * a.tiles_per_seg;
+    }
+    g.seg = t;
+    g.lo = (uint64_t)t * sg.tsz;
+    g.hi = t + 1 == sg.T ? sg.n : g.lo + sg.tsz;
+    const uint64_t nb = t + 1 == sg.T ? a.nb_last : a.nb_reg;
+    const uint64_t blk0 = (uint64_t)ts * TB;
+    g.nblk = nb > blk0 ? (uint32_t)min((uint64_t)TB, nb - blk0) : 0u;
+    g.first = ts == 0;
+    g.e0 = g.lo + 1 + blk0 * L;
+    g.nel = g.nblk ? (uint32_t)min((uint64_t)g.nblk * L, g.hi - g.e0) : 0u;
+    g.seed = 0;
+    g.d = 0;
+    bool bulk = false;
+    if (g.has_seg && g.nblk) {
+      // window [e0-1, e0+nel): element e at sx[e - (e0-1) + d]
+      const uintptr_t xa = (uintptr_t)a.x;
+      const uintptr_t w0 = xa + 4 * (g.e0 - 1), w1 = xa + 4 * (g.e0 + g.nel);
+      const uintptr_t a0 = w0 & ~(uintptr_t)15;
+      g.d = (uint32_t)((w0 - a0) >> 2);
+      const uintptr_t b0 = max(a0, (xa + 15) & ~(uintptr_t)15);
+      const uintptr_t b1 = min((w1 + 15) & ~(uintptr_t)15, (xa + 4 * sg.n) & ~(uintptr_t)15);
+      if (b1 > b0) {
+        bulk = true;
+        mbar_arrive_expect_tx(&s_bar, (uint32_t)(b1 - b0));
+        bulk_load(s_buf + (b0 - a0), reinterpret_cast<const void*>(b0), (uint32_t)(b1 - b0), &s_bar);
+        for (uintptr_t p = w0; p < b0; p += 4) sx[(p - a0) >> 2] = __ldg(reinterpret_cast<const float*>(p));
+        for (uintptr_t p = max(b1, w0); p < w1; p += 4) sx[(p - a0) >> 2] = __ldg(reinterpret_cast<const float*>(p));
+      } else {
+        for (uintptr_t p = w0; p < w1; p += 4) sx[(p - a0) >> 2] = __ldg(reinterpret_cast<const float*>(p));
+      }
+    }
+    if (g.has_seg && g.first && g.hi > g.lo) {
+      uint32_t f = 0;
+      g.seed = quantize(__ldg(a.x + g.lo), inv, f);
+    }
+    s_g = g;
+    s_tk[0] = bulk;
+  }
+  __syncthreads();
+  const TileGeo g = s_g;
+  if (s_tk[0] && !mbar_wait_bounded(&s_bar, 0, 1u << 22)) {
+    if (threadIdx.x == 0) atomicOr(a.err, kErrLookbackTimeout);
+    mbar_wait_bounded(&s_bar, 0, 1u << 22);
+  }
   uint32_t flags = 0;
 
-  const uint32_t wfirst = (uint32_t)warp * ROUNDS * BPR;  // first block of the warp, tile-relative
-  const uint32_t mis = (uint32_t)(((uintptr_t)(a.x + lo + 1)) >> 2) & 3u;
-
+  // ---- analysis: q, deltas, signs, block max, bit count, block size ----
   uint32_t vv[ROUNDS][8];
-  uint32_t sgnb[ROUNDS], bcs[ROUNDS], roff[ROUNDS];
-  uint32_t wbytes = 0;
-  int32_t carry = 0;
-  if (wfirst < ti.nblk && lane == 0) carry = quantize(__ldg(a.x + lo + (ti.blk0 + wfirst) * L), inv, flags);
-
+  uint32_t sgnb[ROUNDS];
+  const uint32_t sh = 1 + g.d;  // shared index of tile element 0
+  const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
 #pragma unroll
   for (int r = 0; r < ROUNDS; r++) {
-    const uint32_t bt = wfirst + r * BPR + grp;  // tile-relative block
-    const uint64_t b = ti.blk0 + bt;
-    const uint64_t bs = lo + 1 + b * L;  // first element of the block
-    const uint32_t m = bt < ti.nblk ? (uint32_t)min((uint64_t)L, hi - bs) : 0u;
-    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+    const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
+    const uint32_t k0 = bt * L + 8 * sub;  // tile-relative first element of the lane
+    const uint32_t ml = (bt < g.nblk && k0 < g.nel) ? min(8u, g.nel - k0) : 0u;
     float xv[8];
-    load8(a.x, bs + 8 * sub, ml, mis, n, xv);
-    int32_t q[8];
-    quantize8(xv, inv, q, flags);
-    int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
-    if (lane == 0) prev = carry;
-    carry = __shfl_sync(0xffffffffu, q[7], 31);
-    uint32_t sb = 0, lmax = 0;
+    const uint32_t i = sh + k0;
     if (__all_sync(0xffffffffu, ml == 8)) {
-      // every lane holds 8 elements: no masking
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
-        prev = q[j];
-        uint32_t v = (uint32_t)abs(d);  // |INT_MIN| wraps to 2^31 like the reference's -diff
-        sb = (sb << 1) + ((uint32_t)d >> 31);  // sign bits MSB first
-        lmax = max(lmax, v);
-        vv[r][j] = v;
+      const float4* q4 = reinterpret_cast<const float4*>(sx + (i & ~3u));
+      const float4 A = q4[0], B = q4[1];
+      if (ph == 0) {
+        xv[0] = A.x; xv[1] = A.y; xv[2] = A.z; xv[3] = A.w; xv[4] = B.x; xv[5] = B.y; xv[6] = B.z; xv[7] = B.w;
+      } else {
+        const float4 C = q4[2];
+        if (ph == 1) {
+          xv[0] = A.y; xv[1] = A.z; xv[2] = A.w; xv[3] = B.x; xv[4] = B.y; xv[5] = B.z; xv[6] = B.w; xv[7] = C.x;
+        } else if (ph == 2) {
+          xv[0] = A.z; xv[1] = A.w; xv[2] = B.x; xv[3] = B.y; xv[4] = B.z; xv[5] = B.w; xv[6] = C.x; xv[7] = C.y;
+        } else {
+          xv[0] = A.w; xv[1] = B.x; xv[2] = B.y; xv[3] = B.z; xv[4] = B.w; xv[5] = C.x; xv[6] = C.y; xv[7] = C.z;
+        }
       }
     } else {
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);
-        prev = q[j];
-        bool valid = (uint32_t)j < ml;
-        uint32_t v = valid ? (uint32_t)abs(d) : 0u;
-        sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
-        lmax = max(lmax, v);
-        vv[r][j] = v;
-      }
+      for (int j = 0; j < 8; j++) xv[j] = (uint32_t)j < ml ? sx[i + j] : 0.0f;
     }
+    int32_t q[8];
+    quantize8(xv, inv, q, flags);
+    int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
+    if (lane == 0) prev = quantize(sx[i - 1], inv, flags);  // the element before the warp's round
+    uint32_t sb = 0, lmax = 0;
 #pragma unroll
-    for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-    uint32_t bc = 0;
-    if (lmax) {
-      int k = 32 - __clz(lmax);
-      bc = k + (k >= 21 && lmax >= s_thr[k + 1] ? 1 : 0);
+    for (int j = 0; j < 8; j++) {
+      const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
+      prev = q[j];
+      const bool valid = (uint32_t)j < ml;
+      const uint32_t v = valid ? (uint32_t)abs(d) : 0u;  // |INT_MIN| is 2^31 as in the reference
+      sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
+      lmax = max(lmax, v);
+      vv[r][j] = v;
     }
     sgnb[r] = sb;
-    bcs[r] = bc;
-    const uint32_t size = m ? block_bytes(m, bc) : 0u;
-    // byte offsets of the blocks of this round: scan over group leaders
-    uint32_t val = sub == 0 ? size : 0u;
-    uint32_t incl = val;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+    for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if (sub == 0 && bt < g.nblk) {
+      uint32_t bc = 0;
+      if (lmax) {
+        const int k = 32 - __clz(lmax);
+        bc = k + (k >= 21 && lmax >= s_thr[k + 1] ? 1 : 0);
+      }
+      const uint32_t m = min(L, g.nel - bt * L);
+      s_bc[bt] = (uint8_t)bc;
+      s_off[bt] = block_bytes(m, bc);
     }
-    const uint32_t gex = __shfl_sync(0xffffffffu, incl - val, grp * LPB);
-    roff[r] = wbytes + gex;
-    wbytes += __shfl_sync(0xffffffffu, incl, 31);
   }
   if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
+  __syncthreads();
 
-  const bool seed = ti.has_seg && ti.first && hi > lo;
-  uint32_t wexcl;
-  const uint32_t agg = scan_warps<WARPS>(s_w, wbytes, warp, lane, wexcl, seed ? 4u : 0u);
-
+  // ---- block offsets in the tile, then the tile's offset in the stream ----
+  const bool seed = g.has_seg && g.first && g.hi > g.lo;
+  const uint32_t agg = cta_scan_excl(s_off, g.nblk, s_part) + (seed ? 4u : 0u);
   if (warp == 0) {
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++)
+#pragma unroll
+      for (int j = 0; j < 8; j++) s_stash[(r * 8 + j) * 32 + lane] = vv[r][j];
     uint64_t excl = 0;
     if (tile == 0) {
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
@@ -377,34 +451,33 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
     if (lane == 0) s_base = excl;
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++)
+#pragma unroll
+      for (int j = 0; j < 8; j++) vv[r][j] = s_stash[(r * 8 + j) * 32 + lane];
   }
   __syncthreads();
-  const uint64_t gpos = 4 + 8ull * sg.T + s_base;  // absolute stream position of the tile
+  const uint64_t gpos = 4 + 8ull * sg.T + s_base;
   if (tile == a.ntiles - 1 && threadIdx.x == 0) *a.out_size = gpos + agg;
-  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, s_base);
+  if (g.has_seg && g.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, g.seg, s_base);
   if (gpos + agg > a.cap) {
     if (threadIdx.x == 0) atomicOr(a.err, kErrCapacity);
     return;
   }
 
-  // ---- pack into shared memory at the destination's 16-byte phase ----
+  // ---- pack into the (now free) buffer at the destination's 16-byte phase ----
   const uint32_t align = (uint32_t)(((uintptr_t)a.out + gpos) & 15);
-  uint8_t* s_tile = s_out + align;
-  if (seed && warp == 0 && lane < 4) {
-    uint32_t f2 = 0;
-    int32_t sq = quantize(__ldg(a.x + lo), inv, f2);
-    s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
-  }
-  const uint32_t front = wexcl;  // includes the 4 seed bytes of a segment's first tile
+  uint8_t* s_tile = s_buf + align;
+  const uint32_t front = seed ? 4u : 0u;
+  if (seed && threadIdx.x < 4) s_tile[threadIdx.x] = (uint8_t)((uint32_t)g.seed >> (8 * threadIdx.x));
 #pragma unroll
   for (int r = 0; r < ROUNDS; r++) {
-    const uint32_t bt = wfirst + r * BPR + grp;
-    if (bt >= ti.nblk) continue;
-    const uint64_t bs = lo + 1 + (ti.blk0 + bt) * L;
-    const uint32_t m = (uint32_t)min((uint64_t)L, hi - bs);
+    const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
+    if (bt >= g.nblk) continue;
+    const uint32_t m = min(L, g.nel - bt * L);
     const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
-    const uint32_t bc = bcs[r];
-    uint8_t* dst = s_tile + front + roff[r];
+    const uint32_t bc = s_bc[bt];
+    uint8_t* dst = s_tile + front + s_off[bt];
     if (sub == 0) dst[0] = (uint8_t)bc;
     if (bc == 0 || ml == 0) continue;
     const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
@@ -414,7 +487,7 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         if ((uint32_t)j < ml) {
-          uint32_t h = vv[r][j] >> rr;
+          const uint32_t h = vv[r][j] >> rr;
           q8[j * B] = (uint8_t)h;
           if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
           if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
@@ -424,9 +497,12 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
     }
     if (rr) {  // remainder bits, MSB first, szp_TypeManager.cc:122-434
       const uint32_t mask = (1u << rr) - 1u;
-      uint64_t acc = 0;
+      uint32_t hi4 = 0, lo4 = 0;  // elements 0-3 and 4-7, 4*rr bits each
 #pragma unroll
-      for (int j = 0; j < 8; j++) acc = (acc << rr) | (uint64_t)((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
+      for (int j = 0; j < 4; j++) hi4 = (hi4 << rr) | ((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
+#pragma unroll
+      for (int j = 4; j < 8; j++) lo4 = (lo4 << rr) | ((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
+      const uint64_t acc = ((uint64_t)hi4 << (4 * rr)) | lo4;  // 8*rr bits, element 0 on top
       uint8_t* rp = dst + 1 + ns + B * m + rr * sub;
       const uint32_t nb = (ml * rr + 7) >> 3;
       const uint32_t top = 8 * rr - 8;
@@ -435,7 +511,7 @@ __global__ void __launch_bounds__(256) compress_fm1_lanes(CompressArgs a) {
         if (k < nb) rp[k] = (uint8_t)(acc >> (top - 8 * k));
     }
   }
-  flush_span_bulk(a.out + gpos, s_out, align, agg);
+  flush_span_bulk(a.out + gpos, s_buf, align, agg);
 }
 
 // ---------------------------------------------------------------------------
@@ -742,12 +818,15 @@ uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw) {
 }
 
 size_t compress_smem_bytes(uint32_t L, uint32_t tb) {
-  return 16 + 4 + (size_t)tb * (max_block_bytes(L) + 4) + 32;
+  // the staged output, or the input window (tb*L+1 floats, 16-byte aligned) it replaces
+  size_t out = 16 + 4 + (size_t)tb * (max_block_bytes(L) + 4) + 32;
+  size_t in = 4 * ((size_t)tb * L + 1) + 32;
+  return out > in ? out : in;
 }
 
 template <int LPB>
 static cudaError_t launch_lanes(const CompressArgs& a, size_t smem, cudaStream_t st) {
-  auto k = compress_fm1_lanes<LPB, kRounds>;
+  auto k = compress_fm1_tma<LPB>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<a.ntiles, 256, smem, st>>>(a);

@@ -642,7 +642,7 @@ __device__ __forceinline__ void store8(float* __restrict__ y, uint64_t s, uint32
 // fastmode1, blockSize L = 8*LPB: LPB lanes per block, 8 elements per lane
 // (the byte layout of 8 elements is self-contained, see compress.cu).
 template <int LPB, int ROUNDS>
-__global__ void __launch_bounds__(256) decode_fm1_lanes(DecArgs a) {
+__global__ void __launch_bounds__(256) decode_fm1_lanes(const __grid_constant__ DecArgs a) {
   constexpr int WARPS = 8;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
@@ -653,7 +653,7 @@ __global__ void __launch_bounds__(256) decode_fm1_lanes(DecArgs a) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_geo[2];  // span start (region offset), span length
   __shared__ __align__(8) uint64_t s_bar;
-  __shared__ uint64_t s_red[2 * WARPS + 2];
+  __shared__ uint32_t s_stash[ROUNDS * 8 * 32];
   uint32_t tile, epoch;
   draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
   if (a.plan->bad) return;
@@ -800,7 +800,19 @@ __global__ void __launch_bounds__(256) decode_fm1_lanes(DecArgs a) {
       }
     } else {
       if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
-      excl = (uint32_t)lookback_sum_cta(a.status, tile, first_tile, epoch, a.err, s_red);
+      if (warp == 0) {
+        // the look-back needs registers: park this warp's prefix sums in shared memory
+        uint32_t* stash = reinterpret_cast<uint32_t*>(s_stash);
+#pragma unroll
+        for (int r = 0; r < ROUNDS; r++)
+#pragma unroll
+          for (int j = 0; j < 8; j++) stash[(r * 8 + j) * 32 + lane] = pre[r][j];
+        excl = (uint32_t)lookback_sum(a.status, tile, first_tile, epoch, a.err);
+#pragma unroll
+        for (int r = 0; r < ROUNDS; r++)
+#pragma unroll
+          for (int j = 0; j < 8; j++) pre[r][j] = stash[(r * 8 + j) * 32 + lane];
+      }
       if (threadIdx.x == 0)
         st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
     }

@@ -116,6 +116,7 @@ extern "C" int szp_gb300_compress_dev_noalloc(const float* d_data, size_t nbEle,
   a.tiles_per_seg = (uint32_t)per_seg;
   a.tb = tb;
   a.bpw = bpw;
+  host_segment_blocks(nbEle, T, blockSize, a.nb_reg, a.nb_last);
   a.thr = host_bitcount_table();
   int launches = 1;
   if (errBoundMode == REL) {

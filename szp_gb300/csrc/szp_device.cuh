@@ -155,42 +155,66 @@ __device__ __forceinline__ void draw_ticket(LaunchState* ls, uint32_t ntiles, ui
 
 constexpr uint32_t kSpinLimit = 1u << 20;  // look-back spins (~1 s) before giving up
 
-// Decoupled look-back over an additive 42-bit quantity (all tiles share one
-// chain; `stop_at` lets a chain restart at a segment boundary: tiles < stop_at
-// are not consulted).  Called by one full warp; returns the exclusive prefix.
-// On timeout sets kErrLookbackTimeout in *err and returns 0.
+// Decoupled look-back over an additive 42-bit quantity, by one full warp.
+// Each lane reads LB_K predecessors per round trip (lane l, slot k holds the
+// tile at distance 1 + l + 32k), so a window covers 32*LB_K tiles: a tile whose
+// nearest finished predecessor is D tiles back waits ceil(D / (32*LB_K)) round
+// trips.  Tiles < stop_at are not consulted (a chain can restart at a segment
+// boundary).  Returns the exclusive prefix; on timeout sets
+// kErrLookbackTimeout and returns 0.
+constexpr int LB_K = 4;
+
 __device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_t tile, uint32_t stop_at,
                                                  uint32_t epoch, uint32_t* err) {
   const int lane = threadIdx.x & 31;
+  const uint32_t ep = epoch & 0xFFFFF;
   uint64_t excl = 0;
-  int64_t base = (int64_t)tile - 1;
+  int64_t base = (int64_t)tile - 1;  // distance 1
   uint32_t spins = 0;
   while (base >= (int64_t)stop_at) {
-    int64_t idx = base - lane;
-    uint64_t s = 0;
-    bool ready = true;
-    if (idx >= (int64_t)stop_at) {
-      s = ld_volatile_u64(status + idx);  // the word carries its value: no acquire needed
-      ready = status_epoch(s) == (epoch & 0xFFFFF) && status_flag(s) != 0;
+    uint64_t s[LB_K];
+    uint32_t incl[LB_K], nready[LB_K];
+#pragma unroll
+    for (int k = 0; k < LB_K; k++) {
+      const int64_t idx = base - lane - 32 * k;
+      s[k] = idx >= (int64_t)stop_at ? ld_volatile_u64(status + idx) : 0;
     }
-    // wait until every lane in the window up to the first inclusive is ready
-    uint32_t incl = __ballot_sync(0xffffffffu, idx >= (int64_t)stop_at && ready && status_flag(s) == kFlagInclusive);
-    uint32_t notready = __ballot_sync(0xffffffffu, !ready);
-    // lanes beyond the first inclusive are irrelevant
-    uint32_t upto = incl ? (incl & (0u - incl)) : 0;  // lowest set bit = nearest inclusive
-    uint32_t relevant = upto ? (upto | (upto - 1)) : 0xffffffffu;
-    if (notready & relevant) {
+    int dstar = 32 * LB_K;  // nearest inclusive (distance index), none yet
+#pragma unroll
+    for (int k = 0; k < LB_K; k++) {
+      const int64_t idx = base - lane - 32 * k;
+      const bool inr = idx >= (int64_t)stop_at;
+      const bool ready = !inr || (status_epoch(s[k]) == ep && status_flag(s[k]) != 0);
+      incl[k] = __ballot_sync(0xffffffffu, inr && ready && status_flag(s[k]) == kFlagInclusive);
+      nready[k] = __ballot_sync(0xffffffffu, !ready);
+      if (dstar == 32 * LB_K && incl[k]) dstar = 32 * k + __ffs(incl[k]) - 1;
+    }
+    // every predecessor closer than (and at) the nearest inclusive must be ready
+    bool wait = false;
+#pragma unroll
+    for (int k = 0; k < LB_K; k++) {
+      const int lo = 32 * k;
+      if (lo > dstar) break;
+      uint32_t rel = dstar - lo >= 31 ? 0xffffffffu : ((2u << (dstar - lo)) - 1u);
+      if (nready[k] & rel) wait = true;
+    }
+    if (wait) {
       if (++spins > kSpinLimit) {
         if (lane == 0) atomicOr(err, kErrLookbackTimeout);
         return 0;
       }
       continue;
     }
-    uint64_t v = (idx >= (int64_t)stop_at && ((relevant >> lane) & 1)) ? status_value(s) : 0;
+    uint64_t v = 0;
+#pragma unroll
+    for (int k = 0; k < LB_K; k++) {
+      const int64_t idx = base - lane - 32 * k;
+      if (idx >= (int64_t)stop_at && lane + 32 * k <= dstar) v += status_value(s[k]);
+    }
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     excl += v;
-    if (upto) break;
-    base -= 32;
+    if (dstar < 32 * LB_K) break;
+    base -= 32 * LB_K;
   }
   return excl;
 }

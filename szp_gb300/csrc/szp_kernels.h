@@ -23,6 +23,8 @@ struct CompressArgs {
   uint32_t tiles_per_seg;  // tiles of segments 0..T-2
   uint32_t tb;           // blocks per tile
   uint32_t bpw;          // blocks per warp (generic kernel)
+  uint64_t nb_reg;       // blocks of segments 0..T-2
+  uint64_t nb_last;      // blocks of segment T-1
   BitcountTable thr;
 };
 
@@ -96,6 +98,7 @@ const BitcountTable& host_bitcount_table();
 int host_resolve_segments(int requested);
 void host_compress_tiles(size_t n, int T, int L, uint64_t& tiles_per_seg, uint64_t& ntiles, uint32_t& tb,
                          uint32_t& bpw);
+void host_segment_blocks(size_t n, int T, int L, uint64_t& nb_reg, uint64_t& nb_last);
 int host_fail(int status, const char* msg);
 void host_clear_error();
 void host_count_launches(int k);
