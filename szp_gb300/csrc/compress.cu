@@ -212,30 +212,38 @@ __device__ __forceinline__ void flush_span_bulk(uint8_t* __restrict__ gdst, uint
   }
 }
 
-// Exact path for the elements whose |x/eb| >= 2^24 (or NaN/inf); kept out
-// of line so the common path issues no FP64 instructions.
-__device__ __noinline__ void quantize8_slow(const float* xv, float inv, int32_t* q, uint32_t* flags) {
+// Exact path for |x/eb| >= 2^24 (or NaN/inf), out of line so the common path
+// issues no FP64 instructions; returns q in the low word, flags in the high.
+__device__ __noinline__ uint64_t quantize_rare(float x, float inv) {
   uint32_t f = 0;
-#pragma unroll
-  for (int j = 0; j < 8; j++) {
-    float p = __fmul_rz(xv[j], inv);
-    if (!(fabsf(p) < 16777216.0f)) q[j] = quantize_slow(xv[j], inv, f);
-  }
-  *flags |= f;
+  const int32_t q = quantize_slow(x, inv, f);
+  return ((uint64_t)f << 32) | (uint32_t)q;
 }
 
-// q = trunc(x/eb) for 8 values (see quantize()); slow lanes fixed by a
-// warp-uniform branch.
+// q = trunc(x/eb) (see quantize()), fast path inline.
+__device__ __forceinline__ int32_t quantize_lean(float x, float inv, uint32_t& flags) {
+  const float p = __fmul_rz(x, inv);
+  int32_t q = __float2int_rz(p);
+  if (!(fabsf(p) < 16777216.0f)) {
+    const uint64_t r = quantize_rare(x, inv);
+    q = (int32_t)(uint32_t)r;
+    flags |= (uint32_t)(r >> 32);
+  }
+  return q;
+}
+
+// q for 8 values; the rare slow elements are redone behind a warp-uniform branch.
 __device__ __forceinline__ void quantize8(const float* xv, float inv, int32_t* q, uint32_t& flags) {
   bool slow = false;
 #pragma unroll
   for (int j = 0; j < 8; j++) {
-    float p = __fmul_rz(xv[j], inv);
+    const float p = __fmul_rz(xv[j], inv);
     q[j] = __float2int_rz(p);
     slow |= !(fabsf(p) < 16777216.0f);
   }
   if (__any_sync(0xffffffffu, slow)) {
-    if (slow) quantize8_slow(xv, inv, q, &flags);
+#pragma unroll
+    for (int j = 0; j < 8; j++) q[j] = quantize_lean(xv[j], inv, flags);
   }
 }
 
@@ -376,6 +384,7 @@ __global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ 
   uint32_t sgnb[ROUNDS];
   const uint32_t sh = 1 + g.d;  // shared index of tile element 0
   const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
+  const bool full = g.nblk == TB && g.nel == TB * L;  // every lane of every round holds 8 elements
 #pragma unroll
   for (int r = 0; r < ROUNDS; r++) {
     const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
@@ -383,7 +392,7 @@ __global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ 
     const uint32_t ml = (bt < g.nblk && k0 < g.nel) ? min(8u, g.nel - k0) : 0u;
     float xv[8];
     const uint32_t i = sh + k0;
-    if (__all_sync(0xffffffffu, ml == 8)) {
+    if (full) {
       const float4* q4 = reinterpret_cast<const float4*>(sx + (i & ~3u));
       const float4 A = q4[0], B = q4[1];
       if (ph == 0) {
@@ -405,17 +414,29 @@ __global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ 
     int32_t q[8];
     quantize8(xv, inv, q, flags);
     int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
-    if (lane == 0) prev = quantize(sx[i - 1], inv, flags);  // the element before the warp's round
+    if (lane == 0) prev = quantize_lean(sx[i - 1], inv, flags);  // the element before the warp's round
     uint32_t sb = 0, lmax = 0;
+    if (full) {
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
-      prev = q[j];
-      const bool valid = (uint32_t)j < ml;
-      const uint32_t v = valid ? (uint32_t)abs(d) : 0u;  // |INT_MIN| is 2^31 as in the reference
-      sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
-      lmax = max(lmax, v);
-      vv[r][j] = v;
+      for (int j = 0; j < 8; j++) {
+        const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
+        prev = q[j];
+        const uint32_t v = (uint32_t)abs(d);  // |INT_MIN| is 2^31 as in the reference
+        sb = (sb << 1) + ((uint32_t)d >> 31);
+        lmax = max(lmax, v);
+        vv[r][j] = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);
+        prev = q[j];
+        const bool valid = (uint32_t)j < ml;
+        const uint32_t v = valid ? (uint32_t)abs(d) : 0u;
+        sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
+        lmax = max(lmax, v);
+        vv[r][j] = v;
+      }
     }
     sgnb[r] = sb;
 #pragma unroll
@@ -470,6 +491,56 @@ __global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ 
   uint8_t* s_tile = s_buf + align;
   const uint32_t front = seed ? 4u : 0u;
   if (seed && threadIdx.x < 4) s_tile[threadIdx.x] = (uint8_t)((uint32_t)g.seed >> (8 * threadIdx.x));
+  if (full) {
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+      const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
+      const uint32_t bc = s_bc[bt];
+      uint8_t* dst = s_tile + front + s_off[bt];
+      if (sub == 0) dst[0] = (uint8_t)bc;
+      const uint32_t B = bc >> 3, rr = bc & 7;
+      constexpr uint32_t ns = L / 8;
+      if (bc) dst[1 + sub] = (uint8_t)sgnb[r];
+      if (__all_sync(0xffffffffu, B <= 1)) {
+        if (B) {
+          uint8_t* q8 = dst + 1 + ns + 8 * sub;
+#pragma unroll
+          for (int j = 0; j < 8; j++) q8[j] = (uint8_t)(vv[r][j] >> rr);
+        }
+      } else if (B) {
+        uint8_t* q8 = dst + 1 + ns + 8 * B * sub;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const uint32_t h = vv[r][j] >> rr;
+          q8[j * B] = (uint8_t)h;
+          if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
+          if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
+          if (B > 3) q8[j * B + 3] = (uint8_t)(h >> 24);
+        }
+      }
+      if (rr) {
+        const uint32_t mask = (1u << rr) - 1u;
+        uint32_t hi4 = 0, lo4 = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) hi4 = (hi4 << rr) | (vv[r][j] & mask);
+#pragma unroll
+        for (int j = 4; j < 8; j++) lo4 = (lo4 << rr) | (vv[r][j] & mask);
+        // 8*rr bits, element 0 first, moved to the top of 64 bits
+        const uint64_t top = (((uint64_t)hi4 << (4 * rr)) | lo4) << (64 - 8 * rr);
+        const uint32_t th = (uint32_t)(top >> 32), tl = (uint32_t)top;
+        uint8_t* rp = dst + 1 + ns + B * L + rr * sub;
+        rp[0] = (uint8_t)(th >> 24);
+        if (rr > 1) rp[1] = (uint8_t)(th >> 16);
+        if (rr > 2) rp[2] = (uint8_t)(th >> 8);
+        if (rr > 3) rp[3] = (uint8_t)th;
+        if (rr > 4) rp[4] = (uint8_t)(tl >> 24);
+        if (rr > 5) rp[5] = (uint8_t)(tl >> 16);
+        if (rr > 6) rp[6] = (uint8_t)(tl >> 8);
+      }
+    }
+    flush_span_bulk(a.out + gpos, s_buf, align, agg);
+    return;
+  }
 #pragma unroll
   for (int r = 0; r < ROUNDS; r++) {
     const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
