@@ -13,6 +13,8 @@
 //   bit count (int)log2f(max)+1                                :253-262
 //   sign bitmap / fixed-length packing   szp_TypeManager.cc:13-94,820-844
 //   fastmode2 per-block seed                                   :812-864
+#include <atomic>
+
 #include "szp_device.cuh"
 #include "szp_kernels.h"
 #include "szp_tma.cuh"
@@ -247,11 +249,60 @@ __device__ __forceinline__ void quantize8(const float* xv, float inv, int32_t* q
   }
 }
 
-// Exclusive scan of n (<= 4*blockDim) values in shared memory by the whole
-// CTA (256 threads); returns the total.  s_part needs 8 words.
-__device__ __forceinline__ uint32_t cta_scan_excl(uint32_t* v, uint32_t n, uint32_t* s_part) {
+// Tile geometry, computed by the producer.
+struct TileGeo {
+  uint64_t lo, hi;  // segment element range
+  uint64_t e0;      // first element of the tile's first block
+  uint32_t seg, nblk, nel;  // blocks, elements of those blocks
+  uint32_t first;   // first tile of its segment
+  uint32_t d;       // slot float index of element e0-1
+  uint32_t has_seg;
+};
+
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised pipeline (fastmode1, blockSize L = 8*LPB).
+//
+// A CTA works through tiles until the tickets run out.  Warp roles:
+//   compute  (warps 0-7)  quantize, delta, sign and bit-count analysis, the
+//                         scan of block sizes, then packing of the blocks into
+//                         the tile's slot from offset 0.  They never wait for
+//                         the tile's stream offset.
+//   control  (kPipeControl warps, tiles round robin)  decoupled look-back for
+//                         the stream offset, then a shifted copy of the packed
+//                         slot to the stream with 16-byte stores.
+//   producer (1 warp)     draws tile tickets and fills free slots with the
+//                         tiles' input windows by bulk copy (TMA).
+// kPipeSlots shared-memory slots cycle through four mbarriers each: full
+// (producer -> compute, control), agg (tile byte count known), packed
+// (compute -> control) and empty (control -> producer).  Tickets are drawn in
+// order and every wait depends only on lower tickets or earlier stages of the
+// same tile, so the pipeline cannot deadlock; every wait is bounded.
+// ---------------------------------------------------------------------------
+constexpr int kPipeSlots = 3, kPipeControl = 2;
+constexpr int kPipeThreads = (8 + kPipeControl + 1) * 32;
+constexpr uint32_t kStopTile = 0xFFFFFFFFu;
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+struct SlotMeta {
+  TileGeo g;
+  uint32_t tile;  // kStopTile: no more tiles for this CTA
+};
+
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// Waits for an mbarrier phase; on timeout flags the launch and waits once more.
+__device__ __forceinline__ void mbar_wait_or_flag(uint64_t* bar, uint32_t parity, uint32_t* err) {
+  if (!mbar_wait_bounded(bar, parity, kWaitLimit)) {
+    atomicOr(err, kErrLookbackTimeout);
+    mbar_wait_bounded(bar, parity, kWaitLimit);
+  }
+}
+
+// Exclusive scan of n (<= 1024) values in shared memory by the 256 compute
+// threads; returns the total.  s_part needs 8 words.
+__device__ __forceinline__ uint32_t compute_scan_excl(uint32_t* v, uint32_t n, uint32_t* s_part) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+  const uint32_t per = (n + 255) / 256;
   const uint32_t i0 = threadIdx.x * per;
   uint32_t loc[4], sum = 0;
 #pragma unroll
@@ -266,9 +317,10 @@ __device__ __forceinline__ uint32_t cta_scan_excl(uint32_t* v, uint32_t n, uint3
     if (lane >= o) incl += y;
   }
   if (lane == 31) s_part[warp] = incl;
-  __syncthreads();
+  compute_sync();
   uint32_t wex = 0, tot = 0;
-  for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+#pragma unroll
+  for (int w = 0; w < 8; w++) {
     uint32_t pw = s_part[w];
     if (w < warp) wex += pw;
     tot += pw;
@@ -279,53 +331,90 @@ __device__ __forceinline__ uint32_t cta_scan_excl(uint32_t* v, uint32_t n, uint3
     if ((uint32_t)k < per && i0 + k < n) v[i0 + k] = run;
     run += loc[k];
   }
-  __syncthreads();
+  compute_sync();
   return tot;
 }
 
-// Tile geometry, computed once by thread 0.
-struct TileGeo {
-  uint64_t lo, hi;  // segment element range
-  uint64_t e0;      // first element of the tile's first block
-  uint32_t seg, nblk, nel;  // blocks, elements of those blocks
-  uint32_t first;   // first tile of its segment
-  uint32_t d;       // shared-memory float index of element e0-1
-  int32_t seed;     // q(x[lo]) for a segment's first tile
-  uint32_t has_seg;
-};
+// eb (big-endian) and, when every segment but the last is empty (n < T),
+// their zero offsets (szp_float.cc:164,280-289); one warp.
+__device__ __forceinline__ void write_header_warp(uint8_t* out, float eb, const Segments& sg, int lane) {
+  const uint32_t b = __float_as_uint(eb);
+  if (lane < 4) out[lane] = (uint8_t)(b >> (24 - 8 * lane));
+  if (sg.tsz == 0) {
+    const uint32_t nz = 8 * (sg.n == 0 ? sg.T : sg.T - 1);
+    for (uint32_t i = lane; i < nz; i += 32) out[4 + i] = 0;
+  }
+}
 
-template <int LPB>
-__global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ CompressArgs a) {
-  constexpr int WARPS = 8, ROUNDS = 4;
-  constexpr uint32_t L = 8 * LPB;
-  constexpr int BPR = 32 / LPB;
-  constexpr uint32_t TB = WARPS * ROUNDS * BPR;
-  extern __shared__ __align__(16) uint8_t s_buf[];  // input window, then the staged output
-  __shared__ uint32_t s_tk[2];
-  __shared__ uint32_t s_off[TB];
-  __shared__ uint8_t s_bc[TB];
-  __shared__ uint32_t s_part[8];
-  __shared__ uint32_t s_thr[36];
-  __shared__ uint32_t s_stash[ROUNDS * 8 * 32];
-  __shared__ uint64_t s_base;
-  __shared__ TileGeo s_g;
-  __shared__ __align__(8) uint64_t s_bar;
+// One warp copies len bytes from shared memory src (16-byte aligned, readable
+// for len + 16 bytes) to global dst (any alignment): 16-byte stores for the
+// aligned middle, the bytes shifted into place with funnel shifts; byte
+// stores for the ragged ends, which neighbouring tiles share.
+__device__ __forceinline__ void warp_store_span(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
+                                                uint32_t len, int lane) {
+  if (len == 0) return;
+  const uint32_t a = (uint32_t)((uintptr_t)dst & 15);
+  uint8_t* g0 = dst - a;                             // 16-byte aligned
+  const uint32_t end = a + len;                      // the span is [a, end) from g0
+  const uint32_t c0 = (a + 15) >> 4, c1 = end >> 4;  // whole 16-byte chunks [c0, c1)
+  if (c0 >= c1) {
+    for (uint32_t b = a + (uint32_t)lane; b < end; b += 32) g0[b] = src[b - a];
+    return;
+  }
+  if ((uint32_t)lane < 16 * c0 - a) g0[a + lane] = src[lane];
+  if ((uint32_t)lane < end - 16 * c1) g0[16 * c1 + lane] = src[16 * c1 + lane - a];
+  const uint32_t sh = (16 - a) & 15;  // chunk c starts at src byte 16c - a = 16(c - 1) + sh when a != 0
+  if (sh == 0) {
+    for (uint32_t c = c0 + lane; c < c1; c += 32)
+      *reinterpret_cast<uint4*>(g0 + 16 * c) = *reinterpret_cast<const uint4*>(src + 16 * c);
+    return;
+  }
+  const uint32_t q = sh >> 2, bs = 8 * (sh & 3);
+  for (uint32_t c = c0 + lane; c < c1; c += 32) {
+    const uint4* line = reinterpret_cast<const uint4*>(src + 16 * (c - 1));
+    const uint4 u = line[0], v = line[1];
+    const uint32_t w[8] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
+    uint4 o;
+#define SZP_FS(i) __funnelshift_r(w[(i)], w[(i) + 1], bs)
+    switch (q) {
+      case 0: o = make_uint4(SZP_FS(0), SZP_FS(1), SZP_FS(2), SZP_FS(3)); break;
+      case 1: o = make_uint4(SZP_FS(1), SZP_FS(2), SZP_FS(3), SZP_FS(4)); break;
+      case 2: o = make_uint4(SZP_FS(2), SZP_FS(3), SZP_FS(4), SZP_FS(5)); break;
+      default: o = make_uint4(SZP_FS(3), SZP_FS(4), SZP_FS(5), SZP_FS(6)); break;
+    }
+#undef SZP_FS
+    *reinterpret_cast<uint4*>(g0 + 16 * c) = o;
+  }
+}
 
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int sub = lane % LPB, grp = lane / LPB;
-  if (threadIdx.x < 36) s_thr[threadIdx.x] = a.thr.thr[threadIdx.x];
-  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
-  uint32_t tile, epoch;
-  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);  // its barriers publish s_thr and s_bar
-
+// Producer: one thread.  Draws tickets, and for each tile computes its
+// geometry and bulk-copies its input window [e0-1, e0+nel) into a free slot
+// (element e at slot float e - (e0-1) + d).
+template <uint32_t L, uint32_t TB, int NS>
+__device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* slots, uint32_t slot_bytes,
+                                              SlotMeta* meta, uint64_t* full, uint64_t* empty,
+                                              uint32_t* s_epoch, volatile uint32_t* s_stop_k) {
   const Segments& sg = a.seg;
-  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
-  const float inv = __fdiv_rn(1.0f, eb);
-  float* sx = reinterpret_cast<float*>(s_buf);
-  if (tile == 0) write_header_common(a.out, eb, sg);
-
-  // ---- thread 0: geometry, then one bulk copy of the tile's input window ----
-  if (threadIdx.x == 0) {
+  *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
+  __threadfence();
+  for (uint32_t k = 0;; k++) {
+    const int s = (int)(k % NS);
+    if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
+    const uint32_t tile = atomicAdd(&a.ls->ticket, 1u);
+    if (tile == a.ntiles + gridDim.x - 1) {
+      // the last draw of the launch: every CTA has read the epoch
+      a.ls->ticket = 0;
+      __threadfence();
+      atomicAdd(&a.ls->epoch, 1u);
+    }
+    SlotMeta& m = meta[s];
+    if (tile >= a.ntiles) {
+      m.tile = kStopTile;
+      *s_stop_k = k;
+      mbar_arrive(&full[s]);
+      return;
+    }
+    float* sx = reinterpret_cast<float*>(slots + (size_t)s * slot_bytes);
     TileGeo g;
     g.has_seg = sg.n > 0;
     uint32_t t = sg.T - 1, ts = tile;
@@ -343,246 +432,331 @@ __global__ void __launch_bounds__(256) compress_fm1_tma(const __grid_constant__ 
     g.first = ts == 0;
     g.e0 = g.lo + 1 + blk0 * L;
     g.nel = g.nblk ? (uint32_t)min((uint64_t)g.nblk * L, g.hi - g.e0) : 0u;
-    g.seed = 0;
     g.d = 0;
-    bool bulk = false;
-    if (g.has_seg && g.nblk) {
-      // window [e0-1, e0+nel): element e at sx[e - (e0-1) + d]
+    uint32_t bytes = 0;
+    uintptr_t b0 = 0, a0 = 0;
+    if (g.has_seg && (g.nblk || (g.first && g.hi > g.lo))) {  // a lone seed still needs x[lo]
       const uintptr_t xa = (uintptr_t)a.x;
       const uintptr_t w0 = xa + 4 * (g.e0 - 1), w1 = xa + 4 * (g.e0 + g.nel);
-      const uintptr_t a0 = w0 & ~(uintptr_t)15;
+      a0 = w0 & ~(uintptr_t)15;
       g.d = (uint32_t)((w0 - a0) >> 2);
-      const uintptr_t b0 = max(a0, (xa + 15) & ~(uintptr_t)15);
+      b0 = max(a0, (xa + 15) & ~(uintptr_t)15);
       const uintptr_t b1 = min((w1 + 15) & ~(uintptr_t)15, (xa + 4 * sg.n) & ~(uintptr_t)15);
       if (b1 > b0) {
-        bulk = true;
-        mbar_arrive_expect_tx(&s_bar, (uint32_t)(b1 - b0));
-        bulk_load(s_buf + (b0 - a0), reinterpret_cast<const void*>(b0), (uint32_t)(b1 - b0), &s_bar);
+        bytes = (uint32_t)(b1 - b0);
         for (uintptr_t p = w0; p < b0; p += 4) sx[(p - a0) >> 2] = __ldg(reinterpret_cast<const float*>(p));
         for (uintptr_t p = max(b1, w0); p < w1; p += 4) sx[(p - a0) >> 2] = __ldg(reinterpret_cast<const float*>(p));
       } else {
         for (uintptr_t p = w0; p < w1; p += 4) sx[(p - a0) >> 2] = __ldg(reinterpret_cast<const float*>(p));
       }
     }
-    if (g.has_seg && g.first && g.hi > g.lo) {
-      uint32_t f = 0;
-      g.seed = quantize(__ldg(a.x + g.lo), inv, f);
-    }
-    s_g = g;
-    s_tk[0] = bulk;
-  }
-  __syncthreads();
-  const TileGeo g = s_g;
-  if (s_tk[0] && !mbar_wait_bounded(&s_bar, 0, 1u << 22)) {
-    if (threadIdx.x == 0) atomicOr(a.err, kErrLookbackTimeout);
-    mbar_wait_bounded(&s_bar, 0, 1u << 22);
-  }
-  uint32_t flags = 0;
-
-  // ---- analysis: q, deltas, signs, block max, bit count, block size ----
-  uint32_t vv[ROUNDS][8];
-  uint32_t sgnb[ROUNDS];
-  const uint32_t sh = 1 + g.d;  // shared index of tile element 0
-  const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
-  const bool full = g.nblk == TB && g.nel == TB * L;  // every lane of every round holds 8 elements
-#pragma unroll
-  for (int r = 0; r < ROUNDS; r++) {
-    const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
-    const uint32_t k0 = bt * L + 8 * sub;  // tile-relative first element of the lane
-    const uint32_t ml = (bt < g.nblk && k0 < g.nel) ? min(8u, g.nel - k0) : 0u;
-    float xv[8];
-    const uint32_t i = sh + k0;
-    if (full) {
-      const float4* q4 = reinterpret_cast<const float4*>(sx + (i & ~3u));
-      const float4 A = q4[0], B = q4[1];
-      if (ph == 0) {
-        xv[0] = A.x; xv[1] = A.y; xv[2] = A.z; xv[3] = A.w; xv[4] = B.x; xv[5] = B.y; xv[6] = B.z; xv[7] = B.w;
-      } else {
-        const float4 C = q4[2];
-        if (ph == 1) {
-          xv[0] = A.y; xv[1] = A.z; xv[2] = A.w; xv[3] = B.x; xv[4] = B.y; xv[5] = B.z; xv[6] = B.w; xv[7] = C.x;
-        } else if (ph == 2) {
-          xv[0] = A.z; xv[1] = A.w; xv[2] = B.x; xv[3] = B.y; xv[4] = B.z; xv[5] = B.w; xv[6] = C.x; xv[7] = C.y;
-        } else {
-          xv[0] = A.w; xv[1] = B.x; xv[2] = B.y; xv[3] = B.z; xv[4] = B.w; xv[5] = C.x; xv[6] = C.y; xv[7] = C.z;
-        }
-      }
+    m.g = g;
+    m.tile = tile;
+    if (bytes) {
+      fence_async_smem();
+      mbar_arrive_expect_tx(&full[s], bytes);
+      bulk_load(reinterpret_cast<uint8_t*>(sx) + (b0 - a0), reinterpret_cast<const void*>(b0), bytes, &full[s]);
     } else {
-#pragma unroll
-      for (int j = 0; j < 8; j++) xv[j] = (uint32_t)j < ml ? sx[i + j] : 0.0f;
-    }
-    int32_t q[8];
-    quantize8(xv, inv, q, flags);
-    int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
-    if (lane == 0) prev = quantize_lean(sx[i - 1], inv, flags);  // the element before the warp's round
-    uint32_t sb = 0, lmax = 0;
-    if (full) {
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
-        prev = q[j];
-        const uint32_t v = (uint32_t)abs(d);  // |INT_MIN| is 2^31 as in the reference
-        sb = (sb << 1) + ((uint32_t)d >> 31);
-        lmax = max(lmax, v);
-        vv[r][j] = v;
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);
-        prev = q[j];
-        const bool valid = (uint32_t)j < ml;
-        const uint32_t v = valid ? (uint32_t)abs(d) : 0u;
-        sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
-        lmax = max(lmax, v);
-        vv[r][j] = v;
-      }
-    }
-    sgnb[r] = sb;
-#pragma unroll
-    for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-    if (sub == 0 && bt < g.nblk) {
-      uint32_t bc = 0;
-      if (lmax) {
-        const int k = 32 - __clz(lmax);
-        bc = k + (k >= 21 && lmax >= s_thr[k + 1] ? 1 : 0);
-      }
-      const uint32_t m = min(L, g.nel - bt * L);
-      s_bc[bt] = (uint8_t)bc;
-      s_off[bt] = block_bytes(m, bc);
+      mbar_arrive(&full[s]);
     }
   }
-  if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
-  __syncthreads();
+}
 
-  // ---- block offsets in the tile, then the tile's offset in the stream ----
-  const bool seed = g.has_seg && g.first && g.hi > g.lo;
-  const uint32_t agg = cta_scan_excl(s_off, g.nblk, s_part) + (seed ? 4u : 0u);
-  if (warp == 0) {
-#pragma unroll
-    for (int r = 0; r < ROUNDS; r++)
-#pragma unroll
-      for (int j = 0; j < 8; j++) s_stash[(r * 8 + j) * 32 + lane] = vv[r][j];
+// Control warp c: tiles c, c + kPipeControl, ... of this CTA.
+template <int NS, int NC>
+__device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const uint8_t* slots,
+                                             uint32_t slot_bytes, const SlotMeta* meta, const uint32_t* s_agg,
+                                             uint64_t* full, uint64_t* aggb, uint64_t* packed, uint64_t* empty,
+                                             const uint32_t* s_epoch, const volatile uint32_t* s_stop_k, float eb) {
+  const int lane = threadIdx.x & 31;
+  const Segments& sg = a.seg;
+  for (uint32_t k = (uint32_t)c;; k += NC) {
+    const int s = (int)(k % NS);
+    const uint32_t par = (k / NS) & 1;
+    bool got = false;
+    for (uint32_t i = 0; i < kWaitLimit; i++) {
+      if ((got = mbar_try_wait(&full[s], par))) break;
+      if (*s_stop_k <= k) break;
+    }
+    if (!__all_sync(0xffffffffu, got)) {
+      if (lane == 0 && *s_stop_k > k) atomicOr(a.err, kErrLookbackTimeout);
+      return;
+    }
+    const uint32_t tile = meta[s].tile;
+    if (tile >= a.ntiles) return;
+    const uint32_t seg = meta[s].g.seg;
+    const bool first_of_seg = meta[s].g.has_seg && meta[s].g.first;
+    mbar_wait_or_flag(&aggb[s], par, a.err);
+    const uint32_t agg = s_agg[s];
+    const uint32_t epoch = *s_epoch;
     uint64_t excl = 0;
     if (tile == 0) {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+      write_header_warp(a.out, eb, sg, lane);
     } else {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
       excl = lookback_sum(a.status, tile, 0, epoch, a.err);
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
-    if (lane == 0) s_base = excl;
-#pragma unroll
-    for (int r = 0; r < ROUNDS; r++)
-#pragma unroll
-      for (int j = 0; j < 8; j++) vv[r][j] = s_stash[(r * 8 + j) * 32 + lane];
+    const uint64_t gpos = 4 + 8ull * sg.T + excl;
+    const bool fits = gpos + agg <= a.cap;
+    if (lane == 0) {
+      if (tile == a.ntiles - 1) *a.out_size = gpos + agg;
+      if (first_of_seg && fits) write_offset(a.out, seg, excl);
+      if (!fits) atomicOr(a.err, kErrCapacity);
+    }
+    mbar_wait_or_flag(&packed[s], par, a.err);
+    if (fits) warp_store_span(a.out + gpos, slots + (size_t)s * slot_bytes, agg, lane);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+}
+
+template <int LPB>
+__global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __grid_constant__ CompressArgs a,
+                                                                     uint32_t slot_bytes) {
+  constexpr int NS = kPipeSlots, NC = kPipeControl, ROUNDS = 4;
+  constexpr uint32_t L = 8 * LPB;
+  constexpr int BPR = 32 / LPB;
+  constexpr uint32_t TB = 8 * ROUNDS * BPR;
+  extern __shared__ __align__(16) uint8_t s_slots[];
+  __shared__ SlotMeta s_meta[NS];
+  __shared__ uint32_t s_agg[NS];
+  __shared__ uint32_t s_off[TB];
+  __shared__ uint8_t s_bc[TB];
+  __shared__ uint32_t s_part[8];
+  __shared__ uint32_t s_thr[36];
+  __shared__ uint32_t s_epoch;
+  __shared__ volatile uint32_t s_stop_k;
+  __shared__ __align__(8) uint64_t s_full[NS], s_aggb[NS], s_packed[NS], s_empty[NS];
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < 36) s_thr[threadIdx.x] = a.thr.thr[threadIdx.x];
+  if (threadIdx.x < NS) s_meta[threadIdx.x].tile = kStopTile;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; s++) {
+      mbar_init(&s_full[s], 1);
+      mbar_init(&s_aggb[s], 1);
+      mbar_init(&s_packed[s], 1);
+      mbar_init(&s_empty[s], 1);
+    }
+    s_stop_k = kStopTile;
   }
   __syncthreads();
-  const uint64_t gpos = 4 + 8ull * sg.T + s_base;
-  if (tile == a.ntiles - 1 && threadIdx.x == 0) *a.out_size = gpos + agg;
-  if (g.has_seg && g.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, g.seg, s_base);
-  if (gpos + agg > a.cap) {
-    if (threadIdx.x == 0) atomicOr(a.err, kErrCapacity);
+
+  const Segments& sg = a.seg;
+  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
+  if (warp == 8 + NC) {
+    if (lane == 0) pipe_producer<L, TB, NS>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
+    return;
+  }
+  if (warp >= 8) {
+    pipe_control<NS, NC>(warp - 8, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_packed, s_empty,
+                         &s_epoch, &s_stop_k, eb);
     return;
   }
 
-  // ---- pack into the (now free) buffer at the destination's 16-byte phase ----
-  const uint32_t align = (uint32_t)(((uintptr_t)a.out + gpos) & 15);
-  uint8_t* s_tile = s_buf + align;
-  const uint32_t front = seed ? 4u : 0u;
-  if (seed && threadIdx.x < 4) s_tile[threadIdx.x] = (uint8_t)((uint32_t)g.seed >> (8 * threadIdx.x));
-  if (full) {
+  // ---- compute warps ----
+  const float inv = __fdiv_rn(1.0f, eb);
+  const int sub = lane % LPB, grp = lane / LPB;
+  for (uint32_t k = 0;; k++) {
+    const int s = (int)(k % NS);
+    const uint32_t par = (k / NS) & 1;
+    mbar_wait_or_flag(&s_full[s], par, a.err);
+    const uint32_t tile = s_meta[s].tile;
+    if (tile >= a.ntiles) return;
+    const TileGeo g = s_meta[s].g;
+    uint8_t* slot = s_slots + (size_t)s * slot_bytes;
+    const float* sx = reinterpret_cast<const float*>(slot);
+    const bool seed = g.has_seg && g.first && g.hi > g.lo;
+    int32_t seedv = 0;
+    uint32_t flags = 0;
+    if (seed && threadIdx.x == 0) seedv = quantize(sx[g.d], inv, flags);  // x[lo] = window element 0
+
+    // ---- analysis: q, deltas, signs, block max, bit count, block size ----
+    uint32_t vv[ROUNDS][8];
+    uint32_t sgnb[ROUNDS];
+    const uint32_t sh = 1 + g.d;  // slot index of tile element 0
+    const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
+    const bool full = g.nblk == TB && g.nel == TB * L;  // every lane of every round holds 8 elements
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
       const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
-      const uint32_t bc = s_bc[bt];
-      uint8_t* dst = s_tile + front + s_off[bt];
-      if (sub == 0) dst[0] = (uint8_t)bc;
-      const uint32_t B = bc >> 3, rr = bc & 7;
-      constexpr uint32_t ns = L / 8;
-      if (bc) dst[1 + sub] = (uint8_t)sgnb[r];
-      if (__all_sync(0xffffffffu, B <= 1)) {
-        if (B) {
-          uint8_t* q8 = dst + 1 + ns + 8 * sub;
-#pragma unroll
-          for (int j = 0; j < 8; j++) q8[j] = (uint8_t)(vv[r][j] >> rr);
+      const uint32_t k0 = bt * L + 8 * sub;  // tile-relative first element of the lane
+      const uint32_t ml = (bt < g.nblk && k0 < g.nel) ? min(8u, g.nel - k0) : 0u;
+      float xv[8];
+      const uint32_t i = sh + k0;
+      if (full) {
+        const float4* q4 = reinterpret_cast<const float4*>(sx + (i & ~3u));
+        const float4 A = q4[0], B = q4[1];
+        if (ph == 0) {
+          xv[0] = A.x; xv[1] = A.y; xv[2] = A.z; xv[3] = A.w; xv[4] = B.x; xv[5] = B.y; xv[6] = B.z; xv[7] = B.w;
+        } else {
+          const float4 C = q4[2];
+          if (ph == 1) {
+            xv[0] = A.y; xv[1] = A.z; xv[2] = A.w; xv[3] = B.x; xv[4] = B.y; xv[5] = B.z; xv[6] = B.w; xv[7] = C.x;
+          } else if (ph == 2) {
+            xv[0] = A.z; xv[1] = A.w; xv[2] = B.x; xv[3] = B.y; xv[4] = B.z; xv[5] = B.w; xv[6] = C.x; xv[7] = C.y;
+          } else {
+            xv[0] = A.w; xv[1] = B.x; xv[2] = B.y; xv[3] = B.z; xv[4] = B.w; xv[5] = C.x; xv[6] = C.y; xv[7] = C.z;
+          }
         }
-      } else if (B) {
-        uint8_t* q8 = dst + 1 + ns + 8 * B * sub;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) xv[j] = (uint32_t)j < ml ? sx[i + j] : 0.0f;
+      }
+      int32_t q[8];
+      quantize8(xv, inv, q, flags);
+      int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
+      if (lane == 0) prev = quantize_lean(sx[i - 1], inv, flags);  // the element before the warp's round
+      uint32_t sb = 0, lmax = 0;
+      if (full) {
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-          const uint32_t h = vv[r][j] >> rr;
-          q8[j * B] = (uint8_t)h;
-          if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
-          if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
-          if (B > 3) q8[j * B + 3] = (uint8_t)(h >> 24);
+          const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);  // wrapping, as the compiled reference
+          prev = q[j];
+          const uint32_t v = (uint32_t)abs(d);  // |INT_MIN| is 2^31 as in the reference
+          sb = (sb << 1) + ((uint32_t)d >> 31);
+          lmax = max(lmax, v);
+          vv[r][j] = v;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int32_t d = (int32_t)((uint32_t)q[j] - (uint32_t)prev);
+          prev = q[j];
+          const bool valid = (uint32_t)j < ml;
+          const uint32_t v = valid ? (uint32_t)abs(d) : 0u;
+          sb = (sb << 1) + (valid ? ((uint32_t)d >> 31) : 0u);
+          lmax = max(lmax, v);
+          vv[r][j] = v;
         }
       }
-      if (rr) {
-        const uint32_t mask = (1u << rr) - 1u;
-        uint32_t hi4 = 0, lo4 = 0;
+      sgnb[r] = sb;
 #pragma unroll
-        for (int j = 0; j < 4; j++) hi4 = (hi4 << rr) | (vv[r][j] & mask);
-#pragma unroll
-        for (int j = 4; j < 8; j++) lo4 = (lo4 << rr) | (vv[r][j] & mask);
-        // 8*rr bits, element 0 first, moved to the top of 64 bits
-        const uint64_t top = (((uint64_t)hi4 << (4 * rr)) | lo4) << (64 - 8 * rr);
-        const uint32_t th = (uint32_t)(top >> 32), tl = (uint32_t)top;
-        uint8_t* rp = dst + 1 + ns + B * L + rr * sub;
-        rp[0] = (uint8_t)(th >> 24);
-        if (rr > 1) rp[1] = (uint8_t)(th >> 16);
-        if (rr > 2) rp[2] = (uint8_t)(th >> 8);
-        if (rr > 3) rp[3] = (uint8_t)th;
-        if (rr > 4) rp[4] = (uint8_t)(tl >> 24);
-        if (rr > 5) rp[5] = (uint8_t)(tl >> 16);
-        if (rr > 6) rp[6] = (uint8_t)(tl >> 8);
+      for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+      if (sub == 0 && bt < g.nblk) {
+        uint32_t bc = 0;
+        if (lmax) {
+          const int kk = 32 - __clz(lmax);
+          bc = kk + (kk >= 21 && lmax >= s_thr[kk + 1] ? 1 : 0);
+        }
+        const uint32_t m = min(L, g.nel - bt * L);
+        s_bc[bt] = (uint8_t)bc;
+        s_off[bt] = block_bytes(m, bc);
       }
     }
-    flush_span_bulk(a.out + gpos, s_buf, align, agg);
-    return;
-  }
+    if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
+    compute_sync();  // block sizes complete; the input window is dead from here on
+
+    // ---- block offsets in the tile; publish the tile's byte count ----
+    const uint32_t front = seed ? 4u : 0u;
+    const uint32_t agg = compute_scan_excl(s_off, g.nblk, s_part) + front;
+    if (threadIdx.x == 0) {
+      s_agg[s] = agg;
+      st_release_u64(a.status + tile, make_status(s_epoch, tile == 0 ? kFlagInclusive : kFlagAggregate, agg));
+      mbar_arrive(&s_aggb[s]);
+    }
+
+    // ---- pack into the slot from offset 0 ----
+    uint8_t* s_tile = slot;
+    if (seed && threadIdx.x == 0) {
+      s_tile[0] = (uint8_t)seedv;
+      s_tile[1] = (uint8_t)((uint32_t)seedv >> 8);
+      s_tile[2] = (uint8_t)((uint32_t)seedv >> 16);
+      s_tile[3] = (uint8_t)((uint32_t)seedv >> 24);
+    }
+    if (full) {
 #pragma unroll
-  for (int r = 0; r < ROUNDS; r++) {
-    const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
-    if (bt >= g.nblk) continue;
-    const uint32_t m = min(L, g.nel - bt * L);
-    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
-    const uint32_t bc = s_bc[bt];
-    uint8_t* dst = s_tile + front + s_off[bt];
-    if (sub == 0) dst[0] = (uint8_t)bc;
-    if (bc == 0 || ml == 0) continue;
-    const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
-    dst[1 + sub] = (uint8_t)sgnb[r];  // sign bits, szp_TypeManager.cc:820-844
-    if (B) {  // byte planes, szp_TypeManager.cc:36-52
-      uint8_t* q8 = dst + 1 + ns + 8 * B * sub;
+      for (int r = 0; r < ROUNDS; r++) {
+        const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
+        const uint32_t bc = s_bc[bt];
+        uint8_t* dst = s_tile + front + s_off[bt];
+        if (sub == 0) dst[0] = (uint8_t)bc;
+        const uint32_t B = bc >> 3, rr = bc & 7;
+        constexpr uint32_t ns = L / 8;
+        if (bc) dst[1 + sub] = (uint8_t)sgnb[r];
+        if (__all_sync(0xffffffffu, B <= 1)) {
+          if (B) {
+            uint8_t* q8 = dst + 1 + ns + 8 * sub;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        if ((uint32_t)j < ml) {
-          const uint32_t h = vv[r][j] >> rr;
-          q8[j * B] = (uint8_t)h;
-          if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
-          if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
-          if (B > 3) q8[j * B + 3] = (uint8_t)(h >> 24);
+            for (int j = 0; j < 8; j++) q8[j] = (uint8_t)(vv[r][j] >> rr);
+          }
+        } else if (B) {
+          uint8_t* q8 = dst + 1 + ns + 8 * B * sub;
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const uint32_t h = vv[r][j] >> rr;
+            q8[j * B] = (uint8_t)h;
+            if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
+            if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
+            if (B > 3) q8[j * B + 3] = (uint8_t)(h >> 24);
+          }
+        }
+        if (rr) {
+          const uint32_t mask = (1u << rr) - 1u;
+          uint32_t hi4 = 0, lo4 = 0;
+#pragma unroll
+          for (int j = 0; j < 4; j++) hi4 = (hi4 << rr) | (vv[r][j] & mask);
+#pragma unroll
+          for (int j = 4; j < 8; j++) lo4 = (lo4 << rr) | (vv[r][j] & mask);
+          // 8*rr bits, element 0 first, moved to the top of 64 bits
+          const uint64_t top = (((uint64_t)hi4 << (4 * rr)) | lo4) << (64 - 8 * rr);
+          const uint32_t th = (uint32_t)(top >> 32), tl = (uint32_t)top;
+          uint8_t* rp = dst + 1 + ns + B * L + rr * sub;
+          rp[0] = (uint8_t)(th >> 24);
+          if (rr > 1) rp[1] = (uint8_t)(th >> 16);
+          if (rr > 2) rp[2] = (uint8_t)(th >> 8);
+          if (rr > 3) rp[3] = (uint8_t)th;
+          if (rr > 4) rp[4] = (uint8_t)(tl >> 24);
+          if (rr > 5) rp[5] = (uint8_t)(tl >> 16);
+          if (rr > 6) rp[6] = (uint8_t)(tl >> 8);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) {
+        const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
+        if (bt >= g.nblk) continue;
+        const uint32_t m = min(L, g.nel - bt * L);
+        const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+        const uint32_t bc = s_bc[bt];
+        uint8_t* dst = s_tile + front + s_off[bt];
+        if (sub == 0) dst[0] = (uint8_t)bc;
+        if (bc == 0 || ml == 0) continue;
+        const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
+        dst[1 + sub] = (uint8_t)sgnb[r];  // sign bits, szp_TypeManager.cc:820-844
+        if (B) {  // byte planes, szp_TypeManager.cc:36-52
+          uint8_t* q8 = dst + 1 + ns + 8 * B * sub;
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            if ((uint32_t)j < ml) {
+              const uint32_t h = vv[r][j] >> rr;
+              q8[j * B] = (uint8_t)h;
+              if (B > 1) q8[j * B + 1] = (uint8_t)(h >> 8);
+              if (B > 2) q8[j * B + 2] = (uint8_t)(h >> 16);
+              if (B > 3) q8[j * B + 3] = (uint8_t)(h >> 24);
+            }
+          }
+        }
+        if (rr) {  // remainder bits, MSB first, szp_TypeManager.cc:122-434
+          const uint32_t mask = (1u << rr) - 1u;
+          uint32_t hi4 = 0, lo4 = 0;  // elements 0-3 and 4-7, 4*rr bits each
+#pragma unroll
+          for (int j = 0; j < 4; j++) hi4 = (hi4 << rr) | ((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
+#pragma unroll
+          for (int j = 4; j < 8; j++) lo4 = (lo4 << rr) | ((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
+          const uint64_t acc = ((uint64_t)hi4 << (4 * rr)) | lo4;  // 8*rr bits, element 0 on top
+          uint8_t* rp = dst + 1 + ns + B * m + rr * sub;
+          const uint32_t nb = (ml * rr + 7) >> 3;
+          const uint32_t top = 8 * rr - 8;
+#pragma unroll
+          for (uint32_t kk = 0; kk < 7; kk++)
+            if (kk < nb) rp[kk] = (uint8_t)(acc >> (top - 8 * kk));
         }
       }
     }
-    if (rr) {  // remainder bits, MSB first, szp_TypeManager.cc:122-434
-      const uint32_t mask = (1u << rr) - 1u;
-      uint32_t hi4 = 0, lo4 = 0;  // elements 0-3 and 4-7, 4*rr bits each
-#pragma unroll
-      for (int j = 0; j < 4; j++) hi4 = (hi4 << rr) | ((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
-#pragma unroll
-      for (int j = 4; j < 8; j++) lo4 = (lo4 << rr) | ((uint32_t)j < ml ? (vv[r][j] & mask) : 0u);
-      const uint64_t acc = ((uint64_t)hi4 << (4 * rr)) | lo4;  // 8*rr bits, element 0 on top
-      uint8_t* rp = dst + 1 + ns + B * m + rr * sub;
-      const uint32_t nb = (ml * rr + 7) >> 3;
-      const uint32_t top = 8 * rr - 8;
-#pragma unroll
-      for (uint32_t k = 0; k < 7; k++)
-        if (k < nb) rp[k] = (uint8_t)(acc >> (top - 8 * k));
-    }
+    compute_sync();  // the slot is packed; s_off and s_bc are free for the next tile
+    if (threadIdx.x == 0) mbar_arrive(&s_packed[s]);
   }
-  flush_span_bulk(a.out + gpos, s_buf, align, agg);
 }
 
 // ---------------------------------------------------------------------------
@@ -895,12 +1069,39 @@ size_t compress_smem_bytes(uint32_t L, uint32_t tb) {
   return out > in ? out : in;
 }
 
+// Bytes of one pipeline slot: the packed tile (read 16 bytes past its end by
+// the shifted copy) or the 16-byte-aligned input window it replaces.
+static uint32_t pipe_slot_bytes(uint32_t L, uint32_t tb) {
+  const size_t out = 4 + (size_t)tb * max_block_bytes(L) + 32;
+  const size_t in = 4 * ((size_t)tb * L + 1) + 32;
+  return (uint32_t)(((out > in ? out : in) + 15) & ~(size_t)15);
+}
+
 template <int LPB>
-static cudaError_t launch_lanes(const CompressArgs& a, size_t smem, cudaStream_t st) {
-  auto k = compress_fm1_tma<LPB>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
+  auto k = compress_fm1_pipe<LPB>;
+  const uint32_t slot = pipe_slot_bytes(a.seg.L, a.tb);
+  const size_t smem = (size_t)kPipeSlots * slot;
+  // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
+  static std::atomic<uint64_t> s_cache{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  k<<<a.ntiles, 256, smem, st>>>(a);
+  uint64_t c = s_cache.load(std::memory_order_relaxed);
+  if ((c >> 32) != (uint64_t)dev + 1) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int occ = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kPipeThreads, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    c = ((uint64_t)dev + 1) << 32 | (uint32_t)((occ < 1 ? 1 : occ) * sms);
+    s_cache.store(c, std::memory_order_relaxed);
+  }
+  const uint32_t s_grid = (uint32_t)c;
+  const uint32_t grid = a.ntiles < s_grid ? a.ntiles : s_grid;
+  k<<<grid, kPipeThreads, smem, st>>>(a, slot);
   return cudaGetLastError();
 }
 
@@ -908,12 +1109,12 @@ cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st) {
   size_t smem = compress_smem_bytes(a.seg.L, a.tb);
   if (!fm2) {
     switch (lanes_per_block(a.seg.L)) {
-      case 1: return launch_lanes<1>(a, smem, st);
-      case 2: return launch_lanes<2>(a, smem, st);
-      case 4: return launch_lanes<4>(a, smem, st);
-      case 8: return launch_lanes<8>(a, smem, st);
-      case 16: return launch_lanes<16>(a, smem, st);
-      case 32: return launch_lanes<32>(a, smem, st);
+      case 1: return launch_lanes<1>(a, st);
+      case 2: return launch_lanes<2>(a, st);
+      case 4: return launch_lanes<4>(a, st);
+      case 8: return launch_lanes<8>(a, st);
+      case 16: return launch_lanes<16>(a, st);
+      case 32: return launch_lanes<32>(a, st);
       default: break;
     }
     auto k = compress_generic<kGenWarps, false>;
