@@ -17,6 +17,7 @@
 
 #include "szp_device.cuh"
 #include "szp_kernels.h"
+#include "szp_pipe.cuh"
 #include "szp_tma.cuh"
 
 namespace szp {
@@ -280,23 +281,11 @@ struct TileGeo {
 // ---------------------------------------------------------------------------
 constexpr int kPipeSlots = 3, kPipeControl = 2;
 constexpr int kPipeThreads = (8 + kPipeControl + 1) * 32;
-constexpr uint32_t kStopTile = 0xFFFFFFFFu;
-constexpr uint32_t kWaitLimit = 1u << 24;
 
 struct SlotMeta {
   TileGeo g;
   uint32_t tile;  // kStopTile: no more tiles for this CTA
 };
-
-__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
-// Waits for an mbarrier phase; on timeout flags the launch and waits once more.
-__device__ __forceinline__ void mbar_wait_or_flag(uint64_t* bar, uint32_t parity, uint32_t* err) {
-  if (!mbar_wait_bounded(bar, parity, kWaitLimit)) {
-    atomicOr(err, kErrLookbackTimeout);
-    mbar_wait_bounded(bar, parity, kWaitLimit);
-  }
-}
 
 // Exclusive scan of n (<= 1024) values in shared memory by the 256 compute
 // threads; returns the total.  s_part needs 8 words.
@@ -400,13 +389,7 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
   for (uint32_t k = 0;; k++) {
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
-    const uint32_t tile = atomicAdd(&a.ls->ticket, 1u);
-    if (tile == a.ntiles + gridDim.x - 1) {
-      // the last draw of the launch: every CTA has read the epoch
-      a.ls->ticket = 0;
-      __threadfence();
-      atomicAdd(&a.ls->epoch, 1u);
-    }
+    const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
     SlotMeta& m = meta[s];
     if (tile >= a.ntiles) {
       m.tile = kStopTile;
@@ -473,15 +456,7 @@ __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const
   for (uint32_t k = (uint32_t)c;; k += NC) {
     const int s = (int)(k % NS);
     const uint32_t par = (k / NS) & 1;
-    bool got = false;
-    for (uint32_t i = 0; i < kWaitLimit; i++) {
-      if ((got = mbar_try_wait(&full[s], par))) break;
-      if (*s_stop_k <= k) break;
-    }
-    if (!__all_sync(0xffffffffu, got)) {
-      if (lane == 0 && *s_stop_k > k) atomicOr(a.err, kErrLookbackTimeout);
-      return;
-    }
+    if (!control_wait_full(&full[s], par, k, s_stop_k, a.err)) return;
     const uint32_t tile = meta[s].tile;
     if (tile >= a.ntiles) return;
     const uint32_t seg = meta[s].g.seg;
@@ -542,7 +517,6 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
   }
   __syncthreads();
 
-  const Segments& sg = a.seg;
   const float eb = a.eb_dev ? *a.eb_dev : a.eb;
   if (warp == 8 + NC) {
     if (lane == 0) pipe_producer<L, TB, NS>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);

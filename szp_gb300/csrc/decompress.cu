@@ -26,8 +26,11 @@
 //                 each (sign byte, byte planes, remainder bits are byte-aligned
 //                 per 8 elements), prefix-add (fastmode1: warp/CTA scans and a
 //                 look-back over the tiles of a segment) and dequantize.
+#include <atomic>
+
 #include "szp_device.cuh"
 #include "szp_kernels.h"
+#include "szp_pipe.cuh"
 #include "szp_tma.cuh"
 
 namespace szp {
@@ -299,48 +302,57 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
   ch.fm2 = FM2;
 
   // ---- speculative walk of each thread's chunk ----
+  // One flat loop advances every lane by one header per iteration, so a warp
+  // stays converged and costs the longest walk of its lanes (nested restart
+  // loops would run the lanes one after another).  A lane's chain starts at
+  // `anchor`; the first position >= cS is the chunk's entry, headers in
+  // [cS, cE) are counted, and the first position >= cE is its exit.  A chain
+  // that meets an invalid header restarts one byte later.
   const uint32_t nactive = (scE - scS + C - 1) / C;
   const uint32_t cS = scS + tid * C, cE = min(cS + C, scE);
   uint32_t h = kPosEnd, x = kPosEnd, k = 0;
-  if ((uint32_t)tid < nactive) {
-    if (j == 0 && tid == 0) {
-      h = 0;  // a segment's block region starts with a header
-      k = ch.walk(0, cE, &x);
-    } else {
-      // the first chunk of a CTA is checked across CTAs (costly to repair), the
-      // others against their neighbour here (cheap): shorter overlap for those
-      const uint32_t W = tid == 0 ? W0 : min(W0, max(512u, 4 * a.maxsz));
-      const uint32_t w0 = cS > st0 + W ? cS - W : st0;
-      uint32_t anchor = w0, budget = 4 * (W + C);
+  {
+    const bool known = j == 0 && tid == 0;  // a segment's block region starts with a header
+    // the first chunk of a CTA is checked across CTAs (costly to repair), the
+    // others against their neighbour here (cheap): shorter overlap for those
+    const uint32_t W = tid == 0 ? W0 : min(W0, max(512u, 4 * a.maxsz));
+    uint32_t anchor = known ? 0u : (cS > st0 + W ? cS - W : st0);
+    uint32_t pos = anchor, entry = anchor >= cS ? anchor : kPosDead, cnt = 0;
+    uint32_t budget = 4 * (W + C);
+    bool done = (uint32_t)tid >= nactive;
+    if (!done) {
       h = kPosDead;
       x = kPosDead;
-      while (anchor < cE && budget) {
-        uint32_t p = anchor;
-        bool alive = true;
-        while (p < cS && budget) {
+    }
+    while (__any_sync(0xffffffffu, !done)) {
+      if (!done) {
+        if (pos >= cE) {
+          h = entry >= rlen ? kPosEnd : entry;
+          x = pos >= rlen ? kPosEnd : pos;
+          k = cnt;
+          done = true;
+        } else if (budget == 0) {
+          done = true;
+        } else {
           budget--;
-          uint32_t sz = ch.step(p);
-          if (!sz) {
-            alive = false;
-            break;
+          const uint32_t sz = ch.step(pos);
+          if (sz) {
+            cnt += pos >= cS ? 1u : 0u;
+            pos += sz;
+            if (entry == kPosDead && pos >= cS) entry = pos;
+          } else if (!known && anchor + 1 < cE) {
+            anchor++;
+            pos = anchor;
+            entry = anchor >= cS ? anchor : kPosDead;
+            cnt = 0;
+          } else {
+            if (known) {
+              h = 0;
+              k = cnt;  // x stays kPosDead: the true chain is broken
+            }
+            done = true;
           }
-          p += sz;
         }
-        if (!alive) {
-          anchor++;
-          continue;
-        }
-        uint32_t ex;
-        uint32_t kk = ch.walk(p, cE, &ex);
-        budget = budget > kk ? budget - kk : 0u;
-        if (ex == kPosDead) {
-          anchor++;
-          continue;
-        }
-        h = p >= rlen ? kPosEnd : p;
-        x = ex;
-        k = kk;
-        break;
       }
     }
   }
@@ -639,201 +651,352 @@ __device__ __forceinline__ void store8(float* __restrict__ y, uint64_t s, uint32
   }
 }
 
-// fastmode1, blockSize L = 8*LPB: LPB lanes per block, 8 elements per lane
-// (the byte layout of 8 elements is self-contained, see compress.cu).
-template <int LPB, int ROUNDS>
-__global__ void __launch_bounds__(256) decode_fm1_lanes(const __grid_constant__ DecArgs a) {
-  constexpr int WARPS = 8;
+constexpr int kDecWarps = 8;
+constexpr int kDecRounds = 4;
+
+// ---------------------------------------------------------------------------
+// fastmode1 decode, blockSize L = 8*LPB, as a persistent, warp-specialised
+// pipeline (the mirror of the compressor's):
+//   producer  draws tile tickets; stages the tile's block offsets and its
+//             stream span in a slot by bulk copy
+//   compute   unpacks the deltas (LPB lanes per block, 8 elements per lane:
+//             the byte layout of 8 elements is self-contained), scans them
+//             inside the tile and stages the tile-relative prefix sums (int32)
+//             in the slot, over the span they came from
+//   control   looks back for the tile's base (the segment's seed plus the
+//             deltas of the tiles before it, szpd_float.cc:76-118), adds it,
+//             dequantizes and stores the tile with 16-byte stores
+// ---------------------------------------------------------------------------
+constexpr int kDecSlots = 3, kDecControl = 2;
+constexpr int kDecPipeThreads = (8 + kDecControl + 1) * 32;
+
+struct DecSlot {
+  uint32_t tile;     // kStopTile: none
+  uint32_t seg;
+  uint32_t nblk;     // blocks in the tile
+  uint32_t nel;      // elements of those blocks
+  uint64_t e0;       // first element of the tile (its segment's lo + 1 + blk0*L)
+  uint32_t first;    // first tile of its segment
+  uint32_t seed;     // q of the segment's element lo (first tile only)
+  uint32_t span0;    // region offset of span byte 0
+  uint32_t spanlen;  // staged span bytes
+  uint32_t sofs;     // slot byte offset of span byte 0
+  uint32_t pofs;     // slot word offset of the tile's first block offset
+};
+
+// Bytes of the block-offset area at the front of a slot.
+__host__ __device__ constexpr uint32_t dec_pos_bytes(uint32_t tb) { return 4 * tb + 32; }
+
+template <uint32_t L, uint32_t TB, int NS>
+__device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, uint32_t slot_bytes, DecSlot* meta,
+                                             uint64_t* full, uint64_t* empty, uint32_t* s_epoch,
+                                             volatile uint32_t* s_stop_k) {
+  const Segments& sg = a.seg;
+  constexpr uint32_t PB = dec_pos_bytes(TB);
+  *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
+  __threadfence();
+  const bool bad = a.plan->bad != 0;
+  for (uint32_t k = 0;;) {
+    const int s = (int)(k % NS);
+    if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
+    const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
+    DecSlot& m = meta[s];
+    if (tile >= a.ntiles) {
+      m.tile = kStopTile;
+      *s_stop_k = k;
+      mbar_arrive(&full[s]);
+      return;
+    }
+    const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, false);
+    // nothing to write: a failed plan, an empty segment, a tile past its segment's blocks
+    if (bad || !dt.any || (dt.nblk == 0 && !dt.first)) continue;  // the slot stays free
+    const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
+    const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
+    const uint32_t rlen = (uint32_t)(R1 - R0);
+    uint8_t* slot = slots + (size_t)s * slot_bytes;
+    m.seg = dt.seg;
+    m.nblk = dt.nblk;
+    m.first = dt.first;
+    m.e0 = lo + 1 + dt.blk0 * L;
+    m.nel = dt.nblk ? (uint32_t)min((uint64_t)dt.nblk * L, hi - m.e0) : 0u;
+    m.seed = 0;
+    if (dt.first) {
+      const uint8_t* sp = a.in + R0 - 4;  // the segment's 4-byte seed precedes its blocks
+      m.seed = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
+               ((uint32_t)__ldg(sp + 3) << 24);
+    }
+    m.span0 = 0;
+    m.spanlen = 0;
+    m.sofs = PB;
+    m.pofs = 0;
+    uint32_t tx = 0;
+    uintptr_t p0 = 0, p1 = 0, q0 = 0, q1 = 0;
+    if (dt.nblk) {
+      const uint32_t* bp = a.blkpos + seg_block_base(sg, dt.seg, false) + dt.blk0;
+      const uint32_t s0 = min(__ldg(bp), rlen);
+      uint32_t s1 = (uint32_t)min((uint64_t)rlen, (uint64_t)__ldg(bp + dt.nblk - 1) + a.maxsz);
+      if (s1 < s0) s1 = s0;
+      m.span0 = s0;
+      m.spanlen = min(s1 - s0, TB * a.maxsz);  // bounds a corrupt index to the slot
+      p0 = (uintptr_t)bp;
+      p1 = p0 + 4ull * dt.nblk;
+      m.pofs = (uint32_t)((p0 & 15) >> 2);
+      tx += stage_range(slot, reinterpret_cast<const uint8_t*>(a.blkpos), 4 * a.nblk_total, p0, p1);
+      q0 = (uintptr_t)(a.in + R0 + s0);
+      q1 = q0 + m.spanlen;
+      m.sofs = PB + (uint32_t)(q0 & 15);
+      tx += stage_range(slot + PB, a.in, a.len, q0, q1);
+    }
+    m.tile = tile;
+    if (tx) {
+      fence_async_smem();
+      mbar_arrive_expect_tx(&full[s], tx);
+      stage_range_issue(slot, reinterpret_cast<const uint8_t*>(a.blkpos), 4 * a.nblk_total, p0, p1, &full[s]);
+      stage_range_issue(slot + PB, a.in, a.len, q0, q1, &full[s]);
+    } else {
+      mbar_arrive(&full[s]);
+    }
+    k++;
+  }
+}
+
+// One warp: y[e] = dequant(base + stage[e - e0]) for the tile's nel elements
+// starting at dst = y + e0; 16-byte stores for the aligned middle, the words
+// picked from two aligned shared-memory lines when dst is not 16-byte aligned.
+// stage is 16-byte aligned and readable for nel + 4 words.
+__device__ __forceinline__ void warp_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
+                                                   uint32_t nel, uint32_t base, float eb, bool ebsp, int lane) {
+  if (nel == 0) return;
+  const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 2) & 3);
+  float* g0 = dst - ph;  // 16-byte aligned
+  const uint32_t end = ph + nel;
+  const uint32_t c0 = (ph + 3) >> 2, c1 = end >> 2;  // whole float4 chunks [c0, c1)
+  if (c0 >= c1) {
+    for (uint32_t i = ph + lane; i < end; i += 32) g0[i] = dequant(base + stage[i - ph], eb, ebsp);
+    return;
+  }
+  if ((uint32_t)lane < 4 * c0 - ph) g0[ph + lane] = dequant(base + stage[lane], eb, ebsp);
+  if ((uint32_t)lane < end - 4 * c1) g0[4 * c1 + lane] = dequant(base + stage[4 * c1 + lane - ph], eb, ebsp);
+  const uint4* s4 = reinterpret_cast<const uint4*>(stage);
+  for (uint32_t c = c0 + lane; c < c1; c += 32) {
+    uint4 w;
+    if (ph == 0) {
+      w = s4[c];
+    } else {
+      const uint4 u = s4[c - 1], v = s4[c];  // stage words [4c-4, 4c+4); chunk c wants [4c-ph, 4c-ph+4)
+      if (ph == 1) w = make_uint4(u.w, v.x, v.y, v.z);
+      else if (ph == 2) w = make_uint4(u.z, u.w, v.x, v.y);
+      else w = make_uint4(u.y, u.z, u.w, v.x);
+    }
+    float4 o;
+    o.x = dequant(base + w.x, eb, ebsp);
+    o.y = dequant(base + w.y, eb, ebsp);
+    o.z = dequant(base + w.z, eb, ebsp);
+    o.w = dequant(base + w.w, eb, ebsp);
+    reinterpret_cast<float4*>(g0)[c] = o;
+  }
+}
+
+template <int NS, int NC, uint32_t TB>
+__device__ __forceinline__ void dec_control(int c, const DecArgs& a, const uint8_t* slots, uint32_t slot_bytes,
+                                            const DecSlot* meta, const uint32_t* s_agg, uint64_t* full,
+                                            uint64_t* aggb, uint64_t* staged, uint64_t* empty,
+                                            const uint32_t* s_epoch, const volatile uint32_t* s_stop_k, float eb,
+                                            bool ebsp) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t k = (uint32_t)c;; k += NC) {
+    const int s = (int)(k % NS);
+    const uint32_t par = (k / NS) & 1;
+    if (!control_wait_full(&full[s], par, k, s_stop_k, a.err)) return;
+    const uint32_t tile = meta[s].tile;
+    if (tile >= a.ntiles) return;
+    const uint32_t seg = meta[s].seg, nel = meta[s].nel;
+    const bool first = meta[s].first;
+    const uint64_t e0 = meta[s].e0;
+    const uint32_t seed = meta[s].seed;
+    mbar_wait_or_flag(&aggb[s], par, a.err);
+    const uint32_t agg = s_agg[s];
+    const uint32_t epoch = *s_epoch;
+    uint32_t base;
+    if (first) {
+      base = seed;
+      if (lane == 0) a.y[e0 - 1] = dequant(seed, eb, ebsp);
+    } else {
+      const uint32_t first_tile = a.tiles_per_seg ? seg * a.tiles_per_seg : 0;
+      base = (uint32_t)lookback_sum(a.status, tile, first_tile, epoch, a.err);
+      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(base + agg)));
+    }
+    mbar_wait_or_flag(&staged[s], par, a.err);
+    const uint32_t* stage = reinterpret_cast<const uint32_t*>(slots + (size_t)s * slot_bytes + dec_pos_bytes(TB));
+    warp_dequant_store(a.y + e0, stage, nel, base, eb, ebsp, lane);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+}
+
+template <int LPB>
+__global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __grid_constant__ DecArgs a,
+                                                                      uint32_t slot_bytes) {
+  constexpr int NS = kDecSlots, NC = kDecControl, ROUNDS = kDecRounds, WARPS = 8;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
   constexpr uint32_t TB = WARPS * ROUNDS * BPR;
-  extern __shared__ __align__(16) uint8_t s_span[];
-  __shared__ uint32_t s_tk[2];
+  constexpr uint32_t PB = dec_pos_bytes(TB);
+  extern __shared__ __align__(16) uint8_t s_slots[];
+  __shared__ DecSlot s_meta[NS];
+  __shared__ uint32_t s_agg[NS];
   __shared__ uint32_t s_w[WARPS + 1];
-  __shared__ uint32_t s_base;
-  __shared__ uint32_t s_geo[2];  // span start (region offset), span length
-  __shared__ __align__(8) uint64_t s_bar;
-  __shared__ uint32_t s_stash[ROUNDS * 8 * 32];
-  uint32_t tile, epoch;
-  draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
-  if (a.plan->bad) return;
+  __shared__ uint32_t s_epoch;
+  __shared__ volatile uint32_t s_stop_k;
+  __shared__ __align__(8) uint64_t s_full[NS], s_aggb[NS], s_staged[NS], s_empty[NS];
+
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int sub = lane % LPB, grp = lane / LPB;
-  const Segments sg = a.seg;
-  const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, false);
-  if (!dt.any) return;
+  if (threadIdx.x < NS) s_meta[threadIdx.x].tile = kStopTile;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; s++) {
+      mbar_init(&s_full[s], 1);
+      mbar_init(&s_aggb[s], 1);
+      mbar_init(&s_staged[s], 1);
+      mbar_init(&s_empty[s], 1);
+    }
+    s_stop_k = kStopTile;
+  }
+  __syncthreads();
   const float eb = a.plan->eb;
   const bool ebsp = !isfinite(eb);
-  const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
-  const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
-  const uint8_t* __restrict__ in = a.in;
-  const uint32_t* __restrict__ bp = a.blkpos + seg_block_base(sg, dt.seg, false) + dt.blk0;
-
-  // ---- stage the tile's stream span in shared memory ----
-  const uint32_t maxsz = a.maxsz;
-  const uint32_t rlen = (uint32_t)(R1 - R0);
-  uint32_t align = 0;
-  if (threadIdx.x == 0) {
-    uint32_t s0 = 0, s1 = 0;
-    if (dt.nblk) {
-      s0 = min(__ldg(bp), rlen);
-      s1 = (uint32_t)min((uint64_t)rlen, (uint64_t)__ldg(bp + dt.nblk - 1) + maxsz);
-      if (s1 < s0) s1 = s0;
-    }
-    s_geo[0] = s0;
-    s_geo[1] = min(s1 - s0, TB * maxsz);  // bounds a corrupt index to the buffer
-    mbar_init(&s_bar, 1);
+  if (warp == WARPS + NC) {
+    if (lane == 0) dec_producer<L, TB, NS>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
+    return;
   }
-  __syncthreads();
-  const uint32_t span0 = s_geo[0], spanlen = s_geo[1];
-  const uint8_t* gspan = in + R0 + span0;
-  align = (uint32_t)((uintptr_t)gspan & 15);
-  {
-    const uint32_t end = align + spanlen;
-    const uint32_t i0 = (align + 15) & ~15u, i1 = end & ~15u;
-    const uint8_t* g0 = gspan - align;
-    bool bulk = i1 > i0;
-    if (threadIdx.x == 0 && bulk) {
-      mbar_arrive_expect_tx(&s_bar, i1 - i0);
-      bulk_load(s_span + i0, g0 + i0, i1 - i0, &s_bar);
-    }
-    if (bulk) {
-      for (uint32_t b = align + threadIdx.x; b < i0; b += blockDim.x) s_span[b] = __ldg(g0 + b);
-      for (uint32_t b = i1 + threadIdx.x; b < end; b += blockDim.x) s_span[b] = __ldg(g0 + b);
-    } else {
-      for (uint32_t b = align + threadIdx.x; b < end; b += blockDim.x) s_span[b] = __ldg(g0 + b);
-    }
-    bool ok = !bulk || mbar_wait_bounded(&s_bar, 0, 1u << 22);
-    if (!ok) {
-      atomicOr(a.err, kErrLookbackTimeout);
-      mbar_wait_bounded(&s_bar, 0, 1u << 22);  // let the copy land before the CTA leaves
-    }
-    __syncthreads();
+  if (warp >= WARPS) {
+    dec_control<NS, NC, TB>(warp - WARPS, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_staged, s_empty,
+                            &s_epoch, &s_stop_k, eb, ebsp);
+    return;
   }
-  const uint8_t* sp = s_span + align;  // span byte i at sp[i]
 
-  // ---- unpack deltas and prefix-add inside each lane ----
+  // ---- compute warps ----
+  const int sub = lane % LPB, grp = lane / LPB;
   const uint32_t wfirst = (uint32_t)warp * ROUNDS * BPR;
-  uint32_t pre[ROUNDS][8];
-  uint32_t lex[ROUNDS], rbase[ROUNDS];
-  uint32_t wtot = 0;
-  bool corrupt = false;
+  for (uint32_t k = 0;; k++) {
+    const int s = (int)(k % NS);
+    const uint32_t par = (k / NS) & 1;
+    mbar_wait_or_flag(&s_full[s], par, a.err);
+    const uint32_t tile = s_meta[s].tile;
+    if (tile >= a.ntiles) return;
+    const uint32_t nblk = s_meta[s].nblk, nel = s_meta[s].nel, span0 = s_meta[s].span0;
+    const uint32_t spanlen = s_meta[s].spanlen;
+    uint8_t* slot = s_slots + (size_t)s * slot_bytes;
+    const uint8_t* sp = slot + s_meta[s].sofs;  // span byte i at sp[i]
+    const uint32_t* bpos = reinterpret_cast<const uint32_t*>(slot) + s_meta[s].pofs;
+
+    // ---- unpack deltas and prefix-add inside each lane ----
+    uint32_t pre[ROUNDS][8];
+    uint32_t lex[ROUNDS], rbase[ROUNDS];
+    uint32_t wtot = 0;
+    bool corrupt = false;
 #pragma unroll
-  for (int r = 0; r < ROUNDS; r++) {
-    const uint32_t bt = wfirst + r * BPR + grp;
-    const uint64_t bs = lo + 1 + (dt.blk0 + bt) * L;
-    const uint32_t m = bt < dt.nblk ? (uint32_t)min((uint64_t)L, hi - bs) : 0u;
-    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
-    uint32_t d[8];
+    for (int r = 0; r < ROUNDS; r++) {
+      const uint32_t bt = wfirst + r * BPR + grp;
+      const uint32_t m = bt < nblk ? min(L, nel - bt * L) : 0u;
+      const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+      uint32_t d[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) d[j] = 0;
-    if (m) {
-      const uint32_t off = __ldg(bp + bt) - span0;
-      uint32_t bc = off < spanlen ? sp[off] : 255u;
-      if (bc > 33 || off + block_bytes(m, bc) > spanlen) {
-        corrupt = true;
-        bc = 0;
-      }
-      if (bc && ml) {
-        const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
-        const uint32_t sb = sp[off + 1 + sub];
-        uint32_t hv[8];
+      for (int j = 0; j < 8; j++) d[j] = 0;
+      if (m) {
+        const uint32_t off = bpos[bt] - span0;
+        uint32_t bc = off < spanlen ? sp[off] : 255u;
+        if (bc > 33 || off + block_bytes(m, bc) > spanlen) {
+          corrupt = true;
+          bc = 0;
+        }
+        if (bc && ml) {
+          const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
+          const uint32_t sb = sp[off + 1 + sub];  // sign bits, szp_TypeManager.cc:820-844
+          uint32_t hv[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) hv[j] = 0;
-        if (B) {
-          const uint8_t* q8 = sp + off + 1 + ns + 8 * B * sub;
+          for (int j = 0; j < 8; j++) hv[j] = 0;
+          if (B) {  // byte planes, szp_TypeManager.cc:36-52
+            const uint8_t* q8 = sp + off + 1 + ns + 8 * B * sub;
 #pragma unroll
-          for (int j = 0; j < 8; j++) {
-            if ((uint32_t)j < ml) {
-              uint32_t h = q8[j * B];
-              if (B > 1) h |= (uint32_t)q8[j * B + 1] << 8;
-              if (B > 2) h |= (uint32_t)q8[j * B + 2] << 16;
-              if (B > 3) h |= (uint32_t)q8[j * B + 3] << 24;
-              hv[j] = h << rr;
+            for (int j = 0; j < 8; j++) {
+              if ((uint32_t)j < ml) {
+                uint32_t h = q8[j * B];
+                if (B > 1) h |= (uint32_t)q8[j * B + 1] << 8;
+                if (B > 2) h |= (uint32_t)q8[j * B + 2] << 16;
+                if (B > 3) h |= (uint32_t)q8[j * B + 3] << 24;
+                hv[j] = h << rr;
+              }
             }
           }
-        }
-        if (rr) {
-          const uint8_t* rp = sp + off + 1 + ns + B * m + rr * sub;
-          const uint32_t nb = (ml * rr + 7) >> 3;
-          uint64_t acc = 0;
+          if (rr) {  // remainder bits, MSB first, szp_TypeManager.cc:122-434
+            const uint8_t* rp = sp + off + 1 + ns + B * m + rr * sub;
+            const uint32_t nb = (ml * rr + 7) >> 3;
+            uint64_t acc = 0;
 #pragma unroll
-          for (uint32_t k = 0; k < 7; k++) acc = (acc << 8) | (uint64_t)(k < nb ? rp[k] : 0u);
-          // 56-bit window: field j occupies bits [56 - rr*(j+1), 56 - rr*j)
-          const uint32_t mask = (1u << rr) - 1u;
+            for (uint32_t kk = 0; kk < 7; kk++) acc = (acc << 8) | (uint64_t)(kk < nb ? rp[kk] : 0u);
+            // 56-bit window: field j occupies bits [56 - rr*(j+1), 56 - rr*j)
+            const uint32_t mask = (1u << rr) - 1u;
 #pragma unroll
-          for (int j = 0; j < 8; j++) hv[j] |= (uint32_t)(acc >> (56 - rr * (j + 1))) & mask;
-        }
+            for (int j = 0; j < 8; j++) hv[j] |= (uint32_t)(acc >> (56 - rr * (j + 1))) & mask;
+          }
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          uint32_t v = (uint32_t)j < ml ? hv[j] : 0u;
-          d[j] = ((sb >> (7 - j)) & 1u) ? 0u - v : v;
+          for (int j = 0; j < 8; j++) {
+            const uint32_t v = (uint32_t)j < ml ? hv[j] : 0u;
+            d[j] = ((sb >> (7 - j)) & 1u) ? 0u - v : v;
+          }
         }
       }
-    }
-    uint32_t run = 0;
+      uint32_t run = 0;
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      run += d[j];
-      pre[r][j] = run;
+      for (int j = 0; j < 8; j++) {
+        run += d[j];
+        pre[r][j] = run;
+      }
+      const uint32_t incl = warp_incl_scan(run, lane);
+      lex[r] = incl - run;
+      rbase[r] = wtot;
+      wtot += __shfl_sync(0xffffffffu, incl, 31);
     }
-    const uint32_t incl = warp_incl_scan(run, lane);
-    lex[r] = incl - run;
-    rbase[r] = wtot;
-    wtot += __shfl_sync(0xffffffffu, incl, 31);
-  }
-  if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
+    if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
 
-  // ---- q chain of the segment: CTA scan + look-back from the seed ----
-  uint32_t wexcl;
-  const uint32_t agg = scan_warps_u32<WARPS>(s_w, wtot, warp, lane, wexcl);
-  const uint32_t first_tile = a.tiles_per_seg ? dt.seg * a.tiles_per_seg : 0;
-  {
-    uint32_t excl;
-    if (dt.first) {
-      const uint8_t* seedp = in + R0 - 4;
-      excl = (uint32_t)seedp[0] | ((uint32_t)seedp[1] << 8) | ((uint32_t)seedp[2] << 16) |
-             ((uint32_t)seedp[3] << 24);
-      if (threadIdx.x == 0) {
-        st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
-        a.y[lo] = dequant(excl, eb, ebsp);
-      }
-    } else {
-      if (threadIdx.x == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
-      if (warp == 0) {
-        // the look-back needs registers: park this warp's prefix sums in shared memory
-        uint32_t* stash = reinterpret_cast<uint32_t*>(s_stash);
+    // ---- tile scan over the warps (its first barrier ends every read of the span) ----
+    if (lane == 0) s_w[warp] = wtot;
+    compute_sync();
+    uint32_t wexcl = 0, agg = 0;
 #pragma unroll
-        for (int r = 0; r < ROUNDS; r++)
-#pragma unroll
-          for (int j = 0; j < 8; j++) stash[(r * 8 + j) * 32 + lane] = pre[r][j];
-        excl = (uint32_t)lookback_sum(a.status, tile, first_tile, epoch, a.err);
-#pragma unroll
-        for (int r = 0; r < ROUNDS; r++)
-#pragma unroll
-          for (int j = 0; j < 8; j++) pre[r][j] = stash[(r * 8 + j) * 32 + lane];
-      }
-      if (threadIdx.x == 0)
-        st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
+    for (int w = 0; w < WARPS; w++) {
+      const uint32_t t = s_w[w];
+      wexcl += w < warp ? t : 0u;
+      agg += t;
     }
-    if (threadIdx.x == 0) s_base = excl;
-  }
-  __syncthreads();
-  const uint32_t qw = s_base + wexcl;
-  const uint32_t mis = (uint32_t)(((uintptr_t)(a.y + lo + 1)) >> 2) & 3u;
+    if (threadIdx.x == 0) {
+      s_agg[s] = agg;
+      const bool first = s_meta[s].first;
+      const uint32_t v = first ? s_meta[s].seed + agg : agg;
+      st_release_u64(a.status + tile, make_status(s_epoch, first ? kFlagInclusive : kFlagAggregate, v));
+      mbar_arrive(&s_aggb[s]);
+    }
+
+    // ---- stage the tile-relative prefix sums over the span ----
+    uint32_t* stage = reinterpret_cast<uint32_t*>(slot + PB);
 #pragma unroll
-  for (int r = 0; r < ROUNDS; r++) {
-    const uint32_t bt = wfirst + r * BPR + grp;
-    if (bt >= dt.nblk) continue;
-    const uint64_t bs = lo + 1 + (dt.blk0 + bt) * L;
-    const uint32_t m = (uint32_t)min((uint64_t)L, hi - bs);
-    const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
-    if (!ml) continue;
-    const uint32_t q0 = qw + rbase[r] + lex[r];
-    float v[8];
+    for (int r = 0; r < ROUNDS; r++) {
+      const uint32_t bt = wfirst + r * BPR + grp;
+      const uint32_t k0 = bt * L + 8 * sub;
+      const uint32_t ml = (bt < nblk && k0 < nel) ? min(8u, nel - k0) : 0u;
+      const uint32_t q0 = wexcl + rbase[r] + lex[r];
+      if (ml == 8) {
+        uint4* d4 = reinterpret_cast<uint4*>(stage + k0);
+        d4[0] = make_uint4(q0 + pre[r][0], q0 + pre[r][1], q0 + pre[r][2], q0 + pre[r][3]);
+        d4[1] = make_uint4(q0 + pre[r][4], q0 + pre[r][5], q0 + pre[r][6], q0 + pre[r][7]);
+      } else {
 #pragma unroll
-    for (int j = 0; j < 8; j++) v[j] = dequant(q0 + pre[r][j], eb, ebsp);
-    store8(a.y, bs + 8 * sub, ml, mis, v);
+        for (int j = 0; j < 8; j++)
+          if ((uint32_t)j < ml) stage[k0 + j] = q0 + pre[r][j];
+      }
+    }
+    compute_sync();  // staged; s_w is free for the next tile
+    if (threadIdx.x == 0) mbar_arrive(&s_staged[s]);
   }
 }
 
@@ -952,9 +1115,6 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
   if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
 }
 
-constexpr int kDecWarps = 8;
-constexpr int kDecRounds = 4;
-
 static int dec_lanes_per_block(uint32_t L) {
   switch (L) {
     case 8: return 1;
@@ -1005,13 +1165,39 @@ cudaError_t launch_locate(const DecArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Bytes of one decode slot: the block offsets, then the stream span or the
+// staged prefix sums that replace it (read 16 bytes past their end).
+static uint32_t dec_slot_bytes(uint32_t L, uint32_t tb, uint32_t maxsz) {
+  const size_t span = (size_t)tb * maxsz + 32, stage = 4 * (size_t)tb * L + 32;
+  return (uint32_t)((dec_pos_bytes(tb) + (span > stage ? span : stage) + 15) & ~(size_t)15);
+}
+
 template <int LPB>
 static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
-  auto k = decode_fm1_lanes<LPB, kDecRounds>;
-  size_t smem = decode_smem_bytes(a.seg.L, a.tb, false);
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto k = decode_fm1_pipe<LPB>;
+  const uint32_t slot = dec_slot_bytes(a.seg.L, a.tb, a.maxsz);
+  const size_t smem = (size_t)kDecSlots * slot;
+  // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
+  static std::atomic<uint64_t> s_cache{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  k<<<a.ntiles, 256, smem, st>>>(a);
+  uint64_t c = s_cache.load(std::memory_order_relaxed);
+  if ((c >> 32) != (uint64_t)dev + 1) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int occ = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kDecPipeThreads, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    c = ((uint64_t)dev + 1) << 32 | (uint32_t)((occ < 1 ? 1 : occ) * sms);
+    s_cache.store(c, std::memory_order_relaxed);
+  }
+  const uint32_t cap = (uint32_t)c;
+  const uint32_t grid = a.ntiles < cap ? a.ntiles : cap;
+  if (grid == 0) return cudaSuccess;
+  k<<<grid, kDecPipeThreads, smem, st>>>(a, slot);
   return cudaGetLastError();
 }
 
