@@ -188,12 +188,15 @@ __device__ __forceinline__ uint32_t chunk_segment(const uint32_t* __restrict__ c
 struct SmemChain {
   const uint8_t* sb;
   uint32_t base0, avail, rlen, L;
+  uint32_t l8;  // L / 8 for fastmode1 with L % 8 == 0 (block size 1 + l8*(b+1)), else 0
   bool fm2;
   // block size at p, 0 when its bit-count byte is invalid or not staged
   __device__ __forceinline__ uint32_t step(uint32_t p) const {
     uint32_t hp = fm2 ? p + 4 : p;
     if (hp >= avail) return 0;
-    return full_block_size(sb[hp - base0], L, fm2);
+    const uint32_t b = sb[hp - base0];
+    if (l8) return b > (uint32_t)kMaxBitCount ? 0u : (b ? 1 + l8 * (b + 1) : 1u);
+    return full_block_size(b, L, fm2);
   }
   // walk from p to cE: header count, exit (kPosEnd past the region, kPosDead)
   __device__ __forceinline__ uint32_t walk(uint32_t p, uint32_t cE, uint32_t* exit) const {
@@ -299,6 +302,7 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
   ch.avail = st1;
   ch.rlen = rlen;
   ch.L = sg.L;
+  ch.l8 = (!FM2 && sg.L % 8 == 0) ? sg.L / 8 : 0u;
   ch.fm2 = FM2;
 
   // ---- speculative walk of each thread's chunk ----
@@ -313,9 +317,9 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
   uint32_t h = kPosEnd, x = kPosEnd, k = 0;
   {
     const bool known = j == 0 && tid == 0;  // a segment's block region starts with a header
-    // the first chunk of a CTA is checked across CTAs (costly to repair), the
-    // others against their neighbour here (cheap): shorter overlap for those
-    const uint32_t W = tid == 0 ? W0 : min(W0, max(512u, 4 * a.maxsz));
+    // a wrong guess is caught by the chain checks (inside the CTA, or across
+    // CTAs for its first chunk) and re-walked from the true exit
+    const uint32_t W = min(W0, max(512u, 4 * a.maxsz));
     uint32_t anchor = known ? 0u : (cS > st0 + W ? cS - W : st0);
     uint32_t pos = anchor, entry = anchor >= cS ? anchor : kPosDead, cnt = 0;
     uint32_t budget = 4 * (W + C);
