@@ -22,6 +22,7 @@ reference sources are not on the GPU host) on the same workload.
 Multi-GPU: replicas only (each rank runs the same step on its own GPU).
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -64,57 +65,125 @@ def measured_peak_gbs():
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    """SM clock, clock-event reasons and power while the timed steps run.
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    Read-only NVML queries (libnvidia-ml, part of the driver) every ~1 ms from
+    a thread, so that even a few-millisecond timed region holds samples;
+    nvidia-smi at 200 ms is the fallback.  Only samples taken between mark(True)
+    and mark(False) are reported.
+    """
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, index):
         self.index = index
+        self.samples = []  # (t, sm_mhz, reasons bitmask or None, watts)
+        self.window = None
+        self.max_mhz = None
+        self.stop_flag = False
         self.proc = None
-        self.lines = []
+        self.nv = self.handle = None
+
+    def _nvml(self):
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return False
+        h = ctypes.c_void_p()
+        rc = -1
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(self.index)
+            bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+            rc = nv.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(h))
+        except Exception:
+            rc = -1
+        if rc != 0:
+            vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+            idx = self.index
+            try:
+                idx = int(vis.split(",")[self.index]) if vis else self.index
+            except (ValueError, IndexError):
+                pass
+            rc = nv.nvmlDeviceGetHandleByIndex_v2(idx, ctypes.byref(h))
+        if rc != 0:
+            return False
+        mx = ctypes.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+        self.reason_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(nv, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        self.nv, self.handle = nv, h
+        return True
+
+    def _poll_nvml(self):
+        nv, h = self.nv, self.handle
+        mhz, rs, mw = ctypes.c_uint(), ctypes.c_ulonglong(), ctypes.c_uint()
+        while not self.stop_flag:
+            t = time.perf_counter()
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0:
+                r = rs.value if self.reason_fn(h, ctypes.byref(rs)) == 0 else None
+                w = mw.value / 1000.0 if nv.nvmlDeviceGetPowerUsage(h, ctypes.byref(mw)) == 0 else None
+                self.samples.append((t, float(mhz.value), r, w))
+            time.sleep(0.0005)
+
+    def _poll_smi(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                      "--format=csv,noheader,nounits", "-lms", "200"],
+                                     stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        bits = [0x8, 0x40, 0x20, 0x4]
+        for line in self.proc.stdout:
+            f = [v.strip() for v in line.split(",")]
+            try:
+                r = sum(b for b, v in zip(bits, f[3:7]) if v.lower() == "active")
+                self.max_mhz = float(f[1])
+                self.samples.append((time.perf_counter(), float(f[0]), r, float(f[2])))
+            except (ValueError, IndexError):
+                continue
 
     def start(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            ok = self._nvml()
         except Exception:
-            self.proc = None
+            ok = False
+        self.source = "nvml" if ok else "nvidia-smi"
+        self.t = threading.Thread(target=self._poll_nvml if ok else self._poll_smi, daemon=True)
+        self.t.start()
+        t0 = time.perf_counter()
+        while not self.samples and time.perf_counter() - t0 < 3.0:  # the sampler is running
+            time.sleep(0.001)
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def mark(self, begin):
+        if begin:
+            self.window = [time.perf_counter(), None]
+        else:
+            self.window[1] = time.perf_counter()
 
     def stop(self):
-        if not self.proc:
-            return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [v.strip() for v in ln.split(",")]
-            if len(f) < 8:
-                continue
+        self.stop_flag = True
+        if self.proc:
+            self.proc.terminate()
             try:
-                sm.append(float(f[0]))
-                mx.append(float(f[1]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, f[4:8]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        self.t.join(timeout=2)
+        t0, t1 = self.window if self.window else (0.0, 0.0)
+        inw = [s for s in list(self.samples) if t0 <= s[0] <= t1]
+        if not inw:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        reasons = set()
+        for _, _, r, _ in inw:
+            for b, nm in self.REASONS.items():
+                if r is not None and r & b:
+                    reasons.add(nm)
+        watts = [w for _, _, _, w in inw if w is not None]
+        return {"sm_mhz": statistics.median(s[1] for s in inw), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(inw), "source": self.source,
+                "power_w": round(statistics.median(watts), 1) if watts else None}
 
 
 def dist_setup(args):
@@ -233,11 +302,13 @@ def main():
         pg.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.mark(True)
     e0.record(stream)
     for i in range(args.steps):
         step(i)
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark(False)
     if pg:
         pg.barrier()
     launches = szp.kernel_launches() - l0
@@ -281,27 +352,47 @@ def main():
             "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
             "alg_bytes_per_launch": alg[dom]}
 
-    # ---- e2e through the host C API ----
+    # ---- e2e through the host C API, as a C caller uses it ----
     e2e = None
     if not args.no_e2e:
+        lib = szp._lib
+        libc = ctypes.CDLL(None)
+        libc.free.argtypes = [ctypes.c_void_p]
         hx = torch.empty(n, dtype=torch.float32, pin_memory=True)
         hx.copy_(x)
-        hxn = hx.numpy()
+        size = ctypes.c_size_t(0)
+
+        def host_step(i):
+            p = lib.szp_compress(1, 0, hx.data_ptr(), ctypes.byref(size), szp.REL, 0.0, RELS[i % 3], n, L)
+            assert p, szp.last_error()
+            sz = size.value
+            q = lib.szp_decompress(1, 0, p, sz, n, L)
+            assert q, szp.last_error()
+            return p, q, sz
+
         for i in range(2):
-            s = szp.szp_compress(hxn, szp.REL, 0.0, RELS[i % 3], L)
-            szp.szp_decompress(s, n, L)
+            p, q, sz = host_step(i)
+            if i == 0:  # the host path returns what the device path computed
+                ref = torch.empty(n, dtype=torch.float32, device=dev)
+                szp.compress_dev(x.data_ptr(), n, d_stream.data_ptr(), cap, szp.REL, 0.0, RELS[0], L, T, 1, st)
+                szp.decompress_dev(d_stream.data_ptr(), sizes[RELS[0]], n, ref.data_ptr(), L, T, 1, st)
+                got = torch.from_numpy(np.ctypeslib.as_array((ctypes.c_float * n).from_address(q)))
+                assert torch.equal(got, ref.cpu()), "host API result differs from the device path"
+                del got, ref
+            libc.free(p)
+            libc.free(q)
         h2d = d2h = 0
         t0 = time.perf_counter()
         for i in range(args.steps):
-            s = szp.szp_compress(hxn, szp.REL, 0.0, RELS[i % 3], L)
-            y = szp.szp_decompress(s, n, L)
-            h2d += 4 * n + len(s)
-            d2h += len(s) + 4 * n
+            p, q, sz = host_step(i)
+            libc.free(p)
+            libc.free(q)
+            h2d += 4 * n + sz
+            d2h += sz + 4 * n
         dt = time.perf_counter() - t0
         e2e = {"value": round(world * 4.0 * n * args.steps / dt / 1e9, 3), "unit": "GB/s",
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
-               "api": "szp_compress/szp_decompress (host C ABI, pinned input)"}
-        del y
+               "api": "szp_compress + szp_decompress (C ABI via ctypes; pinned input, library-malloc'd results)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -10,6 +10,7 @@ fails loudly when the library has not been built.
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -79,6 +80,16 @@ _sig("szp_gb300_last_repairs", ctypes.c_int, [])
 _libc = ctypes.CDLL(None)
 _libc.free.argtypes = [_vp]
 _libc.free.restype = None
+
+
+def _owned_f32(p, n):
+    """float32 array over n floats the library malloc'd at p, freed with the array (no copy)."""
+    if n == 0:
+        _libc.free(p)
+        return np.empty(0, np.float32)
+    buf = (ctypes.c_float * n).from_address(p)
+    weakref.finalize(buf, _libc.free, p)
+    return np.frombuffer(buf, dtype=np.float32)
 
 
 class _Lib:
@@ -165,8 +176,7 @@ def szp_decompress(stream, n, block_size=32, fast_mode=SZP_NONRANDOMACCESS, data
     p = _lib.szp_decompress(fast_mode, data_type, buf.ctypes.data, bl, n, block_size)
     if not p:
         _raise("szp_decompress")
-    y = np.frombuffer(ctypes.string_at(p, 4 * n), dtype=np.float32).copy() if n else np.empty(0, np.float32)
-    _libc.free(p)
+    y = _owned_f32(p, n)
     return y
 
 
@@ -229,8 +239,7 @@ def szp_float_decompress_openmp_threadblock(stream, n, block_size=32, fast_mode=
     p = fn(n, eb, block_size, buf.ctypes.data + 4)
     if not p:
         _raise("szp_float_decompress_openmp_threadblock")
-    y = np.frombuffer(ctypes.string_at(p, 4 * n), dtype=np.float32).copy() if n else np.empty(0, np.float32)
-    _libc.free(p)
+    y = _owned_f32(p, n)
     return y
 
 

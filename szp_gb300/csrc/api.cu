@@ -7,6 +7,7 @@
 // extensions work on caller device memory.  No entry point falls back to the
 // CPU: without a usable GPU they fail with an error.
 #include <omp.h>
+#include <unistd.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -499,6 +500,21 @@ int host_stream_length(const uint8_t* stream, size_t n, int L, int T, int fm, si
 }
 
 // ------------------------------------------------- host-buffer pipelines --
+// Maps fresh host pages (a malloc'd result) in parallel before a device copy
+// lands in them: one write per page from every OpenMP thread, instead of one
+// thread taking every page fault inside the copy.
+void prefault(void* p, size_t bytes) {
+  static const size_t page = [] {
+    long v = sysconf(_SC_PAGESIZE);
+    return v > 0 ? (size_t)v : (size_t)4096;
+  }();
+  if (bytes < (size_t)8 << 20) return;  // small results: not worth the threads
+  volatile uint8_t* b = (volatile uint8_t*)p;
+  const int64_t npages = (int64_t)((bytes + page - 1) / page);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < npages; i++) b[(size_t)i * page] = 0;
+}
+
 int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double rel, int L, int T, int fm,
                   uint8_t** out_malloc, uint8_t* out_user, size_t user_cap, size_t* out_size) {
   Workspace* w;
@@ -523,6 +539,7 @@ int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double
     size_t alloc = sz > 4 + 4 * n ? sz : 4 + 4 * n;  // the reference hands out 4+4n bytes
     dst = (uint8_t*)malloc(alloc);
     if (!dst) return fail(SZP_GB300_ENOMEM, "malloc(%zu) failed", alloc);
+    prefault(dst, sz);
   } else if (sz > user_cap) {
     return fail(SZP_GB300_ECAPACITY, "stream of %zu bytes exceeds the %zu-byte output", sz, user_cap);
   }
@@ -576,13 +593,22 @@ int decompress_host(const uint8_t* bytes, size_t len, bool len_known, size_t n, 
   DecompressJob j{d_stream, total, nullptr, n, L, T, fm, w->out.as<float>()};
   rc = decompress_launch(*w, j, st);
   if (rc) return rc;
-  rc = finish_sync(*w, st, nullptr);
-  w->end(st);
-  if (rc) return rc;
+  // the result buffer is mapped on the CPU while the kernels run
   float* dst = out_user;
   if (!dst) {
     dst = (float*)malloc(n ? n * sizeof(float) : 1);
-    if (!dst) return fail(SZP_GB300_ENOMEM, "malloc failed");
+    if (!dst) {
+      finish_sync(*w, st, nullptr);
+      w->end(st);
+      return fail(SZP_GB300_ENOMEM, "malloc failed");
+    }
+    prefault(dst, n * sizeof(float));
+  }
+  rc = finish_sync(*w, st, nullptr);
+  w->end(st);
+  if (rc) {
+    if (!out_user) free(dst);
+    return rc;
   }
   if (n) {
     cudaError_t e = cudaMemcpyAsync(dst, w->out.p, n * sizeof(float), cudaMemcpyDeviceToHost, st);

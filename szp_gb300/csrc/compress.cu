@@ -941,7 +941,17 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
   }
   const float4* x4 = reinterpret_cast<const float4*>(a.x + headn);
   const uint64_t n4 = (n - headn) >> 2;
-  for (uint64_t i = tid; i < n4; i += stride) {
+  uint64_t i = tid;
+  // four independent 16-byte loads in flight per thread
+  for (; i + 3 * stride < n4; i += 4 * stride) {
+    const float4 v0 = __ldg(x4 + i), v1 = __ldg(x4 + i + stride);
+    const float4 v2 = __ldg(x4 + i + 2 * stride), v3 = __ldg(x4 + i + 3 * stride);
+    mn = fminf(mn, fminf(fminf(fminf(v0.x, v0.y), fminf(v0.z, v0.w)), fminf(fminf(v1.x, v1.y), fminf(v1.z, v1.w))));
+    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v0.x, v0.y), fmaxf(v0.z, v0.w)), fmaxf(fmaxf(v1.x, v1.y), fmaxf(v1.z, v1.w))));
+    mn = fminf(mn, fminf(fminf(fminf(v2.x, v2.y), fminf(v2.z, v2.w)), fminf(fminf(v3.x, v3.y), fminf(v3.z, v3.w))));
+    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v2.x, v2.y), fmaxf(v2.z, v2.w)), fmaxf(fmaxf(v3.x, v3.y), fmaxf(v3.z, v3.w))));
+  }
+  for (; i < n4; i += stride) {
     float4 v = __ldg(x4 + i);
     mn = fminf(fminf(mn, v.x), fminf(v.y, fminf(v.z, v.w)));
     mx = fmaxf(fmaxf(mx, v.x), fmaxf(v.y, fmaxf(v.z, v.w)));
@@ -973,13 +983,29 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
     s_last = done == gridDim.x - 1;
   }
   __syncthreads();
-  if (!s_last || threadIdx.x != 0) return;
+  if (!s_last) return;
+  // the last CTA reduces the per-CTA partials with all its threads
   __threadfence();
   mn = INFINITY;
   mx = -INFINITY;
-  for (uint32_t b = 0; b < gridDim.x; b++) {
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
     mn = fminf(mn, ((volatile float*)a.partial)[2 * b]);
     mx = fmaxf(mx, ((volatile float*)a.partial)[2 * b + 1]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __syncthreads();  // s_mn / s_mx are free again
+  if (lane == 0) {
+    s_mn[warp] = mn;
+    s_mx[warp] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+    mn = fminf(mn, s_mn[w]);
+    mx = fmaxf(mx, s_mx[w]);
   }
   *a.counter = 0;  // ready for the next launch
   float range;
