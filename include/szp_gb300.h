@@ -226,6 +226,48 @@ int szp_gb300_last_repairs(void);
 /* Number of kernels this library has launched in this process. */
 unsigned long long szp_gb300_kernel_launches(void);
 
+/* ---- batched fastmode1, blockSize 32 (no counterpart in the reference) ----
+ * Many fields of uneven sizes and bounds go through one persistent launch per
+ * stage (compress: range pass + tiles; decompress: header setup + locate +
+ * decode), replayed as one CUDA graph.  Every field's stream is byte-identical
+ * to szp_compress on that field alone with the same T.  All buffers are device
+ * memory and must stay valid, and unchanged in size, for the batch's lifetime. */
+typedef struct {
+  const void *input;                       /* compress: float[nbEle]; decompress: the stream */
+  size_t input_bytes;                      /* decompress: stream bytes readable at input */
+  const unsigned long long *input_len_dev; /* decompress: optional device stream length
+                                              (e.g. szp_gb300_batch_sizes_dev() + i), NULL = input_bytes */
+  void *output;                            /* compress: stream buffer; decompress: float[nbEle] */
+  size_t output_bytes;                     /* capacity of output in bytes */
+  size_t nbEle;
+  int errBoundMode;                        /* compress: ABS or REL */
+  double absErrBound;
+  double relBoundRatio;
+} szp_gb300_field;
+
+typedef struct szp_gb300_batch_s *szp_gb300_batch;
+
+#define SZP_GB300_BATCH_COMPRESS 0
+#define SZP_GB300_BATCH_DECOMPRESS 1
+#define SZP_GB300_BATCH_AUTOTUNE 1 /* flags: time each tile size on the batch's inputs, keep the fastest */
+#define SZP_GB300_BATCH_NO_GRAPH 2 /* flags: launch the stages directly instead of replaying a graph */
+#define SZP_GB300_BATCH_ROUNDS(r) ((r) << 8) /* flags: fix the tile size (r = 1, 2 or 4) */
+
+/* Builds the batch's tables on the device and captures its graph; T as for
+ * szp_compress (segments <= 0: OpenMP's thread count). */
+int szp_gb300_batch_create(szp_gb300_batch *out, int direction, const szp_gb300_field *fields, int nfields,
+                           int blockSize, int segments, int flags);
+/* Queues one run on a stream (NULL = legacy default stream). */
+int szp_gb300_batch_run(szp_gb300_batch b, void *stream);
+/* Waits for the last run; per-field stream sizes (compress) and statuses
+ * (SZP_GB300_*), either pointer may be NULL.  Returns the first failure. */
+int szp_gb300_batch_sync(szp_gb300_batch b, unsigned long long *sizes, int *status);
+/* Device array of the per-field stream sizes written by a compress run. */
+const unsigned long long *szp_gb300_batch_sizes_dev(szp_gb300_batch b);
+/* Tile size in use: tiles of 64 * rounds blocks (1, 2 or 4). */
+int szp_gb300_batch_tile_rounds(szp_gb300_batch b);
+void szp_gb300_batch_destroy(szp_gb300_batch b);
+
 #ifdef __cplusplus
 }
 #endif

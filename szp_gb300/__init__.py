@@ -75,6 +75,22 @@ _sig("szp_gb300_set_locate_overlap", None, [ctypes.c_int])
 _sig("szp_gb300_kernel_ms", ctypes.c_double, [ctypes.c_int])
 _sig("szp_gb300_kernel_time", ctypes.c_double, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)])
 _sig("szp_gb300_kernel_launches", ctypes.c_ulonglong, [])
+
+
+class Field(ctypes.Structure):
+    """szp_gb300_field: one field of a batch (device buffers)."""
+    _fields_ = [("input", _vp), ("input_bytes", _sz), ("input_len_dev", _vp), ("output", _vp),
+                ("output_bytes", _sz), ("nbEle", _sz), ("errBoundMode", ctypes.c_int),
+                ("absErrBound", ctypes.c_double), ("relBoundRatio", ctypes.c_double)]
+
+
+_sig("szp_gb300_batch_create", ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(Field), ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int])
+_sig("szp_gb300_batch_run", ctypes.c_int, [_vp, _vp])
+_sig("szp_gb300_batch_sync", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_int)])
+_sig("szp_gb300_batch_sizes_dev", _vp, [_vp])
+_sig("szp_gb300_batch_tile_rounds", ctypes.c_int, [_vp])
+_sig("szp_gb300_batch_destroy", None, [_vp])
 _sig("szp_gb300_last_repairs", ctypes.c_int, [])
 
 _libc = ctypes.CDLL(None)
@@ -338,3 +354,60 @@ def last_repairs():
 
 def kernel_launches():
     return int(_lib.szp_gb300_kernel_launches())
+
+
+BATCH_COMPRESS, BATCH_DECOMPRESS = 0, 1
+BATCH_AUTOTUNE, BATCH_NO_GRAPH = 1, 2
+
+
+class Batch:
+    """A batched compression or decompression (szp_gb300_batch_*).
+
+    ``fields`` is a list of dicts with the keys of szp_gb300_field (device
+    pointers as ints).  ``run`` queues one replay on a stream; ``sync`` waits
+    and returns (sizes, statuses) per field.
+    """
+
+    def __init__(self, direction, fields, block_size=32, segments=0, flags=0):
+        self.n = len(fields)
+        arr = (Field * max(self.n, 1))()
+        for i, f in enumerate(fields):
+            for k, v in f.items():
+                setattr(arr[i], k, v)
+        h = _vp()
+        rc = _lib.szp_gb300_batch_create(ctypes.byref(h), direction, arr, self.n, block_size, segments, flags)
+        if rc != 0:
+            raise SzpError(rc, "batch_create failed: %s" % last_error())
+        self._h = h
+        self.direction = direction
+
+    def run(self, stream=0):
+        rc = _lib.szp_gb300_batch_run(self._h, stream or None)
+        if rc != 0:
+            raise SzpError(rc, "batch_run failed: %s" % last_error())
+
+    def sync(self, check=True):
+        sizes = (ctypes.c_ulonglong * max(self.n, 1))()
+        status = (ctypes.c_int * max(self.n, 1))()
+        rc = _lib.szp_gb300_batch_sync(self._h, sizes, status)
+        if rc != 0 and check:
+            raise SzpError(rc, "batch failed: %s" % last_error())
+        return [int(v) for v in sizes[:self.n]], [int(v) for v in status[:self.n]]
+
+    def sizes_dev(self):
+        """Device address of the per-field stream sizes (unsigned long long[n])."""
+        return _lib.szp_gb300_batch_sizes_dev(self._h)
+
+    def tile_rounds(self):
+        return _lib.szp_gb300_batch_tile_rounds(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.szp_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

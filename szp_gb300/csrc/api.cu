@@ -419,16 +419,17 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
 
   DecArgs a;
   memset(&a, 0, sizeof a);
-  a.in = j.d_in;
-  a.len = j.len;
-  a.len_dev = j.d_len;
-  a.seg = sg;
+  DecField& f = a.f;
+  f.in = j.d_in;
+  f.len = j.len;
+  f.len_dev = j.d_len;
+  f.seg = sg;
   a.fm2 = fm2;
   uint8_t* pb = w.plan.as<uint8_t>();
-  a.plan = reinterpret_cast<DecPlan*>(pb);
-  a.reg0 = reinterpret_cast<uint64_t*>(pb + 64);
-  a.reg1 = a.reg0 + j.T;
-  a.chunk_base = reinterpret_cast<uint32_t*>(a.reg1 + j.T);
+  f.plan = reinterpret_cast<DecPlan*>(pb);
+  f.reg0 = reinterpret_cast<uint64_t*>(pb + 64);
+  f.reg1 = f.reg0 + j.T;
+  f.chunk_base = reinterpret_cast<uint32_t*>(f.reg1 + j.T);
   a.chunk = C;
   a.super_chunk = SC;
   a.overlap = g_overlap >= 0 ? (uint32_t)g_overlap : locate_overlap_bytes(maxsz);
@@ -438,11 +439,16 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.status = w.status.as<uint64_t>();
   a.ls = &dm->ls;
   a.err = &dm->err;
-  a.blkpos = w.blkpos.as<uint32_t>();
-  a.nblk_total = nblk_total;
-  a.y = j.d_y;
+  f.err = &dm->err;
+  f.blkpos = w.blkpos.as<uint32_t>();
+  f.nblk_total = nblk_total;
+  f.y = j.d_y;
+  f.ntiles = (uint32_t)ntiles;
+  f.tiles_per_seg = (uint32_t)per_seg;
+  f.tile_base = 0;
+  f.loc_base = 0;
+  f.loc_ctas = (uint32_t)nlocate;
   a.ntiles = (uint32_t)ntiles;
-  a.tiles_per_seg = (uint32_t)per_seg;
   a.tb = tb;
   a.bpw = bpw;
   a.nlocate_ctas = (uint32_t)nlocate;
@@ -634,6 +640,17 @@ void host_compress_tiles(size_t n, int T, int L, uint64_t& tiles_per_seg, uint64
   Segments sg = make_segments(n, T, L);
   tile_counts(sg, false, tb, tiles_per_seg, ntiles);
 }
+void host_tile_counts(size_t n, int T, int L, uint32_t tb, uint64_t& tiles_per_seg, uint64_t& ntiles) {
+  Segments sg = make_segments(n, T, L);
+  tile_counts(sg, false, tb, tiles_per_seg, ntiles);
+}
+uint64_t host_block_count(size_t n, int T, int L) {
+  Segments sg = make_segments(n, T, L);
+  if (!sg.n) return 0;
+  return (uint64_t)(sg.T - 1) * (sg.tsz ? seg_blocks_host(sg, 0, false) : 0) + seg_blocks_host(sg, sg.T - 1, false);
+}
+size_t host_max_stream_bytes(size_t n, int L, int T) { return max_stream_bytes(n, L, T, 1); }
+int host_status_from_err(uint32_t err) { return status_from_err(err); }
 void host_segment_blocks(size_t n, int T, int L, uint64_t& nb_reg, uint64_t& nb_last) {
   Segments sg = make_segments(n, T, L);
   nb_reg = sg.tsz ? seg_blocks_host(sg, 0, false) : 0;

@@ -282,9 +282,20 @@ struct TileGeo {
 constexpr int kPipeSlots = 3, kPipeControl = 2;
 constexpr int kPipeThreads = (8 + kPipeControl + 1) * 32;
 
+// What the compute and control warps need of a slot's tile, written by the
+// producer before the slot's full barrier completes.
 struct SlotMeta {
   TileGeo g;
-  uint32_t tile;  // kStopTile: no more tiles for this CTA
+  uint32_t tile;       // launch tile (its look-back word); kStopTile: no more tiles
+  uint32_t ltile;      // tile within its field
+  uint32_t tile_base;  // the field's first launch tile
+  uint32_t ntiles;     // tiles of the field
+  float eb, inv;       // the field's bound and 1/bound
+  Segments seg;        // the field's segments
+  uint8_t* out;        // the field's stream
+  uint64_t cap;
+  uint64_t* out_size;
+  uint32_t* err;       // the field's error word
 };
 
 // Exclusive scan of n (<= 1024) values in shared memory by the 256 compute
@@ -379,13 +390,28 @@ __device__ __forceinline__ void warp_store_span(uint8_t* __restrict__ dst, const
 // Producer: one thread.  Draws tickets, and for each tile computes its
 // geometry and bulk-copies its input window [e0-1, e0+nel) into a free slot
 // (element e at slot float e - (e0-1) + d).
-template <uint32_t L, uint32_t TB, int NS>
+template <uint32_t L, uint32_t TB, int NS, bool BATCH>
 __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* slots, uint32_t slot_bytes,
                                               SlotMeta* meta, uint64_t* full, uint64_t* empty,
                                               uint32_t* s_epoch, volatile uint32_t* s_stop_k) {
-  const Segments& sg = a.seg;
   *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
   __threadfence();
+  CompressField f1;  // the single field of a non-batched launch
+  if (!BATCH) {
+    f1.x = a.x;
+    f1.out = a.out;
+    f1.cap = a.cap;
+    f1.seg = a.seg;
+    f1.nb_reg = a.nb_reg;
+    f1.nb_last = a.nb_last;
+    f1.tiles_per_seg = a.tiles_per_seg;
+    f1.ntiles = a.ntiles;
+    f1.tile_base = 0;
+    f1.eb = a.eb_dev ? *a.eb_dev : a.eb;
+    f1.out_size = a.out_size;
+    f1.err = a.err;
+  }
+  const float inv1 = BATCH ? 0.0f : __fdiv_rn(1.0f, f1.eb);
   for (uint32_t k = 0;; k++) {
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
@@ -397,19 +423,32 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
       mbar_arrive(&full[s]);
       return;
     }
+    const CompressField& fd = BATCH ? a.fields[a.tile_field[tile]] : f1;
+    const Segments sg = fd.seg;
+    const uint32_t lt = tile - fd.tile_base;
+    m.ltile = lt;
+    m.tile_base = fd.tile_base;
+    m.ntiles = fd.ntiles;
+    m.eb = fd.eb;
+    m.inv = BATCH ? __fdiv_rn(1.0f, fd.eb) : inv1;
+    m.seg = sg;
+    m.out = fd.out;
+    m.cap = fd.cap;
+    m.out_size = fd.out_size;
+    m.err = fd.err;
     float* sx = reinterpret_cast<float*>(slots + (size_t)s * slot_bytes);
     TileGeo g;
     g.has_seg = sg.n > 0;
-    uint32_t t = sg.T - 1, ts = tile;
-    if (a.tiles_per_seg) {
-      t = tile / a.tiles_per_seg;
+    uint32_t t = sg.T - 1, ts = lt;
+    if (fd.tiles_per_seg) {
+      t = lt / fd.tiles_per_seg;
       if (t > sg.T - 1) t = sg.T - 1;
-      ts = tile - t * a.tiles_per_seg;
+      ts = lt - t * fd.tiles_per_seg;
     }
     g.seg = t;
     g.lo = (uint64_t)t * sg.tsz;
     g.hi = t + 1 == sg.T ? sg.n : g.lo + sg.tsz;
-    const uint64_t nb = t + 1 == sg.T ? a.nb_last : a.nb_reg;
+    const uint64_t nb = t + 1 == sg.T ? fd.nb_last : fd.nb_reg;
     const uint64_t blk0 = (uint64_t)ts * TB;
     g.nblk = nb > blk0 ? (uint32_t)min((uint64_t)TB, nb - blk0) : 0u;
     g.first = ts == 0;
@@ -419,7 +458,7 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
     uint32_t bytes = 0;
     uintptr_t b0 = 0, a0 = 0;
     if (g.has_seg && (g.nblk || (g.first && g.hi > g.lo))) {  // a lone seed still needs x[lo]
-      const uintptr_t xa = (uintptr_t)a.x;
+      const uintptr_t xa = (uintptr_t)fd.x;
       const uintptr_t w0 = xa + 4 * (g.e0 - 1), w1 = xa + 4 * (g.e0 + g.nel);
       a0 = w0 & ~(uintptr_t)15;
       g.d = (uint32_t)((w0 - a0) >> 2);
@@ -450,45 +489,47 @@ template <int NS, int NC>
 __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const uint8_t* slots,
                                              uint32_t slot_bytes, const SlotMeta* meta, const uint32_t* s_agg,
                                              uint64_t* full, uint64_t* aggb, uint64_t* packed, uint64_t* empty,
-                                             const uint32_t* s_epoch, const volatile uint32_t* s_stop_k, float eb) {
+                                             const uint32_t* s_epoch, const volatile uint32_t* s_stop_k) {
   const int lane = threadIdx.x & 31;
-  const Segments& sg = a.seg;
   for (uint32_t k = (uint32_t)c;; k += NC) {
     const int s = (int)(k % NS);
     const uint32_t par = (k / NS) & 1;
     if (!control_wait_full(&full[s], par, k, s_stop_k, a.err)) return;
-    const uint32_t tile = meta[s].tile;
+    const SlotMeta& m = meta[s];
+    const uint32_t tile = m.tile;
     if (tile >= a.ntiles) return;
-    const uint32_t seg = meta[s].g.seg;
-    const bool first_of_seg = meta[s].g.has_seg && meta[s].g.first;
+    const uint32_t seg = m.g.seg, lt = m.ltile;
+    const bool first_of_seg = m.g.has_seg && m.g.first;
+    uint8_t* out = m.out;
+    const uint64_t cap = m.cap;
     mbar_wait_or_flag(&aggb[s], par, a.err);
     const uint32_t agg = s_agg[s];
     const uint32_t epoch = *s_epoch;
     uint64_t excl = 0;
-    if (tile == 0) {
-      write_header_warp(a.out, eb, sg, lane);
+    if (lt == 0) {
+      write_header_warp(out, m.eb, m.seg, lane);
     } else {
-      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
+      excl = lookback_sum(a.status, tile, m.tile_base, epoch, a.err);
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
-    const uint64_t gpos = 4 + 8ull * sg.T + excl;
-    const bool fits = gpos + agg <= a.cap;
+    const uint64_t gpos = 4 + 8ull * m.seg.T + excl;
+    const bool fits = gpos + agg <= cap;
     if (lane == 0) {
-      if (tile == a.ntiles - 1) *a.out_size = gpos + agg;
-      if (first_of_seg && fits) write_offset(a.out, seg, excl);
-      if (!fits) atomicOr(a.err, kErrCapacity);
+      if (lt == m.ntiles - 1) *m.out_size = gpos + agg;
+      if (first_of_seg && fits) write_offset(out, seg, excl);
+      if (!fits) atomicOr(m.err, kErrCapacity);
     }
     mbar_wait_or_flag(&packed[s], par, a.err);
-    if (fits) warp_store_span(a.out + gpos, slots + (size_t)s * slot_bytes, agg, lane);
+    if (fits) warp_store_span(out + gpos, slots + (size_t)s * slot_bytes, agg, lane);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
-template <int LPB>
+template <int LPB, bool BATCH, int ROUNDS>
 __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __grid_constant__ CompressArgs a,
                                                                      uint32_t slot_bytes) {
-  constexpr int NS = kPipeSlots, NC = kPipeControl, ROUNDS = 4;
+  constexpr int NS = kPipeSlots, NC = kPipeControl;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
   constexpr uint32_t TB = 8 * ROUNDS * BPR;
@@ -517,19 +558,18 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
   }
   __syncthreads();
 
-  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
   if (warp == 8 + NC) {
-    if (lane == 0) pipe_producer<L, TB, NS>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
+    if (lane == 0)
+      pipe_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
     return;
   }
   if (warp >= 8) {
     pipe_control<NS, NC>(warp - 8, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_packed, s_empty,
-                         &s_epoch, &s_stop_k, eb);
+                         &s_epoch, &s_stop_k);
     return;
   }
 
   // ---- compute warps ----
-  const float inv = __fdiv_rn(1.0f, eb);
   const int sub = lane % LPB, grp = lane / LPB;
   for (uint32_t k = 0;; k++) {
     const int s = (int)(k % NS);
@@ -538,6 +578,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     const uint32_t tile = s_meta[s].tile;
     if (tile >= a.ntiles) return;
     const TileGeo g = s_meta[s].g;
+    const float inv = s_meta[s].inv;
     uint8_t* slot = s_slots + (size_t)s * slot_bytes;
     const float* sx = reinterpret_cast<const float*>(slot);
     const bool seed = g.has_seg && g.first && g.hi > g.lo;
@@ -618,7 +659,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
         s_off[bt] = block_bytes(m, bc);
       }
     }
-    if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
+    if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(s_meta[s].err, kErrQuantRange);
     compute_sync();  // block sizes complete; the input window is dead from here on
 
     // ---- block offsets in the tile; publish the tile's byte count ----
@@ -626,7 +667,8 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     const uint32_t agg = compute_scan_excl(s_off, g.nblk, s_part) + front;
     if (threadIdx.x == 0) {
       s_agg[s] = agg;
-      st_release_u64(a.status + tile, make_status(s_epoch, tile == 0 ? kFlagInclusive : kFlagAggregate, agg));
+      const bool head = s_meta[s].ltile == 0;  // a field's first tile has no predecessor
+      st_release_u64(a.status + tile, make_status(s_epoch, head ? kFlagInclusive : kFlagAggregate, agg));
       mbar_arrive(&s_aggb[s]);
     }
 
@@ -1077,9 +1119,9 @@ static uint32_t pipe_slot_bytes(uint32_t L, uint32_t tb) {
   return (uint32_t)(((out > in ? out : in) + 15) & ~(size_t)15);
 }
 
-template <int LPB>
+template <int LPB, bool BATCH = false, int ROUNDS = kRounds>
 static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
-  auto k = compress_fm1_pipe<LPB>;
+  auto k = compress_fm1_pipe<LPB, BATCH, ROUNDS>;
   const uint32_t slot = pipe_slot_bytes(a.seg.L, a.tb);
   const size_t smem = (size_t)kPipeSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
@@ -1126,6 +1168,111 @@ cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st) {
     k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
   }
   return cudaGetLastError();
+}
+
+// Order-preserving encoding of a non-NaN float as an unsigned integer.
+__host__ __device__ __forceinline__ uint32_t rel_encode(float v) {
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float rel_decode(uint32_t e) {
+  const uint32_t u = (e & 0x80000000u) ? (e & 0x7FFFFFFFu) : ~e;
+  return __uint_as_float(u);
+}
+uint32_t rel_encode_host(float v) { return rel_encode(v); }
+
+// Range pass of a batch: every CTA reduces work items (a chunk of one REL
+// field) with the single-field pass's rules (fminf/fmaxf, NaN ignored), and
+// the last item of a field turns its range into the bound exactly as
+// rel_bound_kernel does (szp.cc:36-51 semantics).
+__global__ void __launch_bounds__(256) rel_batch_kernel(const __grid_constant__ RelBatchArgs a) {
+  __shared__ float s_mn[8], s_mx[8];
+  __shared__ uint32_t s_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t it = blockIdx.x; it < a.nitems; it += gridDim.x) {
+    const uint32_t f = a.item_field[it];
+    CompressField& fd = a.fields[f];
+    RelFieldState& st = a.state[f];
+    const float* x = fd.x;
+    const uint64_t n = fd.seg.n;
+    const uint64_t lo = (uint64_t)(it - st.first_item) * a.chunk;
+    const uint64_t hi = min(n, lo + a.chunk);
+    float mn = INFINITY, mx = -INFINITY;
+    // scalar head to a 16-byte boundary, 16-byte body, scalar tail
+    uint64_t b0 = lo;
+    while (b0 < hi && (((uintptr_t)(x + b0)) & 15)) b0++;
+    const uint64_t n4 = (hi - b0) >> 2;
+    for (uint64_t i = lo + threadIdx.x; i < b0; i += blockDim.x) {
+      mn = fminf(mn, x[i]);
+      mx = fmaxf(mx, x[i]);
+    }
+    const float4* x4 = reinterpret_cast<const float4*>(x + b0);
+    for (uint64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+      const float4 v = __ldg(x4 + i);
+      mn = fminf(mn, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
+      mx = fmaxf(mx, fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w)));
+    }
+    for (uint64_t i = b0 + 4 * n4 + threadIdx.x; i < hi; i += blockDim.x) {
+      mn = fminf(mn, x[i]);
+      mx = fmaxf(mx, x[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) {
+      s_mn[warp] = mn;
+      s_mx[warp] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < 8; w++) {
+        mn = fminf(mn, s_mn[w]);
+        mx = fmaxf(mx, s_mx[w]);
+      }
+      // +inf / -inf (an all-NaN chunk) leave the field's state unchanged
+      atomicMin(&st.mn, rel_encode(mn));
+      atomicMax(&st.mx, rel_encode(mx));
+      __threadfence();
+      s_last = atomicAdd(&st.done, 1u) == st.nitems - 1;
+      if (s_last) {
+        __threadfence();
+        const float fmn = rel_decode(*(volatile uint32_t*)&st.mn);
+        const float fmx = rel_decode(*(volatile uint32_t*)&st.mx);
+        float range;
+        if (isnan(x[0])) {
+          range = __uint_as_float(__float_as_uint(x[0]) | 0x00400000u);
+        } else if (fmx == fmn && isfinite(fmx)) {
+          range = 0.0f;
+        } else {
+          range = x86_nan_fix(__fsub_rn(fmx, fmn), fmx, fmn);
+        }
+        fd.eb = x86_nan_fix(__fmul_rn(range, fd.rel), range, fd.rel);
+        st.mn = rel_encode(INFINITY);  // ready for the next run
+        st.mx = rel_encode(-INFINITY);
+        st.done = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_rel_batch(const RelBatchArgs& a, uint32_t grid, cudaStream_t st) {
+  if (a.nitems == 0) return cudaSuccess;
+  rel_batch_kernel<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// Batched fastmode1 compression, blockSize 32, tiles of 8*rounds*8 blocks.
+cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds, cudaStream_t st) {
+  if (L != 32) return cudaErrorInvalidValue;
+  switch (rounds) {
+    case 1: return launch_lanes<4, true, 1>(a, st);
+    case 2: return launch_lanes<4, true, 2>(a, st);
+    case 4: return launch_lanes<4, true, 4>(a, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st) {

@@ -77,23 +77,25 @@ __device__ __forceinline__ uint64_t load_u64le(const uint8_t* p) {
 // ---------------------------------------------------------------------------
 // 1. header -> plan
 // ---------------------------------------------------------------------------
-__global__ void dec_setup_kernel(DecArgs a) {
-  const Segments sg = a.seg;
+template <bool BATCH>
+__global__ void dec_setup_kernel(const __grid_constant__ DecArgs a) {
+  const DecField& fd = BATCH ? a.fields[blockIdx.x] : a.f;
+  const Segments sg = fd.seg;
   const uint32_t T = sg.T;
   const uint64_t head = 4 + 8ull * T;
   __shared__ uint32_t s_bad;
-  uint64_t len = a.len;
-  if (a.len_dev) {
-    uint64_t l2 = *a.len_dev;
+  uint64_t len = fd.len;
+  if (fd.len_dev) {
+    uint64_t l2 = *fd.len_dev;
     len = l2 < len ? l2 : len;
   }
   if (threadIdx.x == 0) {
     s_bad = len < head ? 1u : 0u;
     if (!s_bad) {
-      uint32_t b = ((uint32_t)a.in[0] << 24) | ((uint32_t)a.in[1] << 16) | ((uint32_t)a.in[2] << 8) | a.in[3];
-      a.plan->eb = __uint_as_float(b);
+      uint32_t b = ((uint32_t)fd.in[0] << 24) | ((uint32_t)fd.in[1] << 16) | ((uint32_t)fd.in[2] << 8) | fd.in[3];
+      fd.plan->eb = __uint_as_float(b);
     } else {
-      a.plan->eb = 0.0f;
+      fd.plan->eb = 0.0f;
     }
   }
   __syncthreads();
@@ -104,7 +106,7 @@ __global__ void dec_setup_kernel(DecArgs a) {
     uint32_t nch = 0;
     bool bad = false;
     if (len_t > 0 && hdr_ok) {
-      uint64_t off = load_u64le(a.in + 4 + 8ull * t);
+      uint64_t off = load_u64le(fd.in + 4 + 8ull * t);
       uint64_t body = len - head;
       uint64_t end;
       if (off > body) {
@@ -112,7 +114,7 @@ __global__ void dec_setup_kernel(DecArgs a) {
       } else {
         uint64_t start = head + off;
         if (t + 1 < T) {
-          uint64_t off2 = load_u64le(a.in + 4 + 8ull * (t + 1));
+          uint64_t off2 = load_u64le(fd.in + 4 + 8ull * (t + 1));
           if (off2 < off || off2 > body) bad = true;
           end = head + off2;
         } else {
@@ -137,25 +139,25 @@ __global__ void dec_setup_kernel(DecArgs a) {
       atomicOr(&s_bad, 1u);
       nch = 0;
     }
-    a.reg0[t] = r0;
-    a.reg1[t] = r1;
-    a.chunk_base[t + 1] = nch;
+    fd.reg0[t] = r0;
+    fd.reg1[t] = r1;
+    fd.chunk_base[t + 1] = nch;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t acc = 0;
-    a.chunk_base[0] = 0;
+    fd.chunk_base[0] = 0;
     if (s_bad) {
-      for (uint32_t t = 0; t < T; t++) a.chunk_base[t + 1] = 0;
-      atomicOr(a.err, kErrCorrupt);
+      for (uint32_t t = 0; t < T; t++) fd.chunk_base[t + 1] = 0;
+      atomicOr(fd.err, kErrCorrupt);
     } else {
       for (uint32_t t = 0; t < T; t++) {
-        acc += a.chunk_base[t + 1];
-        a.chunk_base[t + 1] = acc;
+        acc += fd.chunk_base[t + 1];
+        fd.chunk_base[t + 1] = acc;
       }
     }
-    a.plan->nchunks = s_bad ? 0 : acc;
-    a.plan->bad = s_bad;
+    fd.plan->nchunks = s_bad ? 0 : acc;
+    fd.plan->bad = s_bad;
   }
 }
 
@@ -244,8 +246,8 @@ __device__ __forceinline__ void rewalk_from(const SmemChain& ch, uint32_t* h, ui
   }
 }
 
-template <bool FM2>
-__global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
+template <bool FM2, bool BATCH>
+__global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_constant__ DecArgs a) {
   constexpr int NT = kLocThreads;
   extern __shared__ __align__(16) uint8_t s_bytes[];
   __shared__ uint32_t s_tk[2];
@@ -256,22 +258,25 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
   __shared__ __align__(8) uint64_t s_bar;
   uint32_t tile, epoch;
   draw_ticket(a.ls, a.nlocate_ctas, tile, epoch, s_tk);
-  const uint32_t nct = a.plan->bad ? 0 : a.chunk_base[a.seg.T];
-  if (tile >= nct) return;
+  // status and aux words are indexed by launch ticket, chunks by field-local ticket
+  const DecField& fd = BATCH ? a.fields[a.loc_field[tile]] : a.f;
+  const uint32_t lt = tile - fd.loc_base;
+  const uint32_t nct = fd.plan->bad ? 0 : fd.chunk_base[fd.seg.T];
+  if (lt >= nct) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const Segments& sg = a.seg;
-  const uint32_t t = chunk_segment(a.chunk_base, sg.T, tile);
-  const uint32_t first = a.chunk_base[t];
+  const Segments sg = fd.seg;
+  const uint32_t t = chunk_segment(fd.chunk_base, sg.T, lt);
+  const uint32_t first = fd.loc_base + fd.chunk_base[t];  // launch ticket of the segment's first chunk
   const uint32_t j = tile - first;
-  const uint64_t R0 = a.reg0[t];
-  const uint32_t rlen = (uint32_t)(a.reg1[t] - R0);
+  const uint64_t R0 = fd.reg0[t];
+  const uint32_t rlen = (uint32_t)(fd.reg1[t] - R0);
   const uint32_t C = a.chunk, SC = a.super_chunk, W0 = a.overlap;
   const uint32_t scS = j * SC, scE = min(scS + SC, rlen);
 
   // ---- stage [scS - W0, scE + maxsz) of the region ----
   const uint32_t st0 = scS > W0 ? scS - W0 : 0u;
   const uint32_t st1 = (uint32_t)min((uint64_t)rlen, (uint64_t)scE + a.maxsz + 8);
-  const uint8_t* g = a.in + R0 + st0;
+  const uint8_t* g = fd.in + R0 + st0;
   const uint32_t align = (uint32_t)((uintptr_t)g & 15);
   {
     if (tid == 0) mbar_init(&s_bar, 1);
@@ -529,17 +534,17 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(DecArgs a) {
   if (kx && p < rlen) {
     for (uint32_t i = 0; i < kx; i++) {
       const uint64_t gi = g0 + i;
-      if (gi < nb) a.blkpos[gb + gi] = p;
+      if (gi < nb) fd.blkpos[gb + gi] = p;
       const uint32_t sz = ch.step(p);
       if (!sz) break;
       p += sz;
     }
   }
   // the last CTA of a segment checks the block total
-  if (tid == 0 && tile + 1 == a.chunk_base[t + 1]) {
+  if (tid == 0 && lt + 1 == fd.chunk_base[t + 1]) {
     const uint64_t total = prefix + K;
     const bool last_seg = t + 1 == sg.T;
-    if (total < nb || (!last_seg && total != nb)) atomicOr(a.err, kErrBlockCount);
+    if (total < nb || (!last_seg && total != nb)) atomicOr(fd.err, kErrBlockCount);
   }
 }
 
@@ -686,20 +691,22 @@ struct DecSlot {
   uint32_t spanlen;  // staged span bytes
   uint32_t sofs;     // slot byte offset of span byte 0
   uint32_t pofs;     // slot word offset of the tile's first block offset
+  uint32_t seg_tile0;  // launch tile of its segment's first tile (the look-back stops there)
+  float eb;          // the field's bound
+  float* y;          // the field's output
+  uint32_t* err;     // the field's error word
 };
 
 // Bytes of the block-offset area at the front of a slot.
 __host__ __device__ constexpr uint32_t dec_pos_bytes(uint32_t tb) { return 4 * tb + 32; }
 
-template <uint32_t L, uint32_t TB, int NS>
+template <uint32_t L, uint32_t TB, int NS, bool BATCH>
 __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, uint32_t slot_bytes, DecSlot* meta,
                                              uint64_t* full, uint64_t* empty, uint32_t* s_epoch,
                                              volatile uint32_t* s_stop_k) {
-  const Segments& sg = a.seg;
   constexpr uint32_t PB = dec_pos_bytes(TB);
   *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
   __threadfence();
-  const bool bad = a.plan->bad != 0;
   for (uint32_t k = 0;;) {
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
@@ -711,21 +718,27 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
       mbar_arrive(&full[s]);
       return;
     }
-    const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, false);
+    const DecField& fd = BATCH ? a.fields[a.tile_field[tile]] : a.f;
+    const Segments sg = fd.seg;
+    const DecTile dt = dec_tile(sg, tile - fd.tile_base, fd.tiles_per_seg, TB, false);
     // nothing to write: a failed plan, an empty segment, a tile past its segment's blocks
-    if (bad || !dt.any || (dt.nblk == 0 && !dt.first)) continue;  // the slot stays free
+    if (fd.plan->bad || !dt.any || (dt.nblk == 0 && !dt.first)) continue;  // the slot stays free
     const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
-    const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
+    const uint64_t R0 = fd.reg0[dt.seg], R1 = fd.reg1[dt.seg];
     const uint32_t rlen = (uint32_t)(R1 - R0);
     uint8_t* slot = slots + (size_t)s * slot_bytes;
     m.seg = dt.seg;
+    m.seg_tile0 = fd.tile_base + (fd.tiles_per_seg ? dt.seg * fd.tiles_per_seg : 0u);
+    m.eb = fd.plan->eb;
+    m.y = fd.y;
+    m.err = fd.err;
     m.nblk = dt.nblk;
     m.first = dt.first;
     m.e0 = lo + 1 + dt.blk0 * L;
     m.nel = dt.nblk ? (uint32_t)min((uint64_t)dt.nblk * L, hi - m.e0) : 0u;
     m.seed = 0;
     if (dt.first) {
-      const uint8_t* sp = a.in + R0 - 4;  // the segment's 4-byte seed precedes its blocks
+      const uint8_t* sp = fd.in + R0 - 4;  // the segment's 4-byte seed precedes its blocks
       m.seed = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
                ((uint32_t)__ldg(sp + 3) << 24);
     }
@@ -736,7 +749,7 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     uint32_t tx = 0;
     uintptr_t p0 = 0, p1 = 0, q0 = 0, q1 = 0;
     if (dt.nblk) {
-      const uint32_t* bp = a.blkpos + seg_block_base(sg, dt.seg, false) + dt.blk0;
+      const uint32_t* bp = fd.blkpos + seg_block_base(sg, dt.seg, false) + dt.blk0;
       const uint32_t s0 = min(__ldg(bp), rlen);
       uint32_t s1 = (uint32_t)min((uint64_t)rlen, (uint64_t)__ldg(bp + dt.nblk - 1) + a.maxsz);
       if (s1 < s0) s1 = s0;
@@ -745,18 +758,18 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
       p0 = (uintptr_t)bp;
       p1 = p0 + 4ull * dt.nblk;
       m.pofs = (uint32_t)((p0 & 15) >> 2);
-      tx += stage_range(slot, reinterpret_cast<const uint8_t*>(a.blkpos), 4 * a.nblk_total, p0, p1);
-      q0 = (uintptr_t)(a.in + R0 + s0);
+      tx += stage_range(slot, reinterpret_cast<const uint8_t*>(fd.blkpos), 4 * fd.nblk_total, p0, p1);
+      q0 = (uintptr_t)(fd.in + R0 + s0);
       q1 = q0 + m.spanlen;
       m.sofs = PB + (uint32_t)(q0 & 15);
-      tx += stage_range(slot + PB, a.in, a.len, q0, q1);
+      tx += stage_range(slot + PB, fd.in, fd.len, q0, q1);
     }
     m.tile = tile;
     if (tx) {
       fence_async_smem();
       mbar_arrive_expect_tx(&full[s], tx);
-      stage_range_issue(slot, reinterpret_cast<const uint8_t*>(a.blkpos), 4 * a.nblk_total, p0, p1, &full[s]);
-      stage_range_issue(slot + PB, a.in, a.len, q0, q1, &full[s]);
+      stage_range_issue(slot, reinterpret_cast<const uint8_t*>(fd.blkpos), 4 * fd.nblk_total, p0, p1, &full[s]);
+      stage_range_issue(slot + PB, fd.in, fd.len, q0, q1, &full[s]);
     } else {
       mbar_arrive(&full[s]);
     }
@@ -805,8 +818,7 @@ template <int NS, int NC, uint32_t TB>
 __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const uint8_t* slots, uint32_t slot_bytes,
                                             const DecSlot* meta, const uint32_t* s_agg, uint64_t* full,
                                             uint64_t* aggb, uint64_t* staged, uint64_t* empty,
-                                            const uint32_t* s_epoch, const volatile uint32_t* s_stop_k, float eb,
-                                            bool ebsp) {
+                                            const uint32_t* s_epoch, const volatile uint32_t* s_stop_k) {
   const int lane = threadIdx.x & 31;
   for (uint32_t k = (uint32_t)c;; k += NC) {
     const int s = (int)(k % NS);
@@ -814,34 +826,36 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const uint8
     if (!control_wait_full(&full[s], par, k, s_stop_k, a.err)) return;
     const uint32_t tile = meta[s].tile;
     if (tile >= a.ntiles) return;
-    const uint32_t seg = meta[s].seg, nel = meta[s].nel;
+    const uint32_t nel = meta[s].nel;
     const bool first = meta[s].first;
     const uint64_t e0 = meta[s].e0;
     const uint32_t seed = meta[s].seed;
+    const float eb = meta[s].eb;
+    const bool ebsp = !isfinite(eb);
+    float* y = meta[s].y;
     mbar_wait_or_flag(&aggb[s], par, a.err);
     const uint32_t agg = s_agg[s];
     const uint32_t epoch = *s_epoch;
     uint32_t base;
     if (first) {
       base = seed;
-      if (lane == 0) a.y[e0 - 1] = dequant(seed, eb, ebsp);
+      if (lane == 0) y[e0 - 1] = dequant(seed, eb, ebsp);
     } else {
-      const uint32_t first_tile = a.tiles_per_seg ? seg * a.tiles_per_seg : 0;
-      base = (uint32_t)lookback_sum(a.status, tile, first_tile, epoch, a.err);
+      base = (uint32_t)lookback_sum(a.status, tile, meta[s].seg_tile0, epoch, a.err);
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(base + agg)));
     }
     mbar_wait_or_flag(&staged[s], par, a.err);
     const uint32_t* stage = reinterpret_cast<const uint32_t*>(slots + (size_t)s * slot_bytes + dec_pos_bytes(TB));
-    warp_dequant_store(a.y + e0, stage, nel, base, eb, ebsp, lane);
+    warp_dequant_store(y + e0, stage, nel, base, eb, ebsp, lane);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
-template <int LPB>
+template <int LPB, bool BATCH, int ROUNDS>
 __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __grid_constant__ DecArgs a,
                                                                       uint32_t slot_bytes) {
-  constexpr int NS = kDecSlots, NC = kDecControl, ROUNDS = kDecRounds, WARPS = 8;
+  constexpr int NS = kDecSlots, NC = kDecControl, WARPS = 8;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
   constexpr uint32_t TB = WARPS * ROUNDS * BPR;
@@ -866,15 +880,14 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
     s_stop_k = kStopTile;
   }
   __syncthreads();
-  const float eb = a.plan->eb;
-  const bool ebsp = !isfinite(eb);
   if (warp == WARPS + NC) {
-    if (lane == 0) dec_producer<L, TB, NS>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
+    if (lane == 0)
+      dec_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
     return;
   }
   if (warp >= WARPS) {
     dec_control<NS, NC, TB>(warp - WARPS, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_staged, s_empty,
-                            &s_epoch, &s_stop_k, eb, ebsp);
+                            &s_epoch, &s_stop_k);
     return;
   }
 
@@ -961,7 +974,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
       rbase[r] = wtot;
       wtot += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
+    if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(s_meta[s].err, kErrCorrupt);
 
     // ---- tile scan over the warps (its first barrier ends every read of the span) ----
     if (lane == 0) s_w[warp] = wtot;
@@ -1007,24 +1020,25 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
 // Any blockSize, fastmode1 or fastmode2: one warp per block in 32-element
 // pieces.  fastmode1 decodes twice (totals, then values after the look-back).
 template <int WARPS, bool FM2>
-__global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
+__global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_constant__ DecArgs a) {
+  const DecField& fd = a.f;
   __shared__ uint32_t s_tk[2];
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint32_t s_base;
   uint32_t tile, epoch;
   draw_ticket(a.ls, a.ntiles, tile, epoch, s_tk);
-  if (a.plan->bad) return;
+  if (fd.plan->bad) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const Segments sg = a.seg;
+  const Segments sg = fd.seg;
   const uint32_t L = sg.L;
   const uint32_t TB = WARPS * a.bpw;
-  const DecTile dt = dec_tile(sg, tile, a.tiles_per_seg, TB, FM2);
+  const DecTile dt = dec_tile(sg, tile, fd.tiles_per_seg, TB, FM2);
   if (!dt.any) return;
-  const float eb = a.plan->eb;
+  const float eb = fd.plan->eb;
   const bool ebsp = !isfinite(eb);
   const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
-  const uint64_t R0 = a.reg0[dt.seg], R1 = a.reg1[dt.seg];
-  const uint8_t* __restrict__ in = a.in;
+  const uint64_t R0 = fd.reg0[dt.seg], R1 = fd.reg1[dt.seg];
+  const uint8_t* __restrict__ in = fd.in;
   const uint64_t gb = seg_block_base(sg, dt.seg, FM2);
   const uint32_t wfirst = warp * a.bpw;
   bool corrupt = false;
@@ -1039,7 +1053,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
   };
   // block header pointer and validation; returns bc or 255 when corrupt
   auto blk_hdr = [&](uint64_t b, uint32_t m, uint64_t& hp) -> uint32_t {
-    hp = R0 + __ldg(a.blkpos + gb + b) + (FM2 ? 4 : 0);
+    hp = R0 + __ldg(fd.blkpos + gb + b) + (FM2 ? 4 : 0);
     if (FM2 && m == 0) return 0;  // one-element block: no header is read (szpd_float.cc:481)
     if (hp >= R1) return 255u;
     uint32_t bc = __ldg(in + hp);
@@ -1070,7 +1084,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
     }
     uint32_t wexcl;
     const uint32_t agg = scan_warps_u32<WARPS>(s_w, wtot, warp, lane, wexcl);
-    const uint32_t first_tile = a.tiles_per_seg ? dt.seg * a.tiles_per_seg : 0;
+    const uint32_t first_tile = fd.tiles_per_seg ? dt.seg * fd.tiles_per_seg : 0;
     if (warp == 0) {
       uint32_t excl;
       if (dt.first) {
@@ -1078,7 +1092,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
         excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
         if (lane == 0) {
           st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
-          a.y[lo] = dequant(excl, eb, ebsp);
+          fd.y[lo] = dequant(excl, eb, ebsp);
         }
       } else {
         if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
@@ -1106,17 +1120,17 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(DecArgs a) {
       const uint8_t* sp = in + hp - 4;
       q0 = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
            ((uint32_t)__ldg(sp + 3) << 24);
-      if (lane == 0) a.y[s - 1] = dequant(q0, eb, ebsp);
+      if (lane == 0) fd.y[s - 1] = dequant(q0, eb, ebsp);
     }
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       uint32_t d = (bc && j < m) ? decode_delta(in + hp, m, bc, j) : 0u;
       uint32_t sc = warp_incl_scan(d, lane);
-      if (j < m) a.y[s + j] = dequant(q0 + sc, eb, ebsp);
+      if (j < m) fd.y[s + j] = dequant(q0 + sc, eb, ebsp);
       q0 += __shfl_sync(0xffffffffu, sc, 31);
     }
   }
-  if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(a.err, kErrCorrupt);
+  if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(fd.err, kErrCorrupt);
 }
 
 static int dec_lanes_per_block(uint32_t L) {
@@ -1148,25 +1162,34 @@ size_t decode_smem_bytes(uint32_t L, uint32_t tb, bool fm2) {
 }
 
 cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st) {
-  dec_setup_kernel<<<1, 256, 0, st>>>(a);
+  dec_setup_kernel<false><<<1, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStream_t st) {
+  if (nfields == 0) return cudaSuccess;
+  dec_setup_kernel<true><<<nfields, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <bool FM2, bool BATCH>
+static cudaError_t launch_locate_t(const DecArgs& a, cudaStream_t st) {
+  const size_t smem = locate_smem_bytes(a.super_chunk, a.overlap, a.maxsz);
+  auto k = locate_kernel<FM2, BATCH>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.nlocate_ctas, kLocThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st) {
   if (a.nlocate_ctas == 0) return cudaSuccess;
-  const size_t smem = locate_smem_bytes(a.super_chunk, a.overlap, a.maxsz);
-  if (a.fm2) {
-    auto k = locate_kernel<true>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<a.nlocate_ctas, kLocThreads, smem, st>>>(a);
-  } else {
-    auto k = locate_kernel<false>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<a.nlocate_ctas, kLocThreads, smem, st>>>(a);
-  }
-  return cudaGetLastError();
+  return a.fm2 ? launch_locate_t<true, false>(a, st) : launch_locate_t<false, false>(a, st);
+}
+
+cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st) {
+  if (a.nlocate_ctas == 0) return cudaSuccess;
+  return launch_locate_t<false, true>(a, st);
 }
 
 // Bytes of one decode slot: the block offsets, then the stream span or the
@@ -1176,10 +1199,10 @@ static uint32_t dec_slot_bytes(uint32_t L, uint32_t tb, uint32_t maxsz) {
   return (uint32_t)((dec_pos_bytes(tb) + (span > stage ? span : stage) + 15) & ~(size_t)15);
 }
 
-template <int LPB>
+template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds>
 static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
-  auto k = decode_fm1_pipe<LPB>;
-  const uint32_t slot = dec_slot_bytes(a.seg.L, a.tb, a.maxsz);
+  auto k = decode_fm1_pipe<LPB, BATCH, ROUNDS>;
+  const uint32_t slot = dec_slot_bytes(8 * LPB, a.tb, a.maxsz);
   const size_t smem = (size_t)kDecSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
   static std::atomic<uint64_t> s_cache{0};
@@ -1210,7 +1233,7 @@ cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {
     decode_generic<kDecWarps, true><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
     return cudaGetLastError();
   }
-  switch (dec_lanes_per_block(a.seg.L)) {
+  switch (dec_lanes_per_block(a.f.seg.L)) {
     case 1: return launch_dec_lanes<1>(a, st);
     case 2: return launch_dec_lanes<2>(a, st);
     case 4: return launch_dec_lanes<4>(a, st);
@@ -1221,6 +1244,17 @@ cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {
   }
   decode_generic<kDecWarps, false><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
   return cudaGetLastError();
+}
+
+// Batched fastmode1 decode, blockSize 32, tiles of 8*rounds*8 blocks.
+cudaError_t launch_decode_batch(const DecArgs& a, uint32_t L, int rounds, cudaStream_t st) {
+  if (L != 32) return cudaErrorInvalidValue;
+  switch (rounds) {
+    case 1: return launch_dec_lanes<4, true, 1>(a, st);
+    case 2: return launch_dec_lanes<4, true, 2>(a, st);
+    case 4: return launch_dec_lanes<4, true, 4>(a, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace szp

@@ -8,6 +8,24 @@
 
 namespace szp {
 
+// One field of a batched compression (a device array, one entry per field).
+struct CompressField {
+  const float* x;
+  uint8_t* out;
+  uint64_t cap;          // bytes available at out
+  Segments seg;
+  uint64_t nb_reg;       // blocks of segments 0..T-2
+  uint64_t nb_last;      // blocks of segment T-1
+  uint32_t tiles_per_seg;
+  uint32_t ntiles;       // tiles of this field
+  uint32_t tile_base;    // its first tile in the launch
+  float eb;              // the bound (REL: written by the range pass)
+  float rel;             // (float)relBoundRatio, or 0 for ABS
+  uint32_t pad;
+  uint64_t* out_size;    // stream bytes of this field
+  uint32_t* err;         // this field's error word
+};
+
 struct CompressArgs {
   const float* x;
   uint8_t* out;
@@ -26,6 +44,26 @@ struct CompressArgs {
   uint64_t nb_reg;       // blocks of segments 0..T-2
   uint64_t nb_last;      // blocks of segment T-1
   BitcountTable thr;
+  // batched launches: tiles of all fields, field of each tile
+  const CompressField* fields;
+  const uint32_t* tile_field;
+};
+
+// Per-field state of the batched range pass: order-preserving encodings of
+// the running min and max, chunks done, and the field's chunk count.  The
+// last chunk of a field computes its bound and resets the state.
+struct RelFieldState {
+  uint32_t mn, mx, done, nitems;
+  uint32_t first_item;  // the field's first work item
+  uint32_t pad[3];
+};
+
+struct RelBatchArgs {
+  CompressField* fields;        // eb written for REL fields
+  RelFieldState* state;         // per field
+  const uint32_t* item_field;   // work item -> field
+  uint32_t nitems;
+  uint32_t chunk;               // elements per work item
 };
 
 struct RelArgs {
@@ -46,39 +84,56 @@ struct DecPlan {
   // followed in memory by: uint32 chunk_base[T+1]; uint64 reg0[T]; uint64 reg1[T]
 };
 
-struct DecArgs {
-  const uint8_t* in;     // stream (device)
-  uint64_t len;          // stream bytes available
+// One field of a decompression: its stream, geometry, plan and output.
+struct DecField {
+  const uint8_t* in;        // stream (device)
+  uint64_t len;             // stream bytes available
   const uint64_t* len_dev;  // optional device-side stream length (min with len)
   Segments seg;
-  bool fm2;
   DecPlan* plan;
-  uint32_t* chunk_base;  // [T+1]
-  uint64_t* reg0;        // [T] absolute start of each segment's block region
-  uint64_t* reg1;        // [T] absolute end of it (exclusive)
+  uint32_t* chunk_base;     // [T+1] locate chunks before each segment
+  uint64_t* reg0;           // [T] absolute start of each segment's block region
+  uint64_t* reg1;           // [T] absolute end of it (exclusive)
+  uint32_t* blkpos;         // per block: header offset relative to its segment's region start
+  uint64_t nblk_total;
+  float* y;                 // output
+  uint32_t ntiles;          // decode tiles of this field
+  uint32_t tiles_per_seg;
+  uint32_t tile_base;       // its first decode tile in the launch
+  uint32_t loc_base;        // its first locate ticket in the launch
+  uint32_t loc_ctas;        // locate tickets it may use
+  uint32_t* err;            // this field's error word
+};
+
+struct DecArgs {
+  DecField f;            // the field of a single-field launch
+  bool fm2;
   uint32_t chunk;        // bytes per locate thread
   uint32_t super_chunk;  // bytes per locate CTA (chunk * threads)
   uint32_t overlap;      // bytes walked before a CTA's region to find the header chain
   uint32_t maxsz;        // largest block (including a fastmode2 seed)
-  uint2* aux;            // per locate CTA: (entry, exit) of its header chain
+  uint2* aux;            // per locate ticket: (entry, exit) of its header chain
   uint32_t* counters;    // [0] repairs of the last launch
   uint64_t* status;      // look-back words
   LaunchState* ls;
-  uint32_t* err;
-  uint32_t* blkpos;      // per block: header offset relative to its segment's region start
-  uint64_t nblk_total;
-  float* y;              // output
-  uint32_t ntiles;
-  uint32_t tiles_per_seg;
+  uint32_t* err;         // launch error word (waits that gave up)
+  uint32_t ntiles;       // decode tiles of the launch
   uint32_t tb;
   uint32_t bpw;
-  uint32_t nlocate_ctas; // CTAs of the locate kernel (upper bound)
+  uint32_t nlocate_ctas; // locate tickets of the launch (upper bound)
+  // batched launches
+  const DecField* fields;
+  const uint32_t* tile_field;  // decode tile -> field
+  const uint32_t* loc_field;   // locate ticket -> field
 };
 
 uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw);
 size_t compress_smem_bytes(uint32_t L, uint32_t tb);
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st);
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st);
+cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds, cudaStream_t st);
+cudaError_t launch_rel_batch(const RelBatchArgs& a, uint32_t grid, cudaStream_t st);
+uint32_t rel_encode_host(float v);
 cudaError_t launch_bitcount_probe(const uint32_t* in, uint8_t* out, uint64_t n, const BitcountTable& thr,
                                   cudaStream_t st);
 
@@ -92,6 +147,10 @@ size_t decode_smem_bytes(uint32_t L, uint32_t tb, bool fm2);
 cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st);
+// batched decompression (fastmode1, blockSize 32)
+cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStream_t st);
+cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st);
+cudaError_t launch_decode_batch(const DecArgs& a, uint32_t L, int rounds, cudaStream_t st);
 
 // host helpers (api.cu)
 const BitcountTable& host_bitcount_table();
@@ -99,6 +158,10 @@ int host_resolve_segments(int requested);
 void host_compress_tiles(size_t n, int T, int L, uint64_t& tiles_per_seg, uint64_t& ntiles, uint32_t& tb,
                          uint32_t& bpw);
 void host_segment_blocks(size_t n, int T, int L, uint64_t& nb_reg, uint64_t& nb_last);
+void host_tile_counts(size_t n, int T, int L, uint32_t tb, uint64_t& tiles_per_seg, uint64_t& ntiles);
+uint64_t host_block_count(size_t n, int T, int L);
+size_t host_max_stream_bytes(size_t n, int L, int T);
+int host_status_from_err(uint32_t err);
 int host_fail(int status, const char* msg);
 void host_clear_error();
 void host_count_launches(int k);
