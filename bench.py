@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--side", type=int, default=N_SIDE)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-fields", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -184,6 +186,88 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(s[1] for s in inw), "sm_max_mhz": self.max_mhz,
                 "reasons": sorted(reasons), "samples": len(inw), "source": self.source,
                 "power_w": round(statistics.median(watts), 1) if watts else None}
+
+
+def batched_workload(szp, torch, dev, T, nfields, reps=3, seed=11):
+    """1024 fields, log-normal sizes 4 KB..64 MB (median 1 MB), each a random
+    walk or a slice of a 3-D Fourier field, REL drawn log-uniform in
+    [1e-5, 1e-2]: one compress + decompress call per field against one batched
+    graph per direction, both on one stream, CUDA-event timed."""
+    from szp_gb300.workloads import fourier3d_torch, walk_torch
+    rng = np.random.default_rng(seed)
+    nbytes = np.clip(np.exp(rng.normal(np.log(1 << 20), 1.4, nfields)), 4096, 64 << 20)
+    ns = [int(b) // 4 for b in nbytes]
+    rels = [float(10 ** rng.uniform(-5, -2)) for _ in range(nfields)]
+    kinds = rng.integers(0, 2, nfields)
+    base = fourier3d_torch(384, seed, dev)
+    xs = []
+    for i, n in enumerate(ns):
+        if kinds[i] == 1 and n <= base.numel():
+            off = int(rng.integers(0, base.numel() - n + 1))
+            xs.append(base[off:off + n].clone())
+        else:
+            xs.append(walk_torch(n, seed * 100003 + i, dev))
+    del base
+    caps = [szp.max_stream_bytes(n, L, T, 1) for n in ns]
+    streams = [torch.empty(c, dtype=torch.uint8, device=dev) for c in caps]
+    outs = [torch.empty(max(n, 1), dtype=torch.float32, device=dev) for n in ns]
+    d_sizes = torch.zeros(nfields, dtype=torch.int64, device=dev)
+    total = 4.0 * sum(ns)
+    st = torch.cuda.current_stream(dev).cuda_stream
+
+    def per_field():
+        for i in range(nfields):
+            szp.compress_dev_async(xs[i].data_ptr(), ns[i], streams[i].data_ptr(), caps[i],
+                                   d_sizes.data_ptr() + 8 * i, szp.REL, 0.0, rels[i], L, T, 1, st)
+            szp.decompress_dev_async(streams[i].data_ptr(), caps[i], d_sizes.data_ptr() + 8 * i, ns[i],
+                                     outs[i].data_ptr(), L, T, 1, st)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            best = t if best is None else min(best, t)
+        return best
+
+    ms_single = timed(per_field)
+    assert szp.sync_status(st) == 0, szp.last_error()
+    ref = [outs[i][:ns[i]].clone() for i in range(0, nfields, 97)]
+    cf = [dict(input=xs[i].data_ptr(), output=streams[i].data_ptr(), output_bytes=caps[i], nbEle=ns[i],
+               errBoundMode=szp.REL, relBoundRatio=rels[i]) for i in range(nfields)]
+    cb = szp.Batch(szp.BATCH_COMPRESS, cf, L, T, szp.BATCH_AUTOTUNE)
+    cb.run(st)
+    cb.sync()
+    df = [dict(input=streams[i].data_ptr(), input_bytes=caps[i], input_len_dev=cb.sizes_dev() + 8 * i,
+               output=outs[i].data_ptr(), output_bytes=4 * max(ns[i], 1), nbEle=ns[i]) for i in range(nfields)]
+    db = szp.Batch(szp.BATCH_DECOMPRESS, df, L, T, szp.BATCH_AUTOTUNE)
+
+    def batched():
+        cb.run(st)
+        db.run(st)
+
+    ms_batch = timed(batched)
+    cb.sync()
+    db.sync()
+    for k, i in enumerate(range(0, nfields, 97)):
+        assert torch.equal(outs[i][:ns[i]], ref[k]), "batched result differs from the per-field calls"
+    res = {"fields": nfields, "bytes": int(total), "median_field_bytes": int(np.median(nbytes)),
+           "per_field_ms": round(ms_single, 3), "batched_ms": round(ms_batch, 3),
+           "per_field_gbs": round(total / (ms_single / 1e3) / 1e9, 2),
+           "batched_gbs": round(total / (ms_batch / 1e3) / 1e9, 2),
+           "speedup": round(ms_single / ms_batch, 2),
+           "tile_rounds": {"compress": cb.tile_rounds(), "decompress": db.tile_rounds()},
+           "metric": "aggregate round-trip GB/s (compress + decompress, uncompressed bytes)",
+           "launches": "per field: 5 kernels x %d fields; batched: 2 graphs (5 kernels)" % nfields}
+    cb.close()
+    db.close()
+    return res
 
 
 def dist_setup(args):
@@ -394,6 +478,10 @@ def main():
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
                "api": "szp_compress + szp_decompress (C ABI via ctypes; pinned input, library-malloc'd results)"}
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_workload(szp, torch, dev, T, args.batched_fields)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle.oracle import Port
@@ -423,6 +511,7 @@ def main():
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "batched": batched,
             "gpu_launches": int(launches),
             "clocks": clk,
         }
