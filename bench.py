@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serving-window", type=float, default=0.2, help="seconds of arrivals per rate")
     ap.add_argument("--batched-fields", type=int, default=1024)
     return ap.parse_args()
 
@@ -270,6 +272,82 @@ def batched_workload(szp, torch, dev, T, nfields, reps=3, seed=11):
     return res
 
 
+def serving_workload(szp, torch, dev, T, window, rates=(2000, 5000, 10000, 20000, 50000), seed=13,
+                     budget=40 << 30):
+    """Poisson arrivals, 60% compress / 40% decompress, sizes log-normal
+    (median 1 MB, 4 KB..64 MB), REL log-uniform in [1e-5, 1e-2], results kept
+    on the device under a 40 GB admission budget.  The continuous-batching
+    server (64 requests per group, 3 lanes) against the same server taking one
+    request at a time; latency is completion minus scheduled arrival."""
+    from szp_gb300.workloads import fourier3d_torch, walk_torch
+    rng = np.random.default_rng(seed)
+    npool = 48
+    ns = [int(b) // 4 for b in np.clip(np.exp(rng.normal(np.log(1 << 20), 1.4, npool)), 4096, 64 << 20)]
+    base = fourier3d_torch(256, seed, dev)
+    st = torch.cuda.current_stream(dev).cuda_stream  # the stream the fields are made on
+    pool = []
+    for i, n in enumerate(ns):
+        if i % 2 and n <= base.numel():
+            off = int(rng.integers(0, base.numel() - n + 1))
+            x = base[off:off + n].clone()
+        else:
+            x = walk_torch(n, seed * 7919 + i, dev)
+        cap = szp.max_stream_bytes(n, L, T, 1)
+        d_s = torch.empty(cap, dtype=torch.uint8, device=dev)
+        rel = float(10 ** rng.uniform(-5, -2))
+        size = szp.compress_dev(x.data_ptr(), n, d_s.data_ptr(), cap, szp.REL, 0.0, rel, L, T, 1, st)
+        pool.append((x, n, rel, d_s, size))
+    del base
+    torch.cuda.synchronize()
+
+    def run(rate, max_batch, lanes):
+        srv = szp.Server(budget, max_batch=max_batch, lanes=lanes, segments=T)
+        r2 = np.random.default_rng(seed + rate)
+        count = max(1, int(rate * window))
+        arr = np.cumsum(r2.exponential(1.0 / rate, count))
+        reqs = []
+        for k in range(count):
+            x, n, rel, d_s, size = pool[int(r2.integers(0, npool))]
+            if r2.random() < 0.6:
+                reqs.append(dict(op=szp.BATCH_COMPRESS, input=x.data_ptr(), nbEle=n, errBoundMode=szp.REL,
+                                 relBoundRatio=float(10 ** r2.uniform(-5, -2))))
+            else:
+                reqs.append(dict(op=szp.BATCH_DECOMPRESS, input=d_s.data_ptr(), input_bytes=size, nbEle=n))
+        t0 = srv.clock() + 0.002
+        nxt, lat, nbytes, done, last = 0, [], 0, 0, t0
+        while done < count:
+            now = srv.clock()
+            k = nxt
+            while k < count and t0 + arr[k] <= now:
+                k += 1
+            if k > nxt:
+                batch = reqs[nxt:k]
+                for j, r in enumerate(batch):
+                    r["arrival"] = t0 + arr[nxt + j]
+                srv.submit(batch)
+                nxt = k
+            for res in srv.completed():
+                assert res["status"] == 0, res
+                lat.append(res["done"] - res["arrival"])
+                last = max(last, res["done"])
+                srv.release(res["id"])
+                done += 1
+        st = srv.stats()
+        nbytes = st["bytes"]
+        srv.close()
+        lat = np.array(lat) * 1e3
+        span = last - t0
+        return {"requests": count, "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                "gbs": round(nbytes / span / 1e9, 2), "offered_gbs": round(nbytes / (arr[-1] + 1e-9) / 1e9, 2),
+                "peak_memory_gb": round(st["memory_peak"] / 1e9, 2)}
+
+    out = {"window_s": window, "budget_gb": budget / 1e9, "rates": {}}
+    for rate in rates:
+        out["rates"][str(rate)] = {"batched": run(rate, 64, 3), "one_at_a_time": run(rate, 1, 1)}
+    return out
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -482,6 +560,10 @@ def main():
     if not args.no_batched:
         batched = batched_workload(szp, torch, dev, T, args.batched_fields)
 
+    serving = None
+    if not args.no_serving:
+        serving = serving_workload(szp, torch, dev, T, args.serving_window)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle.oracle import Port
@@ -512,6 +594,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "batched": batched,
+            "serving": serving,
             "gpu_launches": int(launches),
             "clocks": clk,
         }

@@ -268,6 +268,61 @@ const unsigned long long *szp_gb300_batch_sizes_dev(szp_gb300_batch b);
 int szp_gb300_batch_tile_rounds(szp_gb300_batch b);
 void szp_gb300_batch_destroy(szp_gb300_batch b);
 
+/* ---- request server: continuous batching on device-resident data (no
+ * counterpart in the reference) ----
+ * Requests are admitted in arrival order while their results fit the HBM
+ * budget, launched in groups (one compress batch + one decompress batch per
+ * group) on up to `lanes` streams at once, and keep their results on the
+ * device until released.  Every result is byte-identical to the single-field
+ * calls on the same input.  blockSize is 32. */
+typedef struct {
+  int op;                 /* SZP_GB300_BATCH_COMPRESS or SZP_GB300_BATCH_DECOMPRESS */
+  const void *input;      /* device: float[nbEle] (compress) or a stream (decompress) */
+  size_t input_bytes;     /* decompress: stream bytes */
+  size_t nbEle;
+  int errBoundMode;       /* compress: ABS or REL */
+  double absErrBound;
+  double relBoundRatio;
+  double arrival;         /* server-clock seconds; < 0: the submission time */
+} szp_gb300_request;
+
+typedef struct {
+  unsigned long long id;
+  int status;             /* SZP_GB300_* */
+  void *output;           /* device: the stream or float[nbEle], valid until released */
+  size_t output_bytes;    /* stream bytes, or 4 * nbEle */
+  double arrival, admitted, done; /* server-clock seconds */
+} szp_gb300_result;
+
+typedef struct {
+  size_t hbm_budget;      /* device bytes for results (one arena) */
+  int max_batch;          /* requests per group at most */
+  int lanes;              /* groups in flight at once, 1..16 */
+  int segments;           /* T of every stream; <= 0: OpenMP's thread count */
+  int tile_rounds;        /* 1, 2 or 4; 0: chosen per group from the request sizes */
+} szp_gb300_server_config;
+
+typedef struct {
+  unsigned long long requests, bytes, queued, in_flight, memory_used, memory_peak;
+} szp_gb300_server_stats;
+
+typedef struct szp_gb300_server_s *szp_gb300_server;
+
+int szp_gb300_server_create(szp_gb300_server *out, const szp_gb300_server_config *cfg);
+/* Queues n requests; ids[i] receives each one's id (ids may be NULL). */
+int szp_gb300_server_submit(szp_gb300_server s, const szp_gb300_request *reqs, int n, unsigned long long *ids);
+/* Results finished since the last call, at most max; returns how many. */
+int szp_gb300_server_completed(szp_gb300_server s, szp_gb300_result *res, int max);
+/* Blocks until request id has finished; returns its status. */
+int szp_gb300_server_wait(szp_gb300_server s, unsigned long long id, szp_gb300_result *res);
+/* Frees a finished request's result. */
+int szp_gb300_server_release(szp_gb300_server s, unsigned long long id);
+/* Blocks until nothing is queued or running. */
+int szp_gb300_server_drain(szp_gb300_server s);
+int szp_gb300_server_get_stats(szp_gb300_server s, szp_gb300_server_stats *st);
+double szp_gb300_server_clock(szp_gb300_server s);
+void szp_gb300_server_destroy(szp_gb300_server s);
+
 #ifdef __cplusplus
 }
 #endif

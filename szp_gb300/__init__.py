@@ -91,6 +91,41 @@ _sig("szp_gb300_batch_sync", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_ulonglo
 _sig("szp_gb300_batch_sizes_dev", _vp, [_vp])
 _sig("szp_gb300_batch_tile_rounds", ctypes.c_int, [_vp])
 _sig("szp_gb300_batch_destroy", None, [_vp])
+
+
+class Request(ctypes.Structure):
+    """szp_gb300_request."""
+    _fields_ = [("op", ctypes.c_int), ("input", _vp), ("input_bytes", _sz), ("nbEle", _sz),
+                ("errBoundMode", ctypes.c_int), ("absErrBound", ctypes.c_double), ("relBoundRatio", ctypes.c_double),
+                ("arrival", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    """szp_gb300_result."""
+    _fields_ = [("id", ctypes.c_ulonglong), ("status", ctypes.c_int), ("output", _vp), ("output_bytes", _sz),
+                ("arrival", ctypes.c_double), ("admitted", ctypes.c_double), ("done", ctypes.c_double)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", _sz), ("max_batch", ctypes.c_int), ("lanes", ctypes.c_int),
+                ("segments", ctypes.c_int), ("tile_rounds", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_ulonglong) for k in
+                ("requests", "bytes", "queued", "in_flight", "memory_used", "memory_peak")]
+
+
+_sig("szp_gb300_server_create", ctypes.c_int, [ctypes.POINTER(_vp), ctypes.POINTER(ServerConfig)])
+_sig("szp_gb300_server_submit", ctypes.c_int, [_vp, ctypes.POINTER(Request), ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_ulonglong)])
+_sig("szp_gb300_server_completed", ctypes.c_int, [_vp, ctypes.POINTER(Result), ctypes.c_int])
+_sig("szp_gb300_server_wait", ctypes.c_int, [_vp, ctypes.c_ulonglong, ctypes.POINTER(Result)])
+_sig("szp_gb300_server_release", ctypes.c_int, [_vp, ctypes.c_ulonglong])
+_sig("szp_gb300_server_drain", ctypes.c_int, [_vp])
+_sig("szp_gb300_server_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)])
+_sig("szp_gb300_server_clock", ctypes.c_double, [_vp])
+_sig("szp_gb300_server_destroy", None, [_vp])
 _sig("szp_gb300_last_repairs", ctypes.c_int, [])
 
 _libc = ctypes.CDLL(None)
@@ -404,6 +439,80 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None):
             _lib.szp_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _result_dict(r):
+    return dict(id=int(r.id), status=int(r.status), output=r.output or 0, output_bytes=int(r.output_bytes),
+                arrival=r.arrival, admitted=r.admitted, done=r.done)
+
+
+class Server:
+    """The request server (szp_gb300_server_*): continuous batching of compress
+    and decompress requests on device-resident data under an HBM budget."""
+
+    def __init__(self, hbm_budget, max_batch=256, lanes=3, segments=0, tile_rounds=0):
+        cfg = ServerConfig(hbm_budget, max_batch, lanes, segments, tile_rounds)
+        h = _vp()
+        rc = _lib.szp_gb300_server_create(ctypes.byref(h), ctypes.byref(cfg))
+        if rc != 0:
+            raise SzpError(rc, "server_create failed: %s" % last_error())
+        self._h = h
+        self._buf = (Result * 4096)()
+
+    def clock(self):
+        return _lib.szp_gb300_server_clock(self._h)
+
+    def submit(self, reqs):
+        """reqs: list of dicts with the keys of szp_gb300_request; returns their ids."""
+        n = len(reqs)
+        arr = (Request * max(n, 1))()
+        for i, r in enumerate(reqs):
+            arr[i].arrival = -1.0
+            for k, v in r.items():
+                setattr(arr[i], k, v)
+        ids = (ctypes.c_ulonglong * max(n, 1))()
+        rc = _lib.szp_gb300_server_submit(self._h, arr, n, ids)
+        if rc != 0:
+            raise SzpError(rc, "server_submit failed: %s" % last_error())
+        return [int(v) for v in ids[:n]]
+
+    def completed(self):
+        """Results finished since the last call (dicts)."""
+        out = []
+        while True:
+            k = _lib.szp_gb300_server_completed(self._h, self._buf, len(self._buf))
+            out += [_result_dict(self._buf[i]) for i in range(k)]
+            if k < len(self._buf):
+                return out
+
+    def wait(self, rid):
+        r = Result()
+        _lib.szp_gb300_server_wait(self._h, rid, ctypes.byref(r))
+        return _result_dict(r)
+
+    def release(self, rid):
+        rc = _lib.szp_gb300_server_release(self._h, rid)
+        if rc != 0:
+            raise SzpError(rc, "server_release failed: %s" % last_error())
+
+    def drain(self):
+        return _lib.szp_gb300_server_drain(self._h)
+
+    def stats(self):
+        st = ServerStats()
+        _lib.szp_gb300_server_get_stats(self._h, ctypes.byref(st))
+        return {k: int(getattr(st, k)) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.szp_gb300_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -21,15 +21,13 @@
 #include <cstring>
 #include <vector>
 
+#include "szp_batch.h"
 #include "szp_gb300.h"
 #include "szp_kernels.h"
 
 using namespace szp;
 
 namespace {
-
-constexpr uint32_t kBatchL = 32;
-constexpr uint32_t kRelChunk = 1u << 18;  // floats per range-pass work item
 
 #define BCU(call)                                                                             \
   do {                                                                                        \
@@ -132,164 +130,49 @@ struct szp_gb300_batch_s {
 namespace {
 
 int build_compress(szp_gb300_batch_s& b, Config& c) {
-  const int nf = b.nfields, L = b.L, T = b.T;
-  const uint32_t tb = 8u * (uint32_t)c.rounds * (32u / 4u);
-  std::vector<CompressField> fs(nf);
-  std::vector<uint32_t> tile_field;
-  std::vector<uint32_t> item_field;
-  std::vector<RelFieldState> rs(nf);
-  uint64_t tiles = 0;
-  for (int f = 0; f < nf; f++) {
-    const szp_gb300_field& in = b.fields[f];
-    CompressField& cf = fs[f];
-    memset(&cf, 0, sizeof cf);
-    cf.x = static_cast<const float*>(in.input);
-    cf.out = static_cast<uint8_t*>(in.output);
-    cf.cap = in.output_bytes;
-    cf.seg.n = in.nbEle;
-    cf.seg.T = (uint32_t)T;
-    cf.seg.L = (uint32_t)L;
-    cf.seg.tsz = in.nbEle / (uint64_t)T;
-    host_segment_blocks(in.nbEle, T, L, cf.nb_reg, cf.nb_last);
-    uint64_t per_seg = 0, nt = 0;
-    host_tile_counts(in.nbEle, T, L, tb, per_seg, nt);
-    cf.tiles_per_seg = (uint32_t)per_seg;
-    cf.ntiles = (uint32_t)nt;
-    cf.tile_base = (uint32_t)tiles;
-    cf.out_size = reinterpret_cast<uint64_t*>(b.d_sizes + f);
-    cf.err = b.d_err + f;
-    RelFieldState& st = rs[f];
-    memset(&st, 0, sizeof st);
-    st.mn = rel_encode_host(INFINITY);
-    st.mx = rel_encode_host(-INFINITY);
-    if (in.errBoundMode == REL) {
-      cf.rel = (float)in.relBoundRatio;
-      if (in.nbEle == 0) {
-        cf.eb = empty_rel_bound(cf.rel);
-      } else {
-        st.first_item = (uint32_t)item_field.size();
-        st.nitems = (uint32_t)((in.nbEle + kRelChunk - 1) / kRelChunk);
-        for (uint32_t i = 0; i < st.nitems; i++) item_field.push_back((uint32_t)f);
-      }
-    } else {
-      cf.eb = (float)in.absErrBound;
-    }
-    tile_field.insert(tile_field.end(), nt, (uint32_t)f);
-    tiles += nt;
-    if (tiles >= (1ull << 31)) return host_fail(SZP_GB300_EINVAL, "batch too large for one launch");
-  }
+  const uint32_t tb = batch_tile_blocks(c.rounds);
+  CompressPlan p;
+  int rc = plan_compress(b.fields.data(), b.nfields, b.L, b.T, tb, p);
+  if (rc) return rc;
+  place_compress(p, b.d_sizes, b.d_err);
+  if (p.tiles > b.status_words) return host_fail(SZP_GB300_EINVAL, "look-back words too few for the batch");
   CompressField* d_fields;
   uint32_t *d_tile_field, *d_items;
   RelFieldState* d_state;
-  BCU(upload(c.al, &d_fields, fs));
-  BCU(upload(c.al, &d_tile_field, tile_field));
-  BCU(upload(c.al, &d_items, item_field));
-  BCU(upload(c.al, &d_state, rs));
-  if (tiles > b.status_words) return host_fail(SZP_GB300_EINVAL, "look-back words too few for the batch");
-
-  CompressArgs& a = c.ca;
-  memset(&a, 0, sizeof a);
-  a.seg.L = (uint32_t)L;
-  a.status = b.d_status;
-  a.ls = &b.d_misc->ls;
-  a.err = &b.d_misc->err;
-  a.ntiles = (uint32_t)tiles;
-  a.tb = tb;
-  a.thr = host_bitcount_table();
-  a.fields = d_fields;
-  a.tile_field = d_tile_field;
-  RelBatchArgs& r = c.ra;
-  r.fields = d_fields;
-  r.state = d_state;
-  r.item_field = d_items;
-  r.nitems = (uint32_t)item_field.size();
-  r.chunk = kRelChunk;
+  BCU(upload(c.al, &d_fields, p.fields));
+  BCU(upload(c.al, &d_tile_field, p.tile_field));
+  BCU(upload(c.al, &d_items, p.item_field));
+  BCU(upload(c.al, &d_state, p.rel));
+  args_compress(c.ca, c.ra, p, d_fields, d_tile_field, d_items, d_state, b.d_status, &b.d_misc->ls,
+                &b.d_misc->err, tb);
   int sms = 0;
   BCU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b.device));
-  c.rel_grid = (uint32_t)std::min<uint64_t>(r.nitems, (uint64_t)sms * 8);
+  c.rel_grid = (uint32_t)std::min<uint64_t>(c.ra.nitems, (uint64_t)sms * 8);
   return SZP_GB300_OK;
 }
 
 int build_decompress(szp_gb300_batch_s& b, Config& c) {
-  const int nf = b.nfields, L = b.L, T = b.T;
-  const uint32_t tb = 8u * (uint32_t)c.rounds * (32u / 4u);
-  const uint32_t maxsz = max_block_bytes((uint32_t)L);
-  const uint32_t C = locate_chunk_bytes(maxsz), SC = locate_super_bytes(maxsz);
-  std::vector<DecField> fs(nf);
-  std::vector<uint32_t> tile_field, loc_field;
-  uint64_t tiles = 0, locs = 0, blocks = 0;
-  // per field: DecPlan, reg0[T], reg1[T], chunk_base[T+1], 16-byte aligned
-  const size_t plan_stride = ((sizeof(DecPlan) + 16ull * T + 4ull * (T + 1)) + 15) & ~(size_t)15;
+  const uint32_t tb = batch_tile_blocks(c.rounds);
+  DecompressPlan p;
+  int rc = plan_decompress(b.fields.data(), b.nfields, b.L, b.T, tb, p);
+  if (rc) return rc;
+  if (p.tiles > b.status_words || p.locs > b.status_words)
+    return host_fail(SZP_GB300_EINVAL, "look-back words too few for the batch");
   uint8_t* d_plans;
-  BCU(c.al.get(&d_plans, plan_stride * (size_t)nf));
-  for (int f = 0; f < nf; f++) {
-    const szp_gb300_field& in = b.fields[f];
-    DecField& df = fs[f];
-    memset(&df, 0, sizeof df);
-    df.in = static_cast<const uint8_t*>(in.input);
-    df.len = in.input_bytes;
-    df.len_dev = reinterpret_cast<const uint64_t*>(in.input_len_dev);
-    df.seg.n = in.nbEle;
-    df.seg.T = (uint32_t)T;
-    df.seg.L = (uint32_t)L;
-    df.seg.tsz = in.nbEle / (uint64_t)T;
-    uint8_t* pb = d_plans + plan_stride * (size_t)f;
-    df.plan = reinterpret_cast<DecPlan*>(pb);
-    df.reg0 = reinterpret_cast<uint64_t*>(pb + sizeof(DecPlan));
-    df.reg1 = df.reg0 + T;
-    df.chunk_base = reinterpret_cast<uint32_t*>(df.reg1 + T);
-    df.nblk_total = host_block_count(in.nbEle, T, L);
-    df.y = static_cast<float*>(in.output);
-    uint64_t per_seg = 0, nt = 0;
-    host_tile_counts(in.nbEle, T, L, tb, per_seg, nt);
-    df.ntiles = (uint32_t)nt;
-    df.tiles_per_seg = (uint32_t)per_seg;
-    df.tile_base = (uint32_t)tiles;
-    const uint64_t nloc = in.input_bytes / SC + (uint64_t)T + 1;
-    df.loc_base = (uint32_t)locs;
-    df.loc_ctas = (uint32_t)nloc;
-    df.err = b.d_err + f;
-    df.blkpos = reinterpret_cast<uint32_t*>(blocks);  // offset, made a pointer below
-    tile_field.insert(tile_field.end(), nt, (uint32_t)f);
-    loc_field.insert(loc_field.end(), nloc, (uint32_t)f);
-    tiles += nt;
-    locs += nloc;
-    blocks += df.nblk_total;
-    if (tiles >= (1ull << 31) || locs >= (1ull << 31)) return host_fail(SZP_GB300_EINVAL, "batch too large");
-  }
   uint32_t* d_blkpos;
-  BCU(c.al.get(&d_blkpos, blocks + 1));
-  for (auto& df : fs) df.blkpos = d_blkpos + reinterpret_cast<uintptr_t>(df.blkpos);
   uint2* d_aux;
-  BCU(c.al.get(&d_aux, locs + 1));
+  BCU(c.al.get(&d_plans, p.plan_stride * (size_t)b.nfields + 16));
+  BCU(c.al.get(&d_blkpos, p.blocks + 1));
+  BCU(c.al.get(&d_aux, p.locs + 1));
+  place_decompress(p, d_plans, d_blkpos, b.d_err);
   DecField* d_fields;
   uint32_t *d_tile_field, *d_loc_field;
-  BCU(upload(c.al, &d_fields, fs));
-  BCU(upload(c.al, &d_tile_field, tile_field));
-  BCU(upload(c.al, &d_loc_field, loc_field));
-  if (tiles > b.status_words || locs > b.status_words)
-    return host_fail(SZP_GB300_EINVAL, "look-back words too few for the batch");
-
-  DecArgs& a = c.da;
-  memset(&a, 0, sizeof a);
-  a.fm2 = false;
-  a.chunk = C;
-  a.super_chunk = SC;
-  a.overlap = locate_overlap_bytes(maxsz);
-  a.maxsz = maxsz;
-  a.aux = d_aux;
-  a.counters = b.d_misc->counters;
-  a.status = b.d_status;
-  a.ls = &b.d_misc->ls;
-  a.err = &b.d_misc->err;
-  a.ntiles = (uint32_t)tiles;
-  a.tb = tb;
-  a.bpw = tb / 8;
-  a.nlocate_ctas = (uint32_t)locs;
-  a.fields = d_fields;
-  a.tile_field = d_tile_field;
-  a.loc_field = d_loc_field;
-  c.nfields = (uint32_t)nf;
+  BCU(upload(c.al, &d_fields, p.fields));
+  BCU(upload(c.al, &d_tile_field, p.tile_field));
+  BCU(upload(c.al, &d_loc_field, p.loc_field));
+  args_decompress(c.da, p, d_fields, d_tile_field, d_loc_field, d_aux, b.d_misc->counters, b.d_status,
+                  &b.d_misc->ls, &b.d_misc->err, tb);
+  c.nfields = (uint32_t)b.nfields;
   return SZP_GB300_OK;
 }
 
@@ -297,15 +180,8 @@ int build_decompress(szp_gb300_batch_s& b, Config& c) {
 int issue(szp_gb300_batch_s& b, const Config& c, cudaStream_t st) {
   BCU(cudaMemsetAsync(b.d_err, 0, sizeof(uint32_t) * (size_t)b.nfields, st));
   BCU(cudaMemsetAsync(&b.d_misc->err, 0, sizeof(uint32_t) * 5, st));  // launch error + counters
-  if (b.dir == SZP_GB300_BATCH_COMPRESS) {
-    if (c.ra.nitems) BCU(launch_rel_batch(c.ra, c.rel_grid, st));
-    if (c.ca.ntiles) BCU(launch_compress_batch(c.ca, (uint32_t)b.L, c.rounds, st));
-  } else {
-    BCU(launch_dec_setup_batch(c.da, c.nfields, st));
-    BCU(launch_locate_batch(c.da, st));
-    if (c.da.ntiles) BCU(launch_decode_batch(c.da, (uint32_t)b.L, c.rounds, st));
-  }
-  return SZP_GB300_OK;
+  if (b.dir == SZP_GB300_BATCH_COMPRESS) return issue_compress(c.ca, c.ra, c.rel_grid, c.rounds, st);
+  return issue_decompress(c.da, c.nfields, c.rounds, st);
 }
 
 int make_config(szp_gb300_batch_s& b, int rounds, Config** out) {
@@ -365,6 +241,179 @@ void capture(szp_gb300_batch_s& b) {
 }
 
 }  // namespace
+
+namespace szp {
+
+int plan_compress(const szp_gb300_field* fl, int nf, int L, int T, uint32_t tb, CompressPlan& p) {
+  p.fields.assign(nf, CompressField{});
+  p.rel.assign(nf, RelFieldState{});
+  p.tile_field.clear();
+  p.item_field.clear();
+  p.tiles = 0;
+  for (int f = 0; f < nf; f++) {
+    const szp_gb300_field& in = fl[f];
+    CompressField& cf = p.fields[f];
+    memset(&cf, 0, sizeof cf);
+    cf.x = static_cast<const float*>(in.input);
+    cf.out = static_cast<uint8_t*>(in.output);
+    cf.cap = in.output_bytes;
+    cf.seg.n = in.nbEle;
+    cf.seg.T = (uint32_t)T;
+    cf.seg.L = (uint32_t)L;
+    cf.seg.tsz = in.nbEle / (uint64_t)T;
+    host_segment_blocks(in.nbEle, T, L, cf.nb_reg, cf.nb_last);
+    uint64_t per_seg = 0, nt = 0;
+    host_tile_counts(in.nbEle, T, L, tb, per_seg, nt);
+    cf.tiles_per_seg = (uint32_t)per_seg;
+    cf.ntiles = (uint32_t)nt;
+    cf.tile_base = (uint32_t)p.tiles;
+    cf.out_size = reinterpret_cast<uint64_t*>((uintptr_t)f);
+    cf.err = reinterpret_cast<uint32_t*>((uintptr_t)f);
+    RelFieldState& st = p.rel[f];
+    memset(&st, 0, sizeof st);
+    st.mn = rel_encode_host(INFINITY);
+    st.mx = rel_encode_host(-INFINITY);
+    if (in.errBoundMode == REL) {
+      cf.rel = (float)in.relBoundRatio;
+      if (in.nbEle == 0) {
+        cf.eb = empty_rel_bound(cf.rel);
+      } else {
+        st.first_item = (uint32_t)p.item_field.size();
+        st.nitems = (uint32_t)((in.nbEle + kRelChunk - 1) / kRelChunk);
+        for (uint32_t i = 0; i < st.nitems; i++) p.item_field.push_back((uint32_t)f);
+      }
+    } else {
+      cf.eb = (float)in.absErrBound;
+    }
+    p.tile_field.insert(p.tile_field.end(), nt, (uint32_t)f);
+    p.tiles += nt;
+    if (p.tiles >= (1ull << 31)) return host_fail(SZP_GB300_EINVAL, "batch too large for one launch");
+  }
+  return SZP_GB300_OK;
+}
+
+void place_compress(CompressPlan& p, unsigned long long* d_sizes, uint32_t* d_err) {
+  for (auto& cf : p.fields) {
+    const uintptr_t f = reinterpret_cast<uintptr_t>(cf.err);
+    cf.out_size = reinterpret_cast<uint64_t*>(d_sizes + f);
+    cf.err = d_err + f;
+  }
+}
+
+int plan_decompress(const szp_gb300_field* fl, int nf, int L, int T, uint32_t tb, DecompressPlan& p) {
+  const uint32_t maxsz = max_block_bytes((uint32_t)L);
+  const uint32_t SC = locate_super_bytes(maxsz);
+  p.fields.assign(nf, DecField{});
+  p.tile_field.clear();
+  p.loc_field.clear();
+  p.tiles = p.locs = p.blocks = 0;
+  p.plan_stride = ((sizeof(DecPlan) + 16ull * T + 4ull * (T + 1)) + 15) & ~(size_t)15;
+  for (int f = 0; f < nf; f++) {
+    const szp_gb300_field& in = fl[f];
+    DecField& df = p.fields[f];
+    memset(&df, 0, sizeof df);
+    df.in = static_cast<const uint8_t*>(in.input);
+    df.len = in.input_bytes;
+    df.len_dev = reinterpret_cast<const uint64_t*>(in.input_len_dev);
+    df.seg.n = in.nbEle;
+    df.seg.T = (uint32_t)T;
+    df.seg.L = (uint32_t)L;
+    df.seg.tsz = in.nbEle / (uint64_t)T;
+    df.plan = reinterpret_cast<DecPlan*>((uintptr_t)(p.plan_stride * (size_t)f));
+    df.nblk_total = host_block_count(in.nbEle, T, L);
+    df.blkpos = reinterpret_cast<uint32_t*>((uintptr_t)p.blocks);
+    df.err = reinterpret_cast<uint32_t*>((uintptr_t)f);
+    df.y = static_cast<float*>(in.output);
+    uint64_t per_seg = 0, nt = 0;
+    host_tile_counts(in.nbEle, T, L, tb, per_seg, nt);
+    df.ntiles = (uint32_t)nt;
+    df.tiles_per_seg = (uint32_t)per_seg;
+    df.tile_base = (uint32_t)p.tiles;
+    const uint64_t nloc = in.input_bytes / SC + (uint64_t)T + 1;
+    df.loc_base = (uint32_t)p.locs;
+    df.loc_ctas = (uint32_t)nloc;
+    p.tile_field.insert(p.tile_field.end(), nt, (uint32_t)f);
+    p.loc_field.insert(p.loc_field.end(), nloc, (uint32_t)f);
+    p.tiles += nt;
+    p.locs += nloc;
+    p.blocks += df.nblk_total;
+    if (p.tiles >= (1ull << 31) || p.locs >= (1ull << 31)) return host_fail(SZP_GB300_EINVAL, "batch too large");
+  }
+  return SZP_GB300_OK;
+}
+
+void place_decompress(DecompressPlan& p, uint8_t* d_plans, uint32_t* d_blkpos, uint32_t* d_err) {
+  const int T = p.fields.empty() ? 1 : (int)p.fields[0].seg.T;
+  for (auto& df : p.fields) {
+    uint8_t* pb = d_plans + reinterpret_cast<uintptr_t>(df.plan);
+    df.plan = reinterpret_cast<DecPlan*>(pb);
+    df.reg0 = reinterpret_cast<uint64_t*>(pb + sizeof(DecPlan));
+    df.reg1 = df.reg0 + T;
+    df.chunk_base = reinterpret_cast<uint32_t*>(df.reg1 + T);
+    df.blkpos = d_blkpos + reinterpret_cast<uintptr_t>(df.blkpos);
+    df.err = d_err + reinterpret_cast<uintptr_t>(df.err);
+  }
+}
+
+void args_compress(CompressArgs& a, RelBatchArgs& r, const CompressPlan& p, CompressField* d_fields,
+                   const uint32_t* d_tile_field, const uint32_t* d_items, RelFieldState* d_state, uint64_t* status,
+                   LaunchState* ls, uint32_t* err, uint32_t tb) {
+  memset(&a, 0, sizeof a);
+  a.seg.L = kBatchL;
+  a.status = status;
+  a.ls = ls;
+  a.err = err;
+  a.ntiles = (uint32_t)p.tiles;
+  a.tb = tb;
+  a.thr = host_bitcount_table();
+  a.fields = d_fields;
+  a.tile_field = d_tile_field;
+  memset(&r, 0, sizeof r);
+  r.fields = d_fields;
+  r.state = d_state;
+  r.item_field = d_items;
+  r.nitems = (uint32_t)p.item_field.size();
+  r.chunk = kRelChunk;
+}
+
+void args_decompress(DecArgs& a, const DecompressPlan& p, const DecField* d_fields, const uint32_t* d_tile_field,
+                     const uint32_t* d_loc_field, uint2* aux, uint32_t* counters, uint64_t* status, LaunchState* ls,
+                     uint32_t* err, uint32_t tb) {
+  const uint32_t maxsz = max_block_bytes(kBatchL);
+  memset(&a, 0, sizeof a);
+  a.fm2 = false;
+  a.chunk = locate_chunk_bytes(maxsz);
+  a.super_chunk = locate_super_bytes(maxsz);
+  a.overlap = locate_overlap_bytes(maxsz);
+  a.maxsz = maxsz;
+  a.aux = aux;
+  a.counters = counters;
+  a.status = status;
+  a.ls = ls;
+  a.err = err;
+  a.ntiles = (uint32_t)p.tiles;
+  a.tb = tb;
+  a.bpw = tb / 8;
+  a.nlocate_ctas = (uint32_t)p.locs;
+  a.fields = d_fields;
+  a.tile_field = d_tile_field;
+  a.loc_field = d_loc_field;
+}
+
+int issue_compress(const CompressArgs& a, const RelBatchArgs& r, uint32_t rel_grid, int rounds, cudaStream_t st) {
+  if (r.nitems) BCU(launch_rel_batch(r, rel_grid, st));
+  if (a.ntiles) BCU(launch_compress_batch(a, kBatchL, rounds, st));
+  return SZP_GB300_OK;
+}
+
+int issue_decompress(const DecArgs& a, uint32_t nfields, int rounds, cudaStream_t st) {
+  BCU(launch_dec_setup_batch(a, nfields, st));
+  BCU(launch_locate_batch(a, st));
+  if (a.ntiles) BCU(launch_decode_batch(a, kBatchL, rounds, st));
+  return SZP_GB300_OK;
+}
+
+}  // namespace szp
 
 extern "C" {
 
