@@ -14,6 +14,7 @@
 //   sign bitmap / fixed-length packing   szp_TypeManager.cc:13-94,820-844
 //   fastmode2 per-block seed                                   :812-864
 #include <atomic>
+#include <type_traits>
 
 #include "szp_device.cuh"
 #include "szp_kernels.h"
@@ -370,20 +371,29 @@ __device__ __forceinline__ void warp_store_span(uint8_t* __restrict__ dst, const
     return;
   }
   const uint32_t q = sh >> 2, bs = 8 * (sh & 3);
-  for (uint32_t c = c0 + lane; c < c1; c += 32) {
-    const uint4* line = reinterpret_cast<const uint4*>(src + 16 * (c - 1));
-    const uint4 u = line[0], v = line[1];
-    const uint32_t w[8] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
-    uint4 o;
+  // two chunks per lane per pass: their shared-memory loads are in flight together
+  for (uint32_t cb = c0; cb < c1; cb += 64) {
+    uint4 o[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const uint32_t c = min(cb + lane + 32 * k, c1 - 1);  // clamped: always a readable chunk
+      const uint4* line = reinterpret_cast<const uint4*>(src + 16 * (c - 1));
+      const uint4 u = line[0], v = line[1];
+      const uint32_t w[8] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
 #define SZP_FS(i) __funnelshift_r(w[(i)], w[(i) + 1], bs)
-    switch (q) {
-      case 0: o = make_uint4(SZP_FS(0), SZP_FS(1), SZP_FS(2), SZP_FS(3)); break;
-      case 1: o = make_uint4(SZP_FS(1), SZP_FS(2), SZP_FS(3), SZP_FS(4)); break;
-      case 2: o = make_uint4(SZP_FS(2), SZP_FS(3), SZP_FS(4), SZP_FS(5)); break;
-      default: o = make_uint4(SZP_FS(3), SZP_FS(4), SZP_FS(5), SZP_FS(6)); break;
-    }
+      switch (q) {
+        case 0: o[k] = make_uint4(SZP_FS(0), SZP_FS(1), SZP_FS(2), SZP_FS(3)); break;
+        case 1: o[k] = make_uint4(SZP_FS(1), SZP_FS(2), SZP_FS(3), SZP_FS(4)); break;
+        case 2: o[k] = make_uint4(SZP_FS(2), SZP_FS(3), SZP_FS(4), SZP_FS(5)); break;
+        default: o[k] = make_uint4(SZP_FS(3), SZP_FS(4), SZP_FS(5), SZP_FS(6)); break;
+      }
 #undef SZP_FS
-    *reinterpret_cast<uint4*>(g0 + 16 * c) = o;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const uint32_t c = cb + lane + 32 * k;
+      if (c < c1) *reinterpret_cast<uint4*>(g0 + 16 * c) = o[k];
+    }
   }
 }
 
@@ -592,6 +602,12 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     const uint32_t sh = 1 + g.d;  // slot index of tile element 0
     const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
     const bool full = g.nblk == TB && g.nel == TB * L;  // every lane of every round holds 8 elements
+    // All rounds run on the fast quantization (exact while |x/eb| < 2^24); if
+    // any lane met a larger value the whole tile is redone on the exact path,
+    // so the common case has no per-round branch.
+    auto analyse = [&](auto exact_tag) -> bool {
+      constexpr bool EXACT = decltype(exact_tag)::value;
+      bool slow = false;
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
       const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
@@ -619,9 +635,27 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
         for (int j = 0; j < 8; j++) xv[j] = (uint32_t)j < ml ? sx[i + j] : 0.0f;
       }
       int32_t q[8];
-      quantize8(xv, inv, q, flags);
+      if (EXACT) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) q[j] = quantize_lean(xv[j], inv, flags);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const float pj = __fmul_rz(xv[j], inv);
+          q[j] = __float2int_rz(pj);
+          slow |= !(fabsf(pj) < 16777216.0f);
+        }
+      }
       int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
-      if (lane == 0) prev = quantize_lean(sx[i - 1], inv, flags);  // the element before the warp's round
+      if (lane == 0) {  // the element before the warp's round
+        if (EXACT) {
+          prev = quantize_lean(sx[i - 1], inv, flags);
+        } else {
+          const float pp = __fmul_rz(sx[i - 1], inv);
+          prev = __float2int_rz(pp);
+          slow |= !(fabsf(pp) < 16777216.0f);
+        }
+      }
       uint32_t sb = 0, lmax = 0;
       if (full) {
 #pragma unroll
@@ -659,6 +693,9 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
         s_off[bt] = block_bytes(m, bc);
       }
     }
+      return slow;
+    };
+    if (__any_sync(0xffffffffu, analyse(std::false_type{}))) analyse(std::true_type{});
     if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(s_meta[s].err, kErrQuantRange);
     compute_sync();  // block sizes complete; the input window is dead from here on
 

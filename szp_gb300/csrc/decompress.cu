@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
   __shared__ uint32_t s_h[NT], s_x[NT], s_k[NT];
   __shared__ uint2 s_aux[NT];
   __shared__ uint64_t s_val[NT];
-  __shared__ uint32_t s_misc[8];
+  __shared__ uint32_t s_misc[2 * (NT / 32)];
   __shared__ __align__(8) uint64_t s_bar;
   uint32_t tile, epoch;
   draw_ticket(a.ls, a.nlocate_ctas, tile, epoch, s_tk);
@@ -334,35 +334,31 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
       x = kPosDead;
     }
     while (__any_sync(0xffffffffu, !done)) {
-      if (!done) {
-        if (pos >= cE) {
-          h = entry >= rlen ? kPosEnd : entry;
-          x = pos >= rlen ? kPosEnd : pos;
-          k = cnt;
-          done = true;
-        } else if (budget == 0) {
-          done = true;
-        } else {
-          budget--;
-          const uint32_t sz = ch.step(pos);
-          if (sz) {
-            cnt += pos >= cS ? 1u : 0u;
-            pos += sz;
-            if (entry == kPosDead && pos >= cS) entry = pos;
-          } else if (!known && anchor + 1 < cE) {
-            anchor++;
-            pos = anchor;
-            entry = anchor >= cS ? anchor : kPosDead;
-            cnt = 0;
-          } else {
-            if (known) {
-              h = 0;
-              k = cnt;  // x stays kPosDead: the true chain is broken
-            }
-            done = true;
-          }
-        }
+      // one header step for every lane still inside its chunk; the outcome is
+      // applied with selects, so the warp takes one path per iteration
+      const bool walking = !done && pos < cE && budget != 0;
+      const uint32_t sz = walking ? ch.step(pos) : 0u;
+      budget -= walking ? 1u : 0u;
+      const bool adv = walking && sz != 0, dead = walking && sz == 0;
+      const bool restart = dead && !known && anchor + 1 < cE;
+      cnt = restart ? 0u : cnt + ((adv && pos >= cS) ? 1u : 0u);
+      const uint32_t np = pos + sz;
+      entry = (adv && entry == kPosDead && np >= cS) ? np : entry;
+      anchor += restart ? 1u : 0u;
+      entry = restart ? (anchor >= cS ? anchor : kPosDead) : entry;
+      pos = restart ? anchor : (adv ? np : pos);
+      const bool reached = !done && pos >= cE;
+      const bool gaveup = !done && !reached && (budget == 0 || (dead && !restart));
+      if (reached) {
+        h = entry >= rlen ? kPosEnd : entry;
+        x = pos >= rlen ? kPosEnd : pos;
+        k = cnt;
       }
+      if (gaveup && dead && known) {
+        h = 0;
+        k = cnt;  // x stays kPosDead: the true chain is broken
+      }
+      done = done || reached || gaveup;
     }
   }
   s_h[tid] = h;
@@ -417,10 +413,10 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
         uint2 ax = make_uint2(0, 0);
         bool ready = true, incl = false;
         if (inr) {
-          s1 = ld_volatile_u64(a.status + idx);
-          __threadfence();
-          ax = ld_volatile_u2(a.aux + idx);
-          __threadfence();
+          // seqlock read: acquire loads keep the aux read between the two status reads
+          s1 = ld_acquire_u64(a.status + idx);
+          const uint64_t axw = ld_acquire_u64(reinterpret_cast<const uint64_t*>(a.aux + idx));
+          ax = make_uint2((uint32_t)axw, (uint32_t)(axw >> 32));
           s2 = ld_volatile_u64(a.status + idx);
           const uint64_t f = status_flag(s1);
           ready = s1 == s2 && status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
@@ -471,10 +467,10 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
         // sum the counts of the relevant window entries
         uint64_t v = relevant ? s_val[tid] : 0;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) s_misc[4 + warp] = (uint32_t)v;  // per-warp partials (< 2^32)
+        if (lane == 0) s_misc[NT / 32 + warp] = (uint32_t)v;  // per-warp partials (< 2^32)
         __syncthreads();
         uint64_t tot = 0;
-        for (int w = 0; w < NT / 32; w++) tot += s_misc[4 + w];
+        for (int w = 0; w < NT / 32; w++) tot += s_misc[NT / 32 + w];
         const uint32_t far_h = s_aux[NT - 1].x;
         __syncthreads();
         acc += tot;
@@ -671,10 +667,11 @@ constexpr int kDecRounds = 4;
 //   compute   unpacks the deltas (LPB lanes per block, 8 elements per lane:
 //             the byte layout of 8 elements is self-contained), scans them
 //             inside the tile and stages the tile-relative prefix sums (int32)
-//             in the slot, over the span they came from
-//   control   looks back for the tile's base (the segment's seed plus the
-//             deltas of the tiles before it, szpd_float.cc:76-118), adds it,
-//             dequantizes and stores the tile with 16-byte stores
+//             in the slot, over the span they came from; then finishes the
+//             previous tile: adds its base, dequantizes, 16-byte stores
+//   control   looks back for each tile's base (the segment's seed plus the
+//             deltas of the tiles before it, szpd_float.cc:76-118) while the
+//             compute warps unpack the next tile
 // ---------------------------------------------------------------------------
 constexpr int kDecSlots = 3, kDecControl = 2;
 constexpr int kDecPipeThreads = (8 + kDecControl + 1) * 32;
@@ -777,47 +774,73 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
   }
 }
 
-// One warp: y[e] = dequant(base + stage[e - e0]) for the tile's nel elements
-// starting at dst = y + e0; 16-byte stores for the aligned middle, the words
-// picked from two aligned shared-memory lines when dst is not 16-byte aligned.
-// stage is 16-byte aligned and readable for nel + 4 words.
-__device__ __forceinline__ void warp_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
-                                                   uint32_t nel, uint32_t base, float eb, bool ebsp, int lane) {
+// Little-endian bytes [o, o+8) of shared array b as (lo, hi), from three
+// aligned 32-bit loads and two funnel shifts (reads b[o&~3 .. (o&~3)+12)).
+__device__ __forceinline__ void lds_le64(const uint8_t* b, uint32_t o, uint32_t& lo, uint32_t& hi) {
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(b + (o & ~3u));
+  const uint32_t sh = (o & 3u) * 8u;
+  const uint32_t w0 = w[0], w1 = w[1], w2 = w[2];
+  lo = __funnelshift_r(w0, w1, sh);
+  hi = __funnelshift_r(w1, w2, sh);
+}
+
+// The 256 compute threads: y[e] = dequant(base + stage[e - e0]) for the
+// tile's nel elements starting at dst = y + e0; 16-byte stores for the aligned
+// middle, the words picked from two aligned shared-memory lines when dst is not
+// 16-byte aligned.  stage is 16-byte aligned and readable for nel + 4 words.
+__device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
+                                                  uint32_t nel, uint32_t base, float eb, bool ebsp) {
+  const uint32_t tid = threadIdx.x;
   if (nel == 0) return;
   const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 2) & 3);
   float* g0 = dst - ph;  // 16-byte aligned
   const uint32_t end = ph + nel;
   const uint32_t c0 = (ph + 3) >> 2, c1 = end >> 2;  // whole float4 chunks [c0, c1)
   if (c0 >= c1) {
-    for (uint32_t i = ph + lane; i < end; i += 32) g0[i] = dequant(base + stage[i - ph], eb, ebsp);
+    if (tid < nel) g0[ph + tid] = dequant(base + stage[tid], eb, ebsp);
     return;
   }
-  if ((uint32_t)lane < 4 * c0 - ph) g0[ph + lane] = dequant(base + stage[lane], eb, ebsp);
-  if ((uint32_t)lane < end - 4 * c1) g0[4 * c1 + lane] = dequant(base + stage[4 * c1 + lane - ph], eb, ebsp);
+  if (tid < 4 * c0 - ph) g0[ph + tid] = dequant(base + stage[tid], eb, ebsp);
+  if (tid >= 32 && tid - 32 < end - 4 * c1)
+    g0[4 * c1 + tid - 32] = dequant(base + stage[4 * c1 + tid - 32 - ph], eb, ebsp);
   const uint4* s4 = reinterpret_cast<const uint4*>(stage);
-  for (uint32_t c = c0 + lane; c < c1; c += 32) {
-    uint4 w;
-    if (ph == 0) {
-      w = s4[c];
-    } else {
-      const uint4 u = s4[c - 1], v = s4[c];  // stage words [4c-4, 4c+4); chunk c wants [4c-ph, 4c-ph+4)
-      if (ph == 1) w = make_uint4(u.w, v.x, v.y, v.z);
-      else if (ph == 2) w = make_uint4(u.z, u.w, v.x, v.y);
-      else w = make_uint4(u.y, u.z, u.w, v.x);
+  // four chunks per thread per pass: their shared-memory loads are in flight together
+  constexpr int U = 4;
+  for (uint32_t cb = c0; cb < c1; cb += 256 * U) {
+    uint4 w[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint32_t c = min(cb + tid + 256 * u, c1 - 1);  // clamped: always a readable chunk
+      if (ph == 0) {
+        w[u] = s4[c];
+      } else {
+        const uint4 a = s4[c - 1], b = s4[c];  // stage words [4c-4, 4c+4); chunk c wants [4c-ph, 4c-ph+4)
+        if (ph == 1) w[u] = make_uint4(a.w, b.x, b.y, b.z);
+        else if (ph == 2) w[u] = make_uint4(a.z, a.w, b.x, b.y);
+        else w[u] = make_uint4(a.y, a.z, a.w, b.x);
+      }
     }
-    float4 o;
-    o.x = dequant(base + w.x, eb, ebsp);
-    o.y = dequant(base + w.y, eb, ebsp);
-    o.z = dequant(base + w.z, eb, ebsp);
-    o.w = dequant(base + w.w, eb, ebsp);
-    reinterpret_cast<float4*>(g0)[c] = o;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint32_t c = cb + tid + 256 * u;
+      if (c < c1) {
+        float4 o;
+        o.x = dequant(base + w[u].x, eb, ebsp);
+        o.y = dequant(base + w[u].y, eb, ebsp);
+        o.z = dequant(base + w[u].z, eb, ebsp);
+        o.w = dequant(base + w[u].w, eb, ebsp);
+        reinterpret_cast<float4*>(g0)[c] = o;
+      }
+    }
   }
 }
 
-template <int NS, int NC, uint32_t TB>
-__device__ __forceinline__ void dec_control(int c, const DecArgs& a, const uint8_t* slots, uint32_t slot_bytes,
-                                            const DecSlot* meta, const uint32_t* s_agg, uint64_t* full,
-                                            uint64_t* aggb, uint64_t* staged, uint64_t* empty,
+// Control warp c: tiles c, c + kDecControl, ... of this CTA.  Finds each
+// tile's base q (the segment's seed plus the deltas of the tiles before it) and
+// hands it to the compute warps, which finish the tile.
+template <int NS, int NC>
+__device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSlot* meta, const uint32_t* s_agg,
+                                            uint32_t* s_base, uint64_t* full, uint64_t* aggb, uint64_t* based,
                                             const uint32_t* s_epoch, const volatile uint32_t* s_stop_k) {
   const int lane = threadIdx.x & 31;
   for (uint32_t k = (uint32_t)c;; k += NC) {
@@ -826,29 +849,26 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const uint8
     if (!control_wait_full(&full[s], par, k, s_stop_k, a.err)) return;
     const uint32_t tile = meta[s].tile;
     if (tile >= a.ntiles) return;
-    const uint32_t nel = meta[s].nel;
     const bool first = meta[s].first;
-    const uint64_t e0 = meta[s].e0;
-    const uint32_t seed = meta[s].seed;
-    const float eb = meta[s].eb;
-    const bool ebsp = !isfinite(eb);
-    float* y = meta[s].y;
     mbar_wait_or_flag(&aggb[s], par, a.err);
     const uint32_t agg = s_agg[s];
     const uint32_t epoch = *s_epoch;
     uint32_t base;
     if (first) {
-      base = seed;
-      if (lane == 0) y[e0 - 1] = dequant(seed, eb, ebsp);
+      base = meta[s].seed;
+      if (lane == 0) {
+        const float eb = meta[s].eb;
+        meta[s].y[meta[s].e0 - 1] = dequant(base, eb, !isfinite(eb));
+      }
     } else {
       base = (uint32_t)lookback_sum(a.status, tile, meta[s].seg_tile0, epoch, a.err);
       if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(base + agg)));
     }
-    mbar_wait_or_flag(&staged[s], par, a.err);
-    const uint32_t* stage = reinterpret_cast<const uint32_t*>(slots + (size_t)s * slot_bytes + dec_pos_bytes(TB));
-    warp_dequant_store(y + e0, stage, nel, base, eb, ebsp, lane);
+    if (lane == 0) {
+      s_base[s] = base;
+      mbar_arrive(&based[s]);
+    }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
@@ -866,7 +886,8 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint32_t s_epoch;
   __shared__ volatile uint32_t s_stop_k;
-  __shared__ __align__(8) uint64_t s_full[NS], s_aggb[NS], s_staged[NS], s_empty[NS];
+  __shared__ uint32_t s_base[NS];
+  __shared__ __align__(8) uint64_t s_full[NS], s_aggb[NS], s_based[NS], s_empty[NS];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x < NS) s_meta[threadIdx.x].tile = kStopTile;
@@ -874,7 +895,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
     for (int s = 0; s < NS; s++) {
       mbar_init(&s_full[s], 1);
       mbar_init(&s_aggb[s], 1);
-      mbar_init(&s_staged[s], 1);
+      mbar_init(&s_based[s], 1);
       mbar_init(&s_empty[s], 1);
     }
     s_stop_k = kStopTile;
@@ -886,20 +907,33 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
     return;
   }
   if (warp >= WARPS) {
-    dec_control<NS, NC, TB>(warp - WARPS, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_staged, s_empty,
-                            &s_epoch, &s_stop_k);
+    dec_control<NS, NC>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
     return;
   }
 
   // ---- compute warps ----
+  // Tile k is unpacked and staged, then tile k-1 (whose base the control warps
+  // have looked up meanwhile) is finished: base added, dequantized, stored.
   const int sub = lane % LPB, grp = lane / LPB;
   const uint32_t wfirst = (uint32_t)warp * ROUNDS * BPR;
+  auto finish = [&](uint32_t kp) {
+    const int sp_ = (int)(kp % NS);
+    mbar_wait_or_flag(&s_based[sp_], (kp / NS) & 1, a.err);
+    const float ebp = s_meta[sp_].eb;
+    const uint32_t* stage = reinterpret_cast<const uint32_t*>(s_slots + (size_t)sp_ * slot_bytes + PB);
+    cta_dequant_store(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp));
+    compute_sync();  // every read of the slot is done
+    if (threadIdx.x == 0) mbar_arrive(&s_empty[sp_]);
+  };
   for (uint32_t k = 0;; k++) {
     const int s = (int)(k % NS);
     const uint32_t par = (k / NS) & 1;
     mbar_wait_or_flag(&s_full[s], par, a.err);
     const uint32_t tile = s_meta[s].tile;
-    if (tile >= a.ntiles) return;
+    if (tile >= a.ntiles) {
+      if (k) finish(k - 1);
+      return;
+    }
     const uint32_t nblk = s_meta[s].nblk, nel = s_meta[s].nel, span0 = s_meta[s].span0;
     const uint32_t spanlen = s_meta[s].spanlen;
     uint8_t* slot = s_slots + (size_t)s * slot_bytes;
@@ -919,13 +953,40 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
       uint32_t d[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) d[j] = 0;
+      uint32_t off = 0, bc = 0;
       if (m) {
-        const uint32_t off = bpos[bt] - span0;
-        uint32_t bc = off < spanlen ? sp[off] : 255u;
+        off = bpos[bt] - span0;
+        bc = off < spanlen ? sp[off] : 255u;
         if (bc > 33 || off + block_bytes(m, bc) > spanlen) {
           corrupt = true;
           bc = 0;
         }
+      }
+      if (__all_sync(0xffffffffu, (m == L || m == 0) && bc <= 15)) {
+        // every block of the round is full and has at most one byte plane:
+        // the lane's plane and remainder bytes come from aligned word loads
+        if (bc) {
+          constexpr uint32_t NSB = L / 8;
+          const uint32_t B = bc >> 3, rr = bc & 7;
+          const uint32_t ob = (uint32_t)(sp - s_slots) + off;  // the block in s_slots
+          const uint32_t sb = s_slots[ob + 1 + sub];             // sign bits, szp_TypeManager.cc:820-844
+          uint32_t lo, hi, plo = 0, phi = 0;
+          lds_le64(s_slots, ob + 1 + NSB + B * L + rr * sub, lo, hi);  // remainder, szp_TypeManager.cc:122-434
+          if (B) lds_le64(s_slots, ob + 1 + NSB + 8 * sub, plo, phi);  // byte plane, szp_TypeManager.cc:36-52
+          const uint32_t t = __byte_perm(lo, 0, 0x0123);  // remainder bits 0..31, MSB first
+          const uint32_t t2 = __funnelshift_l(__byte_perm(hi, 0, 0x0123), t, 4 * rr);  // bits 4rr..
+          const uint32_t rs = 32 - rr, pw = 1u << rr;
+          const int32_t sx = (int32_t)(sb << 24);
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const uint32_t f = __funnelshift_rc((j < 4 ? t : t2) << (rr * (j & 3)), 0u, rs);
+            const uint32_t h = __byte_perm(j < 4 ? plo : phi, 0, 0x4440 + (j & 3));
+            const uint32_t v = h * pw + f;
+            const uint32_t sg = (uint32_t)((sx << j) >> 31);
+            d[j] = (v ^ sg) - sg;
+          }
+        }
+      } else if (m) {
         if (bc && ml) {
           const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
           const uint32_t sb = sp[off + 1 + sub];  // sign bits, szp_TypeManager.cc:820-844
@@ -969,10 +1030,27 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
         run += d[j];
         pre[r][j] = run;
       }
-      const uint32_t incl = warp_incl_scan(run, lane);
-      lex[r] = incl - run;
-      rbase[r] = wtot;
-      wtot += __shfl_sync(0xffffffffu, incl, 31);
+      lex[r] = run;
+    }
+    // the rounds' warp scans, interleaved: four independent shuffle chains
+    {
+      uint32_t incl[ROUNDS];
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) incl[r] = lex[r];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int r = 0; r < ROUNDS; r++) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl[r], o);
+          if (lane >= o) incl[r] += y;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) {
+        lex[r] = incl[r] - lex[r];
+        rbase[r] = wtot;
+        wtot += __shfl_sync(0xffffffffu, incl[r], 31);
+      }
     }
     if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(s_meta[s].err, kErrCorrupt);
 
@@ -1013,7 +1091,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
       }
     }
     compute_sync();  // staged; s_w is free for the next tile
-    if (threadIdx.x == 0) mbar_arrive(&s_staged[s]);
+    if (k) finish(k - 1);
   }
 }
 
