@@ -450,6 +450,11 @@ int szp_gb300_batch_create(szp_gb300_batch* out, int direction, const szp_gb300_
     return rc;
   };
   if (cudaGetDevice(&b->device) != cudaSuccess) return fail_out(host_fail(SZP_GB300_ECUDA, "no CUDA device"));
+  {
+    // kernel attributes are set before any capture
+    cudaError_t pe = direction == SZP_GB300_BATCH_COMPRESS ? prepare_compress_batch() : prepare_decompress_batch();
+    if (pe != cudaSuccess) return fail_out(host_fail(SZP_GB300_ECUDA, cudaGetErrorString(pe)));
+  }
   // look-back words: the most tiles / locate tickets any tile size needs
   const uint32_t maxsz = max_block_bytes((uint32_t)blockSize);
   const uint32_t SC = locate_super_bytes(maxsz);

@@ -1180,6 +1180,7 @@ static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
   }
   const uint32_t s_grid = (uint32_t)c;
   const uint32_t grid = a.ntiles < s_grid ? a.ntiles : s_grid;
+  if (grid == 0) return cudaSuccess;
   k<<<grid, kPipeThreads, smem, st>>>(a, slot);
   return cudaGetLastError();
 }
@@ -1299,6 +1300,21 @@ cudaError_t launch_rel_batch(const RelBatchArgs& a, uint32_t grid, cudaStream_t 
   if (a.nitems == 0) return cudaSuccess;
   rel_batch_kernel<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
+}
+
+// Sets the batched compress kernels' shared-memory limits and caches their
+// grids (a no-op launch of zero tiles), so no later launch does that work.
+cudaError_t prepare_compress_batch() {
+  CompressArgs a;
+  memset(&a, 0, sizeof a);
+  a.seg.L = 32;
+  cudaError_t e = cudaSuccess;
+  for (int r : {1, 2, 4}) {
+    a.tb = 8u * (uint32_t)r * 8u;
+    e = r == 1 ? launch_lanes<4, true, 1>(a, 0) : r == 2 ? launch_lanes<4, true, 2>(a, 0) : launch_lanes<4, true, 4>(a, 0);
+    if (e != cudaSuccess) return e;
+  }
+  return e;
 }
 
 // Batched fastmode1 compression, blockSize 32, tiles of 8*rounds*8 blocks.

@@ -1324,6 +1324,24 @@ cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Sets the batched decompression kernels' shared-memory limits and caches
+// their grids without launching anything.
+cudaError_t prepare_decompress_batch() {
+  DecArgs a;
+  memset(&a, 0, sizeof a);
+  a.maxsz = max_block_bytes(32);
+  a.super_chunk = locate_super_bytes(a.maxsz);
+  a.overlap = locate_overlap_bytes(a.maxsz);
+  const size_t smem = locate_smem_bytes(a.super_chunk, a.overlap, a.maxsz);
+  cudaError_t e = cudaFuncSetAttribute(locate_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  for (int r : {1, 2, 4}) {
+    if (e != cudaSuccess) return e;
+    a.tb = 8u * (uint32_t)r * 8u;
+    e = r == 1 ? launch_dec_lanes<4, true, 1>(a, 0) : r == 2 ? launch_dec_lanes<4, true, 2>(a, 0) : launch_dec_lanes<4, true, 4>(a, 0);
+  }
+  return e;
+}
+
 // Batched fastmode1 decode, blockSize 32, tiles of 8*rounds*8 blocks.
 cudaError_t launch_decode_batch(const DecArgs& a, uint32_t L, int rounds, cudaStream_t st) {
   if (L != 32) return cudaErrorInvalidValue;

@@ -105,19 +105,21 @@ struct Req {
   bool finished = false;
 };
 
-// A device buffer that grows on demand (only ever in the worker thread).
+// A buffer that grows on demand (only ever in the worker thread).  Device
+// buffers grow in stream order on their lane (no device-wide synchronisation);
+// they start large enough for typical groups.
 struct Grow {
   void* p = nullptr;
   size_t cap = 0;
-  cudaError_t ensure(size_t n, bool pinned = false) {
+  cudaError_t ensure(size_t n, bool pinned = false, cudaStream_t st = nullptr) {
     if (n <= cap) return cudaSuccess;
-    size_t want = std::max(n + n / 4, (size_t)4096);
+    size_t want = std::max(n + n / 2, (size_t)4096);
     if (p) {
-      if (pinned) cudaFreeHost(p); else cudaFree(p);
+      if (pinned) cudaFreeHost(p); else cudaFreeAsync(p, st);
     }
     p = nullptr;
     cap = 0;
-    cudaError_t e = pinned ? cudaMallocHost(&p, want) : cudaMalloc(&p, want);
+    cudaError_t e = pinned ? cudaMallocHost(&p, want) : cudaMallocAsync(&p, want, st);
     if (e == cudaSuccess) cap = want;
     return e;
   }
@@ -234,14 +236,14 @@ int launch_group(szp_gb300_server_s& s, Lane& ln) {
   if (rc) return rc;
   const size_t nc = cf.size(), nd = df.size();
   // per-lane device buffers for this group
-  SCU(ln.sizes.ensure(8 * (nc + 1)));
-  SCU(ln.errs.ensure(4 * (nc + nd + 2)));
-  SCU(ln.plans.ensure(dp.plan_stride * (nd + 1)));
-  SCU(ln.blkpos.ensure(4 * (dp.blocks + 1)));
-  SCU(ln.aux.ensure(sizeof(uint2) * (dp.locs + 1)));
+  SCU(ln.sizes.ensure(8 * (nc + 1), false, ln.st));
+  SCU(ln.errs.ensure(4 * (nc + nd + 2), false, ln.st));
+  SCU(ln.plans.ensure(dp.plan_stride * (nd + 1), false, ln.st));
+  SCU(ln.blkpos.ensure(4 * (dp.blocks + 1), false, ln.st));
+  SCU(ln.aux.ensure(sizeof(uint2) * (dp.locs + 1), false, ln.st));
   const size_t words = std::max<uint64_t>(std::max(cp.tiles, dp.tiles), std::max<uint64_t>(dp.locs, 1));
   if (words * 8 > ln.status.cap) {
-    SCU(ln.status.ensure(words * 8));
+    SCU(ln.status.ensure(words * 8, false, ln.st));
     SCU(cudaMemsetAsync(ln.status.p, 0, ln.status.cap, ln.st));  // fresh words must not look ready
   }
   unsigned long long* d_sizes = static_cast<unsigned long long*>(ln.sizes.p);
@@ -253,7 +255,7 @@ int launch_group(szp_gb300_server_s& s, Lane& ln) {
   const size_t o_cf = pk.add(cp.fields), o_ctf = pk.add(cp.tile_field), o_it = pk.add(cp.item_field);
   const size_t o_rs = pk.add(cp.rel), o_df = pk.add(dp.fields), o_dtf = pk.add(dp.tile_field);
   const size_t o_lf = pk.add(dp.loc_field);
-  SCU(ln.tables.ensure(pk.buf.size()));
+  SCU(ln.tables.ensure(pk.buf.size(), false, ln.st));
   SCU(ln.htables.ensure(pk.buf.size(), true));
   memcpy(ln.htables.p, pk.buf.data(), pk.buf.size());  // the lane's previous group has finished with it
   uint8_t* tb_d = static_cast<uint8_t*>(ln.tables.p);
@@ -415,8 +417,24 @@ int szp_gb300_server_create(szp_gb300_server* out, const szp_gb300_server_config
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ln.ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ln.misc, sizeof(LaneScalars));
     if (e == cudaSuccess) e = cudaMemset(ln.misc, 0, sizeof(LaneScalars));
+    // room for groups of typical size, so steady state allocates nothing
+    const size_t mb = (size_t)cfg->max_batch + 1;
+    if (e == cudaSuccess) e = ln.status.ensure(8u << 16, false, ln.st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ln.status.p, 0, ln.status.cap, ln.st);
+    if (e == cudaSuccess) e = ln.tables.ensure(1u << 20, false, ln.st);
+    if (e == cudaSuccess) e = ln.htables.ensure(1u << 20, true);
+    if (e == cudaSuccess) e = ln.hresults.ensure(12 * mb + 64, true);
+    if (e == cudaSuccess) e = ln.sizes.ensure(8 * mb, false, ln.st);
+    if (e == cudaSuccess) e = ln.errs.ensure(8 * mb, false, ln.st);
+    if (e == cudaSuccess) e = ln.plans.ensure(512 * mb, false, ln.st);
+    if (e == cudaSuccess) e = ln.blkpos.ensure(16u << 20, false, ln.st);
+    if (e == cudaSuccess) e = ln.aux.ensure(1u << 20, false, ln.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ln.st);
     if (e != cudaSuccess) return bad(e);
   }
+  e = prepare_compress_batch();
+  if (e == cudaSuccess) e = prepare_decompress_batch();
+  if (e != cudaSuccess) return bad(e);
   s->worker = std::thread(worker_main, s);
   *out = s;
   return SZP_GB300_OK;

@@ -132,6 +132,7 @@ size_t compress_smem_bytes(uint32_t L, uint32_t tb);
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st);
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds, cudaStream_t st);
+cudaError_t prepare_compress_batch();
 cudaError_t launch_rel_batch(const RelBatchArgs& a, uint32_t grid, cudaStream_t st);
 uint32_t rel_encode_host(float v);
 cudaError_t launch_bitcount_probe(const uint32_t* in, uint8_t* out, uint64_t n, const BitcountTable& thr,
@@ -151,6 +152,7 @@ cudaError_t launch_decode(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStream_t st);
 cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode_batch(const DecArgs& a, uint32_t L, int rounds, cudaStream_t st);
+cudaError_t prepare_decompress_batch();
 
 // host helpers (api.cu)
 const BitcountTable& host_bitcount_table();
