@@ -403,7 +403,7 @@ __device__ __forceinline__ void warp_store_span(uint8_t* __restrict__ dst, const
 template <uint32_t L, uint32_t TB, int NS, bool BATCH>
 __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* slots, uint32_t slot_bytes,
                                               SlotMeta* meta, uint64_t* full, uint64_t* empty,
-                                              uint32_t* s_epoch, volatile uint32_t* s_stop_k) {
+                                              uint32_t* s_epoch, volatile uint32_t* s_stop_k, const volatile uint32_t* s_started) {
   *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
   __threadfence();
   CompressField f1;  // the single field of a non-batched launch
@@ -425,6 +425,10 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
   for (uint32_t k = 0;; k++) {
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
+    // draw the ticket only once the compute warps have started the previous
+    // position: a tile's predecessors are then never more than a tile behind it
+    // in their work, which keeps the look-back short
+    for (uint32_t i = 0; i < kWaitLimit && *s_started < k; i++) __nanosleep(64);
     const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
     SlotMeta& m = meta[s];
     if (tile >= a.ntiles) {
@@ -552,6 +556,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
   __shared__ uint32_t s_thr[36];
   __shared__ uint32_t s_epoch;
   __shared__ volatile uint32_t s_stop_k;
+  __shared__ volatile uint32_t s_started;
   __shared__ __align__(8) uint64_t s_full[NS], s_aggb[NS], s_packed[NS], s_empty[NS];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -565,12 +570,13 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
       mbar_init(&s_empty[s], 1);
     }
     s_stop_k = kStopTile;
+    s_started = 0;
   }
   __syncthreads();
 
   if (warp == 8 + NC) {
     if (lane == 0)
-      pipe_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
+      pipe_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k, &s_started);
     return;
   }
   if (warp >= 8) {
@@ -586,6 +592,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     const uint32_t par = (k / NS) & 1;
     mbar_wait_or_flag(&s_full[s], par, a.err);
     const uint32_t tile = s_meta[s].tile;
+    if (threadIdx.x == 0) s_started = k + 1;
     if (tile >= a.ntiles) return;
     const TileGeo g = s_meta[s].g;
     const float inv = s_meta[s].inv;

@@ -700,13 +700,17 @@ __host__ __device__ constexpr uint32_t dec_pos_bytes(uint32_t tb) { return 4 * t
 template <uint32_t L, uint32_t TB, int NS, bool BATCH>
 __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, uint32_t slot_bytes, DecSlot* meta,
                                              uint64_t* full, uint64_t* empty, uint32_t* s_epoch,
-                                             volatile uint32_t* s_stop_k) {
+                                             volatile uint32_t* s_stop_k, const volatile uint32_t* s_started) {
   constexpr uint32_t PB = dec_pos_bytes(TB);
   *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
   __threadfence();
   for (uint32_t k = 0;;) {
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
+    // draw the ticket only once the compute warps have started the previous
+    // position: a tile's predecessors are then never more than a tile behind it
+    // in their work, which keeps the look-back short
+    for (uint32_t i = 0; i < kWaitLimit && *s_started < k; i++) __nanosleep(64);
     const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
     DecSlot& m = meta[s];
     if (tile >= a.ntiles) {
@@ -886,6 +890,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
   __shared__ uint32_t s_w[WARPS + 1];
   __shared__ uint32_t s_epoch;
   __shared__ volatile uint32_t s_stop_k;
+  __shared__ volatile uint32_t s_started;
   __shared__ uint32_t s_base[NS];
   __shared__ __align__(8) uint64_t s_full[NS], s_aggb[NS], s_based[NS], s_empty[NS];
 
@@ -899,11 +904,12 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
       mbar_init(&s_empty[s], 1);
     }
     s_stop_k = kStopTile;
+    s_started = 0;
   }
   __syncthreads();
   if (warp == WARPS + NC) {
     if (lane == 0)
-      dec_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k);
+      dec_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k, &s_started);
     return;
   }
   if (warp >= WARPS) {
@@ -930,6 +936,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
     const uint32_t par = (k / NS) & 1;
     mbar_wait_or_flag(&s_full[s], par, a.err);
     const uint32_t tile = s_meta[s].tile;
+    if (threadIdx.x == 0) s_started = k + 1;
     if (tile >= a.ntiles) {
       if (k) finish(k - 1);
       return;

@@ -199,6 +199,7 @@ __device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_
       if (nready[k] & rel) wait = true;
     }
     if (wait) {
+      __nanosleep(200);  // a predecessor is still working: leave the issue slots to the compute warps
       if (++spins > kSpinLimit) {
         if (lane == 0) atomicOr(err, kErrLookbackTimeout);
         return 0;
