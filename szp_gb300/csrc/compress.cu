@@ -400,7 +400,7 @@ __device__ __forceinline__ void warp_store_span(uint8_t* __restrict__ dst, const
 // Producer: one thread.  Draws tickets, and for each tile computes its
 // geometry and bulk-copies its input window [e0-1, e0+nel) into a free slot
 // (element e at slot float e - (e0-1) + d).
-template <uint32_t L, uint32_t TB, int NS, bool BATCH>
+template <uint32_t L, uint32_t TB, int NS, bool BATCH, bool FM2>
 __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* slots, uint32_t slot_bytes,
                                               SlotMeta* meta, uint64_t* full, uint64_t* empty,
                                               uint32_t* s_epoch, volatile uint32_t* s_stop_k, const volatile uint32_t* s_started) {
@@ -466,14 +466,18 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
     const uint64_t blk0 = (uint64_t)ts * TB;
     g.nblk = nb > blk0 ? (uint32_t)min((uint64_t)TB, nb - blk0) : 0u;
     g.first = ts == 0;
-    g.e0 = g.lo + 1 + blk0 * L;
+    // fastmode1: blocks start after the segment's seed, the window starts one
+    // element before block 0; fastmode2: block b starts at lo + bL with its own
+    // seed, the window starts at block 0's seed.  Either way the data element j
+    // of block b lies at window index 1 + bL + j.
+    g.e0 = FM2 ? g.lo + blk0 * L : g.lo + 1 + blk0 * L;
     g.nel = g.nblk ? (uint32_t)min((uint64_t)g.nblk * L, g.hi - g.e0) : 0u;
     g.d = 0;
     uint32_t bytes = 0;
     uintptr_t b0 = 0, a0 = 0;
-    if (g.has_seg && (g.nblk || (g.first && g.hi > g.lo))) {  // a lone seed still needs x[lo]
+    if (g.has_seg && (g.nblk || (!FM2 && g.first && g.hi > g.lo))) {  // a lone seed still needs x[lo]
       const uintptr_t xa = (uintptr_t)fd.x;
-      const uintptr_t w0 = xa + 4 * (g.e0 - 1), w1 = xa + 4 * (g.e0 + g.nel);
+      const uintptr_t w0 = xa + 4 * (FM2 ? g.e0 : g.e0 - 1), w1 = xa + 4 * (g.e0 + g.nel);
       a0 = w0 & ~(uintptr_t)15;
       g.d = (uint32_t)((w0 - a0) >> 2);
       b0 = max(a0, (xa + 15) & ~(uintptr_t)15);
@@ -540,9 +544,9 @@ __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const
   }
 }
 
-template <int LPB, bool BATCH, int ROUNDS>
-__global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __grid_constant__ CompressArgs a,
-                                                                     uint32_t slot_bytes) {
+template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false>
+__global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_constant__ CompressArgs a,
+                                                                 uint32_t slot_bytes) {
   constexpr int NS = kPipeSlots, NC = kPipeControl;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
@@ -576,7 +580,8 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
 
   if (warp == 8 + NC) {
     if (lane == 0)
-      pipe_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k, &s_started);
+      pipe_producer<L, TB, NS, BATCH, FM2>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k,
+                                           &s_started);
     return;
   }
   if (warp >= 8) {
@@ -598,7 +603,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     const float inv = s_meta[s].inv;
     uint8_t* slot = s_slots + (size_t)s * slot_bytes;
     const float* sx = reinterpret_cast<const float*>(slot);
-    const bool seed = g.has_seg && g.first && g.hi > g.lo;
+    const bool seed = !FM2 && g.has_seg && g.first && g.hi > g.lo;  // the segment's seed (fastmode1)
     int32_t seedv = 0;
     uint32_t flags = 0;
     if (seed && threadIdx.x == 0) seedv = quantize(sx[g.d], inv, flags);  // x[lo] = window element 0
@@ -606,9 +611,11 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     // ---- analysis: q, deltas, signs, block max, bit count, block size ----
     uint32_t vv[ROUNDS][8];
     uint32_t sgnb[ROUNDS];
+    int32_t bseed[ROUNDS];  // fastmode2: each block's seed, in its first lane
     const uint32_t sh = 1 + g.d;  // slot index of tile element 0
     const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
-    const bool full = g.nblk == TB && g.nel == TB * L;  // every lane of every round holds 8 elements
+    // every lane of every round holds 8 elements (never in fastmode2: a block has L-1 deltas)
+    const bool full = !FM2 && g.nblk == TB && g.nel == TB * L;
     // All rounds run on the fast quantization (exact while |x/eb| < 2^24); if
     // any lane met a larger value the whole tile is redone on the exact path,
     // so the common case has no per-round branch.
@@ -619,7 +626,14 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
     for (int r = 0; r < ROUNDS; r++) {
       const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
       const uint32_t k0 = bt * L + 8 * sub;  // tile-relative first element of the lane
-      const uint32_t ml = (bt < g.nblk && k0 < g.nel) ? min(8u, g.nel - k0) : 0u;
+      uint32_t ml;                          // elements (deltas) of the lane
+      if (FM2) {
+        const uint32_t mblk = bt < g.nblk ? min(L, g.nel - bt * L) : 0u;
+        const uint32_t md = mblk ? mblk - 1 : 0u;
+        ml = md > 8u * sub ? min(8u, md - 8u * sub) : 0u;
+      } else {
+        ml = (bt < g.nblk && k0 < g.nel) ? min(8u, g.nel - k0) : 0u;
+      }
       float xv[8];
       const uint32_t i = sh + k0;
       if (full) {
@@ -654,15 +668,17 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
         }
       }
       int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
-      if (lane == 0) {  // the element before the warp's round
+      if (FM2 ? sub == 0 : lane == 0) {  // the element before the lane's first: fastmode2 the block's seed
+        const float xp = bt < g.nblk ? sx[i - 1] : 0.0f;  // past the tile's blocks the slot holds no input
         if (EXACT) {
-          prev = quantize_lean(sx[i - 1], inv, flags);
+          prev = quantize_lean(xp, inv, flags);
         } else {
-          const float pp = __fmul_rz(sx[i - 1], inv);
+          const float pp = __fmul_rz(xp, inv);
           prev = __float2int_rz(pp);
           slow |= !(fabsf(pp) < 16777216.0f);
         }
       }
+      bseed[r] = prev;
       uint32_t sb = 0, lmax = 0;
       if (full) {
 #pragma unroll
@@ -697,7 +713,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
         }
         const uint32_t m = min(L, g.nel - bt * L);
         s_bc[bt] = (uint8_t)bc;
-        s_off[bt] = block_bytes(m, bc);
+        s_off[bt] = FM2 ? 4 + block_bytes(m - 1, bc) : block_bytes(m, bc);  // fastmode2: seed, L-1 deltas
       }
     }
       return slow;
@@ -776,10 +792,20 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_fm1_pipe(const __gri
       for (int r = 0; r < ROUNDS; r++) {
         const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
         if (bt >= g.nblk) continue;
-        const uint32_t m = min(L, g.nel - bt * L);
+        const uint32_t mblk = min(L, g.nel - bt * L);
+        const uint32_t m = FM2 ? mblk - 1 : mblk;  // values packed in the block
         const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
         const uint32_t bc = s_bc[bt];
         uint8_t* dst = s_tile + front + s_off[bt];
+        if (FM2) {
+          if (sub == 0) {  // the block's seed, szp_float.cc:812-864
+            dst[0] = (uint8_t)bseed[r];
+            dst[1] = (uint8_t)((uint32_t)bseed[r] >> 8);
+            dst[2] = (uint8_t)((uint32_t)bseed[r] >> 16);
+            dst[3] = (uint8_t)((uint32_t)bseed[r] >> 24);
+          }
+          dst += 4;
+        }
         if (sub == 0) dst[0] = (uint8_t)bc;
         if (bc == 0 || ml == 0) continue;
         const uint32_t ns = (m + 7) >> 3, B = bc >> 3, rr = bc & 7;
@@ -1157,16 +1183,16 @@ size_t compress_smem_bytes(uint32_t L, uint32_t tb) {
 
 // Bytes of one pipeline slot: the packed tile (read 16 bytes past its end by
 // the shifted copy) or the 16-byte-aligned input window it replaces.
-static uint32_t pipe_slot_bytes(uint32_t L, uint32_t tb) {
-  const size_t out = 4 + (size_t)tb * max_block_bytes(L) + 32;
+static uint32_t pipe_slot_bytes(uint32_t L, uint32_t tb, bool fm2) {
+  const size_t out = 4 + (size_t)tb * (max_block_bytes(L) + (fm2 ? 4 : 0)) + 32;  // fastmode2: a seed per block
   const size_t in = 4 * ((size_t)tb * L + 1) + 32;
   return (uint32_t)(((out > in ? out : in) + 15) & ~(size_t)15);
 }
 
-template <int LPB, bool BATCH = false, int ROUNDS = kRounds>
+template <int LPB, bool BATCH = false, int ROUNDS = kRounds, bool FM2 = false>
 static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
-  auto k = compress_fm1_pipe<LPB, BATCH, ROUNDS>;
-  const uint32_t slot = pipe_slot_bytes(a.seg.L, a.tb);
+  auto k = compress_pipe<LPB, BATCH, ROUNDS, FM2>;
+  const uint32_t slot = pipe_slot_bytes(a.seg.L, a.tb, FM2);
   const size_t smem = (size_t)kPipeSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
   static std::atomic<uint64_t> s_cache{0};
@@ -1194,6 +1220,17 @@ static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
 
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st) {
   size_t smem = compress_smem_bytes(a.seg.L, a.tb);
+  if (fm2) {
+    switch (lanes_per_block(a.seg.L)) {
+      case 1: return launch_lanes<1, false, kRounds, true>(a, st);
+      case 2: return launch_lanes<2, false, kRounds, true>(a, st);
+      case 4: return launch_lanes<4, false, kRounds, true>(a, st);
+      case 8: return launch_lanes<8, false, kRounds, true>(a, st);
+      case 16: return launch_lanes<16, false, kRounds, true>(a, st);
+      case 32: return launch_lanes<32, false, kRounds, true>(a, st);
+      default: break;
+    }
+  }
   if (!fm2) {
     switch (lanes_per_block(a.seg.L)) {
       case 1: return launch_lanes<1>(a, st);

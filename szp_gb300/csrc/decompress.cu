@@ -697,7 +697,7 @@ struct DecSlot {
 // Bytes of the block-offset area at the front of a slot.
 __host__ __device__ constexpr uint32_t dec_pos_bytes(uint32_t tb) { return 4 * tb + 32; }
 
-template <uint32_t L, uint32_t TB, int NS, bool BATCH>
+template <uint32_t L, uint32_t TB, int NS, bool BATCH, bool FM2>
 __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, uint32_t slot_bytes, DecSlot* meta,
                                              uint64_t* full, uint64_t* empty, uint32_t* s_epoch,
                                              volatile uint32_t* s_stop_k, const volatile uint32_t* s_started) {
@@ -721,9 +721,10 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     }
     const DecField& fd = BATCH ? a.fields[a.tile_field[tile]] : a.f;
     const Segments sg = fd.seg;
-    const DecTile dt = dec_tile(sg, tile - fd.tile_base, fd.tiles_per_seg, TB, false);
+    const DecTile dt = dec_tile(sg, tile - fd.tile_base, fd.tiles_per_seg, TB, FM2);
     // nothing to write: a failed plan, an empty segment, a tile past its segment's blocks
-    if (fd.plan->bad || !dt.any || (dt.nblk == 0 && !dt.first)) continue;  // the slot stays free
+    // (fastmode1 keeps a segment's first tile for its seed)
+    if (fd.plan->bad || !dt.any || (dt.nblk == 0 && (FM2 || !dt.first))) continue;  // the slot stays free
     const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
     const uint64_t R0 = fd.reg0[dt.seg], R1 = fd.reg1[dt.seg];
     const uint32_t rlen = (uint32_t)(R1 - R0);
@@ -735,10 +736,10 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     m.err = fd.err;
     m.nblk = dt.nblk;
     m.first = dt.first;
-    m.e0 = lo + 1 + dt.blk0 * L;
+    m.e0 = FM2 ? lo + dt.blk0 * L : lo + 1 + dt.blk0 * L;  // fastmode2 blocks start with their seed
     m.nel = dt.nblk ? (uint32_t)min((uint64_t)dt.nblk * L, hi - m.e0) : 0u;
     m.seed = 0;
-    if (dt.first) {
+    if (!FM2 && dt.first) {
       const uint8_t* sp = fd.in + R0 - 4;  // the segment's 4-byte seed precedes its blocks
       m.seed = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
                ((uint32_t)__ldg(sp + 3) << 24);
@@ -750,7 +751,7 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     uint32_t tx = 0;
     uintptr_t p0 = 0, p1 = 0, q0 = 0, q1 = 0;
     if (dt.nblk) {
-      const uint32_t* bp = fd.blkpos + seg_block_base(sg, dt.seg, false) + dt.blk0;
+      const uint32_t* bp = fd.blkpos + seg_block_base(sg, dt.seg, FM2) + dt.blk0;
       const uint32_t s0 = min(__ldg(bp), rlen);
       uint32_t s1 = (uint32_t)min((uint64_t)rlen, (uint64_t)__ldg(bp + dt.nblk - 1) + a.maxsz);
       if (s1 < s0) s1 = s0;
@@ -876,9 +877,9 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
   }
 }
 
-template <int LPB, bool BATCH, int ROUNDS>
-__global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __grid_constant__ DecArgs a,
-                                                                      uint32_t slot_bytes) {
+template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false>
+__global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_constant__ DecArgs a,
+                                                                  uint32_t slot_bytes) {
   constexpr int NS = kDecSlots, NC = kDecControl, WARPS = 8;
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
@@ -909,11 +910,13 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
   __syncthreads();
   if (warp == WARPS + NC) {
     if (lane == 0)
-      dec_producer<L, TB, NS, BATCH>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k, &s_started);
+      dec_producer<L, TB, NS, BATCH, FM2>(a, s_slots, slot_bytes, s_meta, s_full, s_empty, &s_epoch, &s_stop_k,
+                                          &s_started);
     return;
   }
   if (warp >= WARPS) {
-    dec_control<NS, NC>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
+    // fastmode2 blocks carry their own seeds: no look-back, nothing to control
+    if (!FM2) dec_control<NS, NC>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
     return;
   }
 
@@ -938,7 +941,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
     const uint32_t tile = s_meta[s].tile;
     if (threadIdx.x == 0) s_started = k + 1;
     if (tile >= a.ntiles) {
-      if (k) finish(k - 1);
+      if (!FM2 && k) finish(k - 1);  // fastmode2 tiles are finished at once
       return;
     }
     const uint32_t nblk = s_meta[s].nblk, nel = s_meta[s].nel, span0 = s_meta[s].span0;
@@ -950,18 +953,39 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
     // ---- unpack deltas and prefix-add inside each lane ----
     uint32_t pre[ROUNDS][8];
     uint32_t lex[ROUNDS], rbase[ROUNDS];
+    uint32_t seedv[ROUNDS];  // fastmode2: each block's seed
     uint32_t wtot = 0;
     bool corrupt = false;
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
       const uint32_t bt = wfirst + r * BPR + grp;
-      const uint32_t m = bt < nblk ? min(L, nel - bt * L) : 0u;
+      const uint32_t mblk = bt < nblk ? min(L, nel - bt * L) : 0u;
+      const uint32_t m = FM2 ? (mblk ? mblk - 1 : 0u) : mblk;  // values packed in the block
       const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
       uint32_t d[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) d[j] = 0;
       uint32_t off = 0, bc = 0;
-      if (m) {
+      seedv[r] = 0;
+      if (FM2 && mblk) {
+        // fastmode2: the block's 4-byte seed, then its header (a one-element
+        // block has no header on the decode side, szpd_float.cc:481)
+        const uint32_t b0 = bpos[bt] - span0;
+        if (b0 + 4 > spanlen) {
+          corrupt = true;
+        } else {
+          seedv[r] = (uint32_t)sp[b0] | ((uint32_t)sp[b0 + 1] << 8) | ((uint32_t)sp[b0 + 2] << 16) |
+                     ((uint32_t)sp[b0 + 3] << 24);
+        }
+        off = b0 + 4;
+        if (m) {
+          bc = off < spanlen ? sp[off] : 255u;
+          if (bc > 33 || off + block_bytes(m, bc) > spanlen) {
+            corrupt = true;
+            bc = 0;
+          }
+        }
+      } else if (!FM2 && m) {
         off = bpos[bt] - span0;
         bc = off < spanlen ? sp[off] : 255u;
         if (bc > 33 || off + block_bytes(m, bc) > spanlen) {
@@ -969,7 +993,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
           bc = 0;
         }
       }
-      if (__all_sync(0xffffffffu, (m == L || m == 0) && bc <= 15)) {
+      if (!FM2 && __all_sync(0xffffffffu, (m == L || m == 0) && bc <= 15)) {
         // every block of the round is full and has at most one byte plane:
         // the lane's plane and remainder bytes come from aligned word loads
         if (bc) {
@@ -1038,6 +1062,42 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_fm1_pipe(const __gr
         pre[r][j] = run;
       }
       lex[r] = run;
+    }
+    if constexpr (FM2) {
+      // every block restarts from its seed: a scan over the block's LPB lanes,
+      // the values staged, then the tile finished at once
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) {
+        uint32_t incl = lex[r];
+#pragma unroll
+        for (int o = 1; o < LPB; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o, LPB);
+          if (sub >= o) incl += y;
+        }
+        lex[r] = incl - lex[r];
+      }
+      if (__any_sync(0xffffffffu, corrupt) && lane == 0) atomicOr(s_meta[s].err, kErrCorrupt);
+      compute_sync();  // every read of the span is done
+      uint32_t* stage = reinterpret_cast<uint32_t*>(slot + PB);
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) {
+        const uint32_t bt = wfirst + r * BPR + grp;
+        const uint32_t mblk = bt < nblk ? min(L, nel - bt * L) : 0u;
+        const uint32_t m = mblk ? mblk - 1 : 0u;
+        const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+        if (mblk && sub == 0) stage[bt * L] = seedv[r];
+        const uint32_t q0 = seedv[r] + lex[r];
+        const uint32_t k1 = bt * L + 1 + 8 * sub;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          if ((uint32_t)j < ml) stage[k1 + j] = q0 + pre[r][j];
+      }
+      compute_sync();
+      const float ebp = s_meta[s].eb;
+      cta_dequant_store(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
+      compute_sync();  // every read of the slot is done
+      if (threadIdx.x == 0) mbar_arrive(&s_empty[s]);
+      continue;
     }
     // the rounds' warp scans, interleaved: four independent shuffle chains
     {
@@ -1284,9 +1344,9 @@ static uint32_t dec_slot_bytes(uint32_t L, uint32_t tb, uint32_t maxsz) {
   return (uint32_t)((dec_pos_bytes(tb) + (span > stage ? span : stage) + 15) & ~(size_t)15);
 }
 
-template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds>
+template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds, bool FM2 = false>
 static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
-  auto k = decode_fm1_pipe<LPB, BATCH, ROUNDS>;
+  auto k = decode_pipe<LPB, BATCH, ROUNDS, FM2>;
   const uint32_t slot = dec_slot_bytes(8 * LPB, a.tb, a.maxsz);
   const size_t smem = (size_t)kDecSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
@@ -1315,6 +1375,15 @@ static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
 
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {
   if (a.fm2) {
+    switch (dec_lanes_per_block(a.f.seg.L)) {
+      case 1: return launch_dec_lanes<1, false, kDecRounds, true>(a, st);
+      case 2: return launch_dec_lanes<2, false, kDecRounds, true>(a, st);
+      case 4: return launch_dec_lanes<4, false, kDecRounds, true>(a, st);
+      case 8: return launch_dec_lanes<8, false, kDecRounds, true>(a, st);
+      case 16: return launch_dec_lanes<16, false, kDecRounds, true>(a, st);
+      case 32: return launch_dec_lanes<32, false, kDecRounds, true>(a, st);
+      default: break;
+    }
     decode_generic<kDecWarps, true><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
     return cudaGetLastError();
   }

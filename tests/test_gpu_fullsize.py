@@ -3,7 +3,7 @@ checked bit for bit against the oracle (the C restatement runs them in a
 few seconds on the host cores):
 
 * random walk, 2^24 floats, ABS eb = 1e-4 * range
-* 512^3 Fourier field, REL 1e-2 / 1e-3 / 1e-4
+* 512^3 Fourier field, REL 1e-2 / 1e-3 / 1e-4 (and fastmode2 at 1e-3)
 * 8192^2 Laplace field with 40% zero blocks, ABS 1e-5
 
 plus size-independent properties: decompressed values equal the oracle's,
@@ -26,27 +26,27 @@ def torch():
     return t
 
 
-def _roundtrip(szp, torch, dx, n, eb_mode, bound, T):
-    cap = szp.max_stream_bytes(n, 32, T, 1)
+def _roundtrip(szp, torch, dx, n, eb_mode, bound, T, mode=1):
+    cap = szp.max_stream_bytes(n, 32, T, mode)
     dout = torch.empty(cap, dtype=torch.uint8, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
     size = szp.compress_dev(dx.data_ptr(), n, dout.data_ptr(), cap, eb_mode,
                             bound if eb_mode == szp.ABS else 0.0, bound if eb_mode == szp.REL else 0.0,
-                            32, T, 1, st)
+                            32, T, mode, st)
     dy = torch.empty(n, dtype=torch.float32, device="cuda")
-    szp.decompress_dev(dout.data_ptr(), size, n, dy.data_ptr(), 32, T, 1, st)
+    szp.decompress_dev(dout.data_ptr(), size, n, dy.data_ptr(), 32, T, mode, st)
     assert szp.sync_status(st) == 0, szp.last_error()
     return dout[:size].cpu().numpy().tobytes(), dy.cpu().numpy()
 
 
-def _check(szp, port, torch, x, eb_mode, bound, T=T_HOST):
+def _check(szp, port, torch, x, eb_mode, bound, T=T_HOST, mode=1):
     dx = torch.from_numpy(x).cuda()
-    s, y = _roundtrip(szp, torch, dx, x.size, eb_mode, bound, T)
+    s, y = _roundtrip(szp, torch, dx, x.size, eb_mode, bound, T, mode)
     eb = port.rel_bound(x, bound) if eb_mode == szp.REL else bound
-    s_or = port.compress(x, eb, 32, T, 1)
+    s_or = port.compress(x, eb, 32, T, mode)
     assert len(s) == len(s_or)
     assert s == s_or
-    y_or = port.decompress(s_or, x.size, 32, T, 1)
+    y_or = port.decompress(s_or, x.size, 32, T, mode)
     assert np.array_equal(y.view(np.uint32), y_or.view(np.uint32))
     ebf = np.float32(eb)
     viol = np.abs(x.astype(np.float64) - y.astype(np.float64)) > float(ebf)
@@ -68,6 +68,13 @@ def test_fourier_512cube(szp, port, torch, rel):
     from szp_gb300.workloads import fourier3d_torch
     x = fourier3d_torch(512, 2, device="cuda").cpu().numpy()
     _check(szp, port, torch, x, szp.REL, rel)
+
+
+def test_fourier_512cube_fastmode2(szp, port, torch):
+    """fastmode2 (a seed per block, no cross-block prefix) at full size."""
+    from szp_gb300.workloads import fourier3d_torch
+    x = fourier3d_torch(512, 2, device="cuda").cpu().numpy()
+    _check(szp, port, torch, x, szp.REL, 1e-3, mode=2)
 
 
 def test_laplace_8192sq(szp, port, torch):
