@@ -1,11 +1,12 @@
 // compress.cu -- SZp fastmode1 / fastmode2 float32 compressors for sm_103a.
 //
-// One launch does the whole stream: every CTA ("tile") owns up to WARPS*BPW
-// consecutive SZp blocks of one segment, quantizes them, reduces each block's
-// max |delta| to its bit count, finds its byte offset with a decoupled
-// look-back over the tiles' byte counts, packs the blocks into shared memory
-// at the destination's alignment, and writes its contiguous span with 16-byte
-// stores.  HBM traffic: 4n bytes read, stream bytes written.
+// blockSize 8..256 (a power of two): compress_pipe, a persistent,
+// warp-specialised pipeline (a producer warp stages tile inputs by TMA, eight
+// compute warps quantize, analyse and pack each tile in shared memory, control
+// warps find the tile's stream offset by decoupled look-back and write it with
+// 16-byte stores).  Other blockSizes: compress_generic, one warp per block.
+// The REL range pass (rel_bound_kernel, rel_batch_kernel for batches) runs
+// first.  HBM traffic: 4n bytes read (twice with REL), stream bytes written.
 //
 // Reference semantics followed (SZp/src/szp_float.cc):
 //   quantize  (int)(x * (double)(1.0f/eb))                    :185,209,228
@@ -22,65 +23,6 @@
 #include "szp_tma.cuh"
 
 namespace szp {
-
-// Writes the block's bytes into shared memory at dst (any alignment).
-// Called by a full warp; lane j owns element j.  m = elements (1..32),
-// sign = ballot of negative deltas (valid lanes only), v = |delta| (0 for
-// lanes >= m).
-__device__ __forceinline__ void pack_block32(uint8_t* dst, uint32_t m, uint32_t bc, uint32_t sign, uint32_t v,
-                                             int lane) {
-  if (lane == 0) dst[0] = (uint8_t)bc;
-  if (bc == 0) return;
-  const uint32_t ns = (m + 7) >> 3;
-  // sign bits: element j -> bit 7-(j%8) of byte j/8 (szp_TypeManager.cc:820-844)
-  if ((uint32_t)lane < ns) dst[1 + lane] = (uint8_t)(__brev(sign) >> (24 - 8 * lane));
-  uint8_t* p = dst + 1 + ns;
-  const uint32_t B = bc >> 3, r = bc & 7;
-  if (B) {
-    // byte planes: B little-endian bytes of v>>r per element (szp_TypeManager.cc:36-52)
-    if ((uint32_t)lane < m) {
-      uint32_t hi = v >> r;
-      uint8_t* q = p + lane * B;
-      q[0] = (uint8_t)hi;
-      if (B > 1) q[1] = (uint8_t)(hi >> 8);
-      if (B > 2) q[2] = (uint8_t)(hi >> 16);
-      if (B > 3) q[3] = (uint8_t)(hi >> 24);
-    }
-    p += B * m;
-  }
-  if (r) {
-    // remainder: the low r bits of every element as one MSB-first bit string
-    // (szp_TypeManager.cc:122-434).  Lane k assembles output byte k.
-    const uint32_t nrem = (r * m + 7) >> 3;
-    const uint32_t lo = v & ((1u << r) - 1u);
-    if (r == 1) {
-      uint32_t bits = __ballot_sync(0xffffffffu, lo != 0);
-      if ((uint32_t)lane < nrem) p[lane] = (uint8_t)(__brev(bits) >> (24 - 8 * lane));
-    } else {
-      const uint32_t k = lane;
-      const uint32_t j0 = (8 * k) / r;
-      uint32_t acc = 0;
-#pragma unroll
-      for (int s = 0; s < 4; s++) {
-        uint32_t j = j0 + s;
-        uint32_t val = __shfl_sync(0xffffffffu, lo, j & 31);
-        int start = (int)(j * r) - (int)(8 * k);
-        if (j < 32 && start < 8) {
-          int sh = 8 - start - (int)r;
-          acc |= sh >= 0 ? (val << sh) : (val >> (-sh));
-        }
-      }
-      if (k < nrem) p[k] = (uint8_t)acc;
-    }
-  }
-}
-
-__device__ __forceinline__ void store_u32le(uint8_t* p, uint32_t v) {
-  p[0] = (uint8_t)v;
-  p[1] = (uint8_t)(v >> 8);
-  p[2] = (uint8_t)(v >> 16);
-  p[3] = (uint8_t)(v >> 24);
-}
 
 // Copy `len` bytes staged in shared memory starting at s_out[align] to global
 // dst (where (uintptr_t)dst % 16 == align).  16-byte stores for whole
@@ -186,35 +128,12 @@ __device__ __forceinline__ uint32_t scan_warps(uint32_t* s_w, uint32_t mine, int
 // per lane.  Eight elements fill whole bytes in every section of a block
 // (one sign byte, 8*B bytes of byte planes, r bytes of remainder bits), so
 // each lane packs its part of a block without talking to other lanes; only
-// the block max (LPB-lane reduction) and the byte offsets (warp scan, CTA
-// scan, decoupled look-back) are shared.  A warp handles ROUNDS groups of
-// 32/LPB consecutive blocks; a 256-thread CTA a tile of 8*ROUNDS*32/LPB blocks.
+// the block max (LPB-lane reduction) and the byte offsets (CTA scan,
+// decoupled look-back) are shared.  A warp handles ROUNDS groups of 32/LPB
+// consecutive blocks; the 8 compute warps a tile of 8*ROUNDS*32/LPB blocks.
+// fastmode2 keeps the layout: a block's L-1 deltas leave its last lane 7.
 // ---------------------------------------------------------------------------
 
-// Stages a tile's bytes (shared memory s_out[align .. align+len)) to global
-// dst (dst % 16 == align): bulk copy for the 16-byte-aligned middle, byte
-// stores for the ragged ends.  Every thread of the CTA calls it.
-__device__ __forceinline__ void flush_span_bulk(uint8_t* __restrict__ gdst, uint8_t* __restrict__ s_out,
-                                                uint32_t align, uint32_t len) {
-  fence_async_smem();
-  __syncthreads();
-  if (len == 0) return;
-  uint8_t* g0 = gdst - align;
-  const uint32_t end = align + len;
-  const uint32_t i0 = (align + 15) & ~15u;
-  const uint32_t i1 = end & ~15u;
-  if (i1 > i0) {
-    if (threadIdx.x == 0) {
-      bulk_store(g0 + i0, s_out + i0, i1 - i0);
-      bulk_commit();
-    }
-    for (uint32_t b = align + threadIdx.x; b < i0; b += blockDim.x) g0[b] = s_out[b];
-    for (uint32_t b = i1 + threadIdx.x; b < end; b += blockDim.x) g0[b] = s_out[b];
-    if (threadIdx.x == 0) bulk_wait_read();
-  } else {
-    for (uint32_t b = align + threadIdx.x; b < end; b += blockDim.x) g0[b] = s_out[b];
-  }
-}
 
 // Exact path for |x/eb| >= 2^24 (or NaN/inf), out of line so the common path
 // issues no FP64 instructions; returns q in the low word, flags in the high.
@@ -236,20 +155,6 @@ __device__ __forceinline__ int32_t quantize_lean(float x, float inv, uint32_t& f
   return q;
 }
 
-// q for 8 values; the rare slow elements are redone behind a warp-uniform branch.
-__device__ __forceinline__ void quantize8(const float* xv, float inv, int32_t* q, uint32_t& flags) {
-  bool slow = false;
-#pragma unroll
-  for (int j = 0; j < 8; j++) {
-    const float p = __fmul_rz(xv[j], inv);
-    q[j] = __float2int_rz(p);
-    slow |= !(fabsf(p) < 16777216.0f);
-  }
-  if (__any_sync(0xffffffffu, slow)) {
-#pragma unroll
-    for (int j = 0; j < 8; j++) q[j] = quantize_lean(xv[j], inv, flags);
-  }
-}
 
 // Tile geometry, computed by the producer.
 struct TileGeo {
@@ -262,7 +167,8 @@ struct TileGeo {
 };
 
 // ---------------------------------------------------------------------------
-// Persistent, warp-specialised pipeline (fastmode1, blockSize L = 8*LPB).
+// Persistent, warp-specialised pipeline (blockSize L = 8*LPB; fastmode1, and
+// fastmode2 with its per-block seeds).
 //
 // A CTA works through tiles until the tickets run out.  Warp roles:
 //   compute  (warps 0-7)  quantize, delta, sign and bit-count analysis, the

@@ -1,7 +1,7 @@
 // decompress.cu -- SZp fastmode1 / fastmode2 float32 decompressors for sm_103a.
 //
 // The stream keeps no block index: a block's position depends on the bit
-// counts of all blocks before it in its segment (szpd_float.cc:76-118).  Four
+// counts of all blocks before it in its segment (szpd_float.cc:76-118).  Three
 // launches recover the positions and decode:
 //
 //  1. dec_setup   one CTA reads eb and the T segment offsets, validates them and
@@ -21,11 +21,15 @@
 //                 (entry, exit) pairs the predecessors published; a CTA whose
 //                 entry proves wrong re-walks from the true one.  Each chunk then
 //                 writes the header offset of each of its blocks.
-//  3. decode      per tile of blocks: the tile's stream span is staged in shared
-//                 memory by a bulk copy; LPB lanes per block unpack 8 elements
-//                 each (sign byte, byte planes, remainder bits are byte-aligned
-//                 per 8 elements), prefix-add (fastmode1: warp/CTA scans and a
-//                 look-back over the tiles of a segment) and dequantize.
+//  3. decode      decode_pipe (blockSize 8..256, a power of two), a persistent,
+//                 warp-specialised pipeline: per tile of blocks the stream span
+//                 and block offsets are staged in shared memory by TMA; LPB
+//                 lanes per block unpack 8 elements each (sign byte, byte
+//                 planes and remainder bits are byte-aligned per 8 elements),
+//                 prefix-add (fastmode1: warp and tile scans and a look-back
+//                 over the tiles of a segment; fastmode2: a scan inside the
+//                 block from its seed) and dequantize.  decode_generic covers
+//                 the other blockSizes.
 #include <atomic>
 
 #include "szp_device.cuh"
@@ -217,11 +221,6 @@ struct SmemChain {
   }
 };
 
-__device__ __forceinline__ uint2 ld_volatile_u2(const uint2* p) {
-  uint2 v;
-  asm volatile("ld.volatile.global.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
-  return v;
-}
 
 // Re-walks, in order, every chunk from `from` on whose first header is not
 // the exit of the chunk before it (e = exit before chunk `from`); thread-serial.
@@ -638,23 +637,6 @@ __device__ __forceinline__ DecTile dec_tile(const Segments& sg, uint32_t tile, u
   return d;
 }
 
-// Stores 8 consecutive floats at y[s..) (ml valid); mis = s mod 4 of the
-// float address (same for every lane of the tile).
-__device__ __forceinline__ void store8(float* __restrict__ y, uint64_t s, uint32_t ml, uint32_t mis,
-                                       const float v[8]) {
-  float* p = y + s;
-  if (ml == 8 && mis == 0) {
-    reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
-    reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
-  } else if (ml == 8 && mis == 2) {
-#pragma unroll
-    for (int j = 0; j < 8; j += 2) reinterpret_cast<float2*>(p)[j / 2] = make_float2(v[j], v[j + 1]);
-  } else {
-#pragma unroll
-    for (int j = 0; j < 8; j++)
-      if ((uint32_t)j < ml) p[j] = v[j];
-  }
-}
 
 constexpr int kDecWarps = 8;
 constexpr int kDecRounds = 4;

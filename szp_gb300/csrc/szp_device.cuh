@@ -220,73 +220,5 @@ __device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_
   return excl;
 }
 
-// CTA-wide decoupled look-back: every thread of the CTA (a multiple of 32,
-// at most 1024) reads one predecessor per round trip, so a tile whose
-// nearest finished predecessor is D tiles back waits ceil(D / blockDim.x)
-// round trips instead of ceil(D / 32).  All threads must call it; returns the
-// exclusive prefix to every thread.  s_red needs 2 * (blockDim.x / 32) + 2 words.
-__device__ __forceinline__ uint64_t lookback_sum_cta(const uint64_t* status, uint32_t tile, uint32_t stop_at,
-                                                     uint32_t epoch, uint32_t* err, uint64_t* s_red) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
-  uint32_t* s_first = reinterpret_cast<uint32_t*>(s_red + nwarps + 2);  // nwarps words
-  uint64_t excl = 0;
-  int64_t base = (int64_t)tile - 1;
-  uint32_t spins = 0;
-  while (base >= (int64_t)stop_at) {
-    const int64_t idx = base - threadIdx.x;  // distance grows with the thread index
-    uint64_t s = 0;
-    bool ready = true, incl = false;
-    if (idx >= (int64_t)stop_at) {
-      s = ld_volatile_u64(status + idx);
-      ready = status_epoch(s) == (epoch & 0xFFFFF) && status_flag(s) != 0;
-      incl = ready && status_flag(s) == kFlagInclusive;
-    }
-    const uint32_t bi = __ballot_sync(0xffffffffu, incl);
-    const uint32_t bn = __ballot_sync(0xffffffffu, !ready);
-    if (lane == 0) {
-      s_first[warp] = bi ? (uint32_t)(__ffs(bi) - 1) : 32u;  // nearest inclusive in this warp
-      s_red[warp] = bn;                                        // not-ready lanes
-    }
-    __syncthreads();
-    // nearest inclusive over the whole window
-    int wstar = nwarps;
-    uint32_t lstar = 32;
-    for (int w = 0; w < nwarps; w++)
-      if (s_first[w] < 32) {
-        wstar = w;
-        lstar = s_first[w];
-        break;
-      }
-    // every predecessor up to it must be ready
-    bool wait = false;
-    for (int w = 0; w < nwarps && w <= wstar; w++) {
-      uint32_t nr = (uint32_t)s_red[w];
-      if (w == wstar) nr &= (lstar == 31) ? 0xffffffffu : ((2u << lstar) - 1u);
-      if (nr) wait = true;
-    }
-    __syncthreads();
-    if (wait) {
-      if (++spins > kSpinLimit) {
-        if (threadIdx.x == 0) atomicOr(err, kErrLookbackTimeout);
-        return 0;
-      }
-      continue;
-    }
-    const bool mine = idx >= (int64_t)stop_at &&
-                      (warp < wstar || (warp == wstar && (uint32_t)lane <= lstar));
-    uint64_t v = mine ? status_value(s) : 0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) s_red[warp] = v;
-    __syncthreads();
-    uint64_t tot = 0;
-    for (int w = 0; w < nwarps; w++) tot += s_red[w];
-    __syncthreads();
-    excl += tot;
-    if (wstar < nwarps) break;
-    base -= blockDim.x;
-  }
-  return excl;
-}
 
 }  // namespace szp
