@@ -18,7 +18,8 @@ cpu_baseline  the oracle (C restatement of the reference, OpenMP on all host
         cores, same T) on a 2^25-value sample of the field.
 
 --impl reference times the reference's CPU algorithm (the oracle port; the
-reference sources are not on the GPU host) on the same workload.
+reference's sources are not present where the benchmark runs) on the same
+workload.
 Multi-GPU: replicas only (each rank runs the same step on its own GPU).
 """
 import argparse

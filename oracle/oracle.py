@@ -3,8 +3,8 @@
 Two CPU implementations of SZp's float32 fastmode1/fastmode2 codec live here:
 
 * ``Port``: the C restatement in ``oracle/szp_oracle.c`` (explicit segment
-  count T, caller buffers).  This is the checker for the CUDA library and the
-  "port" CPU baseline of bench.py.
+  count T, caller buffers).  The tests compare the CUDA library against it,
+  and bench.py times it as the "port" CPU baseline.
 * ``Reference``: the reference library compiled from its own sources into
   ``oracle/_ref/libszp_ref.so`` (only where the sources exist).  Its segment
   count is the OpenMP thread count, set here with ``omp_set_num_threads``.
