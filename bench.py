@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-fm2", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-window", type=float, default=0.2, help="seconds of arrivals per rate")
     ap.add_argument("--batched-fields", type=int, default=1024)
@@ -568,6 +569,43 @@ def main():
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
                "api": "szp_compress + szp_decompress (C ABI via ctypes; pinned input, library-malloc'd results)"}
 
+    # fastmode2 (SZP_RANDOMACCESS: a seed per block) on the same field, REL 1e-3
+    fm2 = None
+    if not args.no_fm2:
+        cap2 = szp.max_stream_bytes(n, L, T, 2)
+        d_s2 = torch.empty(cap2, dtype=torch.uint8, device=dev)
+        szp.set_timing(True)
+        for i in range(4):
+            szp.compress_dev_async(x.data_ptr(), n, d_s2.data_ptr(), cap2, d_size.data_ptr(), szp.REL, 0.0, 1e-3,
+                                   L, T, 2, st)
+            szp.decompress_dev_async(d_s2.data_ptr(), cap2, d_size.data_ptr(), n, d_y.data_ptr(), L, T, 2, st)
+            if i == 0:
+                torch.cuda.synchronize()
+                for slot in range(5):
+                    szp.kernel_time(slot)  # drop the first round trip
+        torch.cuda.synchronize()
+        assert szp.sync_status(st) == 0, szp.last_error()
+        kt = {name: szp.kernel_time(slot) for slot, name in
+              enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
+        szp.set_timing(False)
+        avg = {k: v[0] / v[1] for k, v in kt.items() if v[1]}
+        size2 = int(d_size.item())
+        # both fastmodes quantize and dequantize alike: fastmode1 at the same bound
+        # must give the same floats bit for bit
+        y1 = torch.empty_like(d_y)
+        szp.compress_dev_async(x.data_ptr(), n, d_stream.data_ptr(), cap, d_size.data_ptr(), szp.REL, 0.0, 1e-3,
+                               L, T, 1, st)
+        szp.decompress_dev_async(d_stream.data_ptr(), cap, d_size.data_ptr(), n, y1.data_ptr(), L, T, 1, st)
+        torch.cuda.synchronize()
+        assert szp.sync_status(st) == 0, szp.last_error()
+        assert torch.equal(y1.view(torch.int32), d_y.view(torch.int32)), "fastmode2 and fastmode1 results differ"
+        del y1
+        fm2 = {"rel": 1e-3, "ratio": round(4.0 * n / size2, 3),
+               "compress_gbs": round(4.0 * n / ((avg["rel_range"] + avg["compress"]) / 1e3) / 1e9, 2),
+               "decompress_gbs": round(4.0 * n / ((avg["dec_setup"] + avg["locate"] + avg["decode"]) / 1e3) / 1e9, 2),
+               "kernels_ms": {k: round(v, 4) for k, v in avg.items()}}
+        del d_s2
+
     batched = None
     if not args.no_batched:
         batched = batched_workload(szp, torch, dev, T, args.batched_fields)
@@ -605,6 +643,7 @@ def main():
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "fastmode2": fm2,
             "batched": batched,
             "serving": serving,
             "gpu_launches": int(launches),

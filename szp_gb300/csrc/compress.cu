@@ -1196,7 +1196,18 @@ __global__ void __launch_bounds__(256) rel_batch_kernel(const __grid_constant__ 
       mx = fmaxf(mx, x[i]);
     }
     const float4* x4 = reinterpret_cast<const float4*>(x + b0);
-    for (uint64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+    const uint32_t bs = blockDim.x;
+    uint64_t i = threadIdx.x;
+    // four independent 16-byte loads in flight per thread
+    for (; i + 3 * bs < n4; i += 4 * bs) {
+      const float4 v0 = __ldg(x4 + i), v1 = __ldg(x4 + i + bs);
+      const float4 v2 = __ldg(x4 + i + 2 * bs), v3 = __ldg(x4 + i + 3 * bs);
+      mn = fminf(mn, fminf(fminf(fminf(v0.x, v0.y), fminf(v0.z, v0.w)), fminf(fminf(v1.x, v1.y), fminf(v1.z, v1.w))));
+      mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v0.x, v0.y), fmaxf(v0.z, v0.w)), fmaxf(fmaxf(v1.x, v1.y), fmaxf(v1.z, v1.w))));
+      mn = fminf(mn, fminf(fminf(fminf(v2.x, v2.y), fminf(v2.z, v2.w)), fminf(fminf(v3.x, v3.y), fminf(v3.z, v3.w))));
+      mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v2.x, v2.y), fmaxf(v2.z, v2.w)), fmaxf(fmaxf(v3.x, v3.y), fmaxf(v3.z, v3.w))));
+    }
+    for (; i < n4; i += bs) {
       const float4 v = __ldg(x4 + i);
       mn = fminf(mn, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
       mx = fmaxf(mx, fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w)));

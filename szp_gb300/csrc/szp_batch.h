@@ -15,7 +15,7 @@
 namespace szp {
 
 constexpr uint32_t kBatchL = 32;          // blockSize of the batched path
-constexpr uint32_t kRelChunk = 1u << 18;  // floats per range-pass work item
+constexpr uint32_t kRelChunk = 1u << 15;  // floats per range-pass work item (128 KiB: 32 loads per thread)
 
 inline uint32_t batch_tile_blocks(int rounds) { return 8u * (uint32_t)rounds * 8u; }
 
