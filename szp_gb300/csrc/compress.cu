@@ -128,8 +128,9 @@ __device__ __forceinline__ uint32_t scan_warps(uint32_t* s_w, uint32_t mine, int
 // per lane.  Eight elements fill whole bytes in every section of a block
 // (one sign byte, 8*B bytes of byte planes, r bytes of remainder bits), so
 // each lane packs its part of a block without talking to other lanes; only
-// the block max (LPB-lane reduction) and the byte offsets (CTA scan,
-// decoupled look-back) are shared.  A warp handles ROUNDS groups of 32/LPB
+// the block max (LPB-lane reduction) and the byte offsets (a scan over the
+// warp's lane groups and rounds, the warps' totals, decoupled look-back) are
+// shared.  A warp handles ROUNDS groups of 32/LPB
 // consecutive blocks; the 8 compute warps a tile of 8*ROUNDS*32/LPB blocks.
 // fastmode2 keeps the layout: a block's L-1 deltas leave its last lane 7.
 // ---------------------------------------------------------------------------
@@ -171,10 +172,11 @@ struct TileGeo {
 // fastmode2 with its per-block seeds).
 //
 // A CTA works through tiles until the tickets run out.  Warp roles:
-//   compute  (warps 0-7)  quantize, delta, sign and bit-count analysis, the
-//                         scan of block sizes, then packing of the blocks into
-//                         the tile's slot from offset 0.  They never wait for
-//                         the tile's stream offset.
+//   compute  (warps 0-7)  quantize, delta, sign and bit-count analysis, a
+//                         scan of each warp's block sizes in registers, one
+//                         barrier for the warps' totals, then packing of the
+//                         blocks into the tile's slot from offset 0.  They
+//                         never wait for the tile's stream offset.
 //   control  (kPipeControl warps, tiles round robin)  decoupled look-back for
 //                         the stream offset, then a shifted copy of the packed
 //                         slot to the stream with 16-byte stores.
@@ -182,7 +184,7 @@ struct TileGeo {
 //                         tiles' input windows by bulk copy (TMA).
 // kPipeSlots shared-memory slots cycle through four mbarriers each: full
 // (producer -> compute, control), agg (tile byte count known), packed
-// (compute -> control) and empty (control -> producer).  Tickets are drawn in
+// (every compute warp -> control) and empty (control -> producer).  Tickets are drawn in
 // order and every wait depends only on lower tickets or earlier stages of the
 // same tile, so the pipeline cannot deadlock; every wait is bounded.
 // ---------------------------------------------------------------------------
@@ -204,43 +206,6 @@ struct SlotMeta {
   uint64_t* out_size;
   uint32_t* err;       // the field's error word
 };
-
-// Exclusive scan of n (<= 1024) values in shared memory by the 256 compute
-// threads; returns the total.  s_part needs 8 words.
-__device__ __forceinline__ uint32_t compute_scan_excl(uint32_t* v, uint32_t n, uint32_t* s_part) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t per = (n + 255) / 256;
-  const uint32_t i0 = threadIdx.x * per;
-  uint32_t loc[4], sum = 0;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    loc[k] = ((uint32_t)k < per && i0 + k < n) ? v[i0 + k] : 0u;
-    sum += loc[k];
-  }
-  uint32_t incl = sum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += y;
-  }
-  if (lane == 31) s_part[warp] = incl;
-  compute_sync();
-  uint32_t wex = 0, tot = 0;
-#pragma unroll
-  for (int w = 0; w < 8; w++) {
-    uint32_t pw = s_part[w];
-    if (w < warp) wex += pw;
-    tot += pw;
-  }
-  uint32_t run = wex + incl - sum;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    if ((uint32_t)k < per && i0 + k < n) v[i0 + k] = run;
-    run += loc[k];
-  }
-  compute_sync();
-  return tot;
-}
 
 // eb (big-endian) and, when every segment but the last is empty (n < T),
 // their zero offsets (szp_float.cc:164,280-289); one warp.
@@ -460,9 +425,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
   extern __shared__ __align__(16) uint8_t s_slots[];
   __shared__ SlotMeta s_meta[NS];
   __shared__ uint32_t s_agg[NS];
-  __shared__ uint32_t s_off[TB];
-  __shared__ uint8_t s_bc[TB];
-  __shared__ uint32_t s_part[8];
+  __shared__ uint32_t s_wtot[2][8];  // compute warps' packed bytes, by tile parity
   __shared__ uint32_t s_thr[36];
   __shared__ uint32_t s_epoch;
   __shared__ volatile uint32_t s_stop_k;
@@ -476,7 +439,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
     for (int s = 0; s < NS; s++) {
       mbar_init(&s_full[s], 1);
       mbar_init(&s_aggb[s], 1);
-      mbar_init(&s_packed[s], 1);
+      mbar_init(&s_packed[s], 8);  // one arrival per compute warp
       mbar_init(&s_empty[s], 1);
     }
     s_stop_k = kStopTile;
@@ -517,6 +480,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
     // ---- analysis: q, deltas, signs, block max, bit count, block size ----
     uint32_t vv[ROUNDS][8];
     uint32_t sgnb[ROUNDS];
+    uint32_t rinfo[ROUNDS];  // the lane's block: bit count, then (after the scan) its offset in the warp's run * 64
     int32_t bseed[ROUNDS];  // fastmode2: each block's seed, in its first lane
     const uint32_t sh = 1 + g.d;  // slot index of tile element 0
     const uint32_t ph = sh & 3;   // its 16-byte phase (same for every lane: L % 8 == 0)
@@ -611,26 +575,58 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
       sgnb[r] = sb;
 #pragma unroll
       for (int o = 1; o < LPB; o <<= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-      if (sub == 0 && bt < g.nblk) {
-        uint32_t bc = 0;
-        if (lmax) {
-          const int kk = 32 - __clz(lmax);
-          bc = kk + (kk >= 21 && lmax >= s_thr[kk + 1] ? 1 : 0);
-        }
-        const uint32_t m = min(L, g.nel - bt * L);
-        s_bc[bt] = (uint8_t)bc;
-        s_off[bt] = FM2 ? 4 + block_bytes(m - 1, bc) : block_bytes(m, bc);  // fastmode2: seed, L-1 deltas
+      // every lane of the block holds its bit count and size
+      uint32_t bc = 0;
+      if (lmax) {
+        const int kk = 32 - __clz(lmax);
+        bc = kk + (kk >= 21 && lmax >= s_thr[kk + 1] ? 1 : 0);
       }
+      rinfo[r] = bc;
     }
       return slow;
     };
     if (__any_sync(0xffffffffu, analyse(std::false_type{}))) analyse(std::true_type{});
     if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(s_meta[s].err, kErrQuantRange);
-    compute_sync();  // block sizes complete; the input window is dead from here on
 
-    // ---- block offsets in the tile; publish the tile's byte count ----
+    // ---- block offsets: a scan of the warp's block sizes over its lane
+    // groups and rounds, then one barrier for the warps' totals (which also
+    // ends every read of the input window) ----
+    uint32_t wrun = 0;
+    {
+      uint32_t incl[ROUNDS], bsz[ROUNDS];
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) {
+        const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
+        const uint32_t m = bt < g.nblk ? min(L, g.nel - bt * L) : 0u;
+        const uint32_t bc = rinfo[r];
+        bsz[r] = m ? (FM2 ? 4 + block_bytes(m - 1, bc) : block_bytes(m, bc)) : 0u;  // fastmode2: seed, L-1 deltas
+        incl[r] = bsz[r];
+      }
+#pragma unroll
+      for (int o = LPB; o < 32; o <<= 1) {
+#pragma unroll
+        for (int r = 0; r < ROUNDS; r++) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl[r], o);
+          if (lane >= o) incl[r] += y;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < ROUNDS; r++) {
+        rinfo[r] |= (wrun + incl[r] - bsz[r]) << 6;
+        wrun += __shfl_sync(0xffffffffu, incl[r], 31);
+      }
+    }
+    uint32_t* wtot = s_wtot[k & 1];  // alternate: a fast warp's next tile never meets a slow warp's reads
+    if (lane == 0) wtot[warp] = wrun;
+    compute_sync();
     const uint32_t front = seed ? 4u : 0u;
-    const uint32_t agg = compute_scan_excl(s_off, g.nblk, s_part) + front;
+    uint32_t wexcl = front, agg = front;
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+      const uint32_t t = wtot[w];
+      wexcl += w < warp ? t : 0u;
+      agg += t;
+    }
     if (threadIdx.x == 0) {
       s_agg[s] = agg;
       const bool head = s_meta[s].ltile == 0;  // a field's first tile has no predecessor
@@ -649,9 +645,8 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
     if (full) {
 #pragma unroll
       for (int r = 0; r < ROUNDS; r++) {
-        const uint32_t bt = (warp * ROUNDS + r) * BPR + grp;
-        const uint32_t bc = s_bc[bt];
-        uint8_t* dst = s_tile + front + s_off[bt];
+        const uint32_t bc = rinfo[r] & 63;
+        uint8_t* dst = s_tile + wexcl + (rinfo[r] >> 6);
         if (sub == 0) dst[0] = (uint8_t)bc;
         const uint32_t B = bc >> 3, rr = bc & 7;
         constexpr uint32_t ns = L / 8;
@@ -701,8 +696,8 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
         const uint32_t mblk = min(L, g.nel - bt * L);
         const uint32_t m = FM2 ? mblk - 1 : mblk;  // values packed in the block
         const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
-        const uint32_t bc = s_bc[bt];
-        uint8_t* dst = s_tile + front + s_off[bt];
+        const uint32_t bc = rinfo[r] & 63;
+        uint8_t* dst = s_tile + wexcl + (rinfo[r] >> 6);
         if (FM2) {
           if (sub == 0) {  // the block's seed, szp_float.cc:812-864
             dst[0] = (uint8_t)bseed[r];
@@ -746,8 +741,14 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
         }
       }
     }
-    compute_sync();  // the slot is packed; s_off and s_bc are free for the next tile
-    if (threadIdx.x == 0) mbar_arrive(&s_packed[s]);
+    // fastmode1 tiles measured faster with the compute warps kept in step by
+    // an end-of-tile barrier, fastmode2 tiles without it
+    if (FM2) {
+      __syncwarp();
+    } else {
+      compute_sync();
+    }
+    if (lane == 0) mbar_arrive(&s_packed[s]);  // the warp's part of the slot is packed
   }
 }
 
