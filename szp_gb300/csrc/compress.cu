@@ -399,7 +399,7 @@ __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const
       write_header_warp(out, m.eb, m.seg, lane);
     } else {
       excl = lookback_sum(a.status, tile, m.tile_base, epoch, a.err);
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+      if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
     const uint64_t gpos = 4 + 8ull * m.seg.T + excl;
     const bool fits = gpos + agg <= cap;
@@ -630,7 +630,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
     if (threadIdx.x == 0) {
       s_agg[s] = agg;
       const bool head = s_meta[s].ltile == 0;  // a field's first tile has no predecessor
-      st_release_u64(a.status + tile, make_status(s_epoch, head ? kFlagInclusive : kFlagAggregate, agg));
+      st_relaxed_u64(a.status + tile, make_status(s_epoch, head ? kFlagInclusive : kFlagAggregate, agg));
       mbar_arrive(&s_aggb[s]);
     }
 
@@ -825,11 +825,11 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   if (warp == 0) {
     uint64_t excl = 0;
     if (tile == 0) {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
+      if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, agg));
     } else {
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+      if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
       excl = lookback_sum(a.status, tile, 0, epoch, a.err);
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
+      if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
     if (lane == 0) s_base = excl;
   }

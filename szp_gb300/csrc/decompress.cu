@@ -849,7 +849,7 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
       }
     } else {
       base = (uint32_t)lookback_sum(a.status, tile, meta[s].seg_tile0, epoch, a.err);
-      if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(base + agg)));
+      if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(base + agg)));
     }
     if (lane == 0) {
       s_base[s] = base;
@@ -1117,7 +1117,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       s_agg[s] = agg;
       const bool first = s_meta[s].first;
       const uint32_t v = first ? s_meta[s].seed + agg : agg;
-      st_release_u64(a.status + tile, make_status(s_epoch, first ? kFlagInclusive : kFlagAggregate, v));
+      st_relaxed_u64(a.status + tile, make_status(s_epoch, first ? kFlagInclusive : kFlagAggregate, v));
       mbar_arrive(&s_aggb[s]);
     }
 
@@ -1218,13 +1218,13 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
         const uint8_t* sp = in + R0 - 4;
         excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
         if (lane == 0) {
-          st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
+          st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
           fd.y[lo] = dequant(excl, eb, ebsp);
         }
       } else {
-        if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
+        if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
         excl = (uint32_t)lookback_sum(a.status, tile, first_tile, epoch, a.err);
-        if (lane == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
+        if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
       }
       if (lane == 0) s_base = excl;
     }

@@ -115,6 +115,13 @@ __device__ __forceinline__ uint64_t ld_volatile_u64(const uint64_t* p) {
 __device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// Look-back words carry their value, so publishing one orders nothing else:
+// a relaxed store, which does not wait for the thread's earlier global writes
+// to drain (a release store held the publishing warp, and with it the CTA at
+// the next barrier, for that long).
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
   uint64_t v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
