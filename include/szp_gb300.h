@@ -204,6 +204,13 @@ void szp_gb300_bitcount_thresholds(uint32_t *thr34);
 /* Runs the device bit-count rule on n device values (diagnostics). */
 int szp_gb300_bitcount_probe(const uint32_t *d_max, uint8_t *d_bc, size_t n, void *stream);
 
+/* Checks the device's bounded waits: one device thread waits on a barrier
+ * that nothing completes, for at most limit_ns nanoseconds.  Returns
+ * SZP_GB300_ETIMEOUT when the wait gave up as it must (the time waited in
+ * *waited_ns); the device stays usable.  Every wait inside this library's
+ * kernels gives up the same way, after about two seconds. */
+int szp_gb300_wait_probe(unsigned long long limit_ns, unsigned long long *waited_ns);
+
 /* Per-kernel timing with CUDA events on the launching stream.  When enabled,
  * szp_gb300_kernel_ms(slot) returns the duration of the last launch of:
  * 0 REL range, 1 compress, 2 decompress setup, 3 locate, 4 decode. */

@@ -127,6 +127,7 @@ _sig("szp_gb300_server_get_stats", ctypes.c_int, [_vp, ctypes.POINTER(ServerStat
 _sig("szp_gb300_server_clock", ctypes.c_double, [_vp])
 _sig("szp_gb300_server_destroy", None, [_vp])
 _sig("szp_gb300_last_repairs", ctypes.c_int, [])
+_sig("szp_gb300_wait_probe", ctypes.c_int, [ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)])
 
 _libc = ctypes.CDLL(None)
 _libc.free.argtypes = [_vp]
@@ -381,6 +382,14 @@ def kernel_time(slot):
 
 
 SLOT_REL, SLOT_COMPRESS, SLOT_SETUP, SLOT_LOCATE, SLOT_DECODE = range(5)
+
+
+def wait_probe(limit_ns):
+    """One device wait on a barrier nothing completes, bounded by limit_ns:
+    (status, nanoseconds waited); the status is ETIMEOUT when it gave up."""
+    waited = ctypes.c_ulonglong(0)
+    rc = _lib.szp_gb300_wait_probe(int(limit_ns), ctypes.byref(waited))
+    return rc, waited.value
 
 
 def last_repairs():

@@ -974,6 +974,23 @@ int szp_gb300_bitcount_probe(const uint32_t* d_max, uint8_t* d_bc, size_t n, voi
   return SZP_GB300_OK;
 }
 
+int szp_gb300_wait_probe(unsigned long long limit_ns, unsigned long long* waited_ns) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  cudaStream_t st = w->begin_own();
+  DevMisc* dm = w->dm();
+  CU(cudaMemsetAsync(&dm->err, 0, sizeof(uint32_t), st));
+  CU(launch_wait_probe(limit_ns, &dm->err, reinterpret_cast<unsigned long long*>(&dm->out_size), st));
+  count_launches(1);
+  size_t waited = 0;
+  rc = finish_sync(*w, st, &waited);
+  w->end(st);
+  if (waited_ns) *waited_ns = waited;
+  return rc;
+}
+
 void szp_gb300_set_timing(int enable) { g_timing = enable ? 1 : 0; }
 
 void szp_gb300_set_locate_overlap(int bytes) { g_overlap = bytes; }

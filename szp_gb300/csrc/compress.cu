@@ -303,6 +303,7 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
     const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
     SlotMeta& m = meta[s];
     if (tile >= a.ntiles) {
+      drain_copies<NS>(full, k);
       m.tile = kStopTile;
       *s_stop_k = k;
       mbar_arrive(&full[s]);
@@ -1292,6 +1293,24 @@ cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds,
 
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st) {
   rel_bound_kernel<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// Diagnostics of the bounded waits: one thread waits on an mbarrier that
+// nothing arrives at, for at most limit_ns; it records the time it waited and
+// flags the launch like a pipeline wait that gives up.
+__global__ void wait_probe_kernel(uint64_t limit_ns, uint32_t* err, unsigned long long* waited) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  const uint64_t t0 = globaltimer_ns();
+  const bool done = mbar_wait_ns(&bar, 0, limit_ns);
+  *waited = globaltimer_ns() - t0;
+  if (!done) atomicOr(err, kErrLookbackTimeout);
+}
+
+cudaError_t launch_wait_probe(uint64_t limit_ns, uint32_t* err, unsigned long long* waited, cudaStream_t st) {
+  wait_probe_kernel<<<1, 32, 0, st>>>(limit_ns, err, waited);
   return cudaGetLastError();
 }
 

@@ -294,9 +294,9 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
     } else {
       for (uint32_t b = align + tid; b < end; b += NT) s_bytes[b] = __ldg(g0 + b);
     }
-    if (bulk && !mbar_wait_bounded(&s_bar, 0, 1u << 22)) {
+    if (bulk && !mbar_wait_ns(&s_bar, 0, kWaitNs)) {
       atomicOr(a.err, kErrLookbackTimeout);
-      mbar_wait_bounded(&s_bar, 0, 1u << 22);
+      mbar_wait_ns(&s_bar, 0, kWaitNs);  // the copy lands before the CTA may exit
     }
     __syncthreads();
   }
@@ -696,6 +696,7 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
     DecSlot& m = meta[s];
     if (tile >= a.ntiles) {
+      drain_copies<NS>(full, k);
       m.tile = kStopTile;
       *s_stop_k = k;
       mbar_arrive(&full[s]);

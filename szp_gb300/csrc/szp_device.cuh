@@ -16,7 +16,7 @@ constexpr int kMaxBitCount = 33;
 
 // Error bits written by kernels into Workspace::err (never a trap).
 enum : uint32_t {
-  kErrLookbackTimeout = 1u << 0,   // a look-back spin hit its iteration limit
+  kErrLookbackTimeout = 1u << 0,   // a wait (look-back or pipeline hand-off) gave up
   kErrCapacity = 1u << 1,          // stream larger than the caller's buffer
   kErrCorrupt = 1u << 2,           // malformed stream (bad bc, walk past end)
   kErrBlockCount = 1u << 3,        // segment did not hold the expected blocks
@@ -162,6 +162,13 @@ __device__ __forceinline__ void draw_ticket(LaunchState* ls, uint32_t ntiles, ui
 
 constexpr uint32_t kSpinLimit = 1u << 20;  // look-back polls (about a second) before giving up
 
+// True once a wait of the launch has given up: later waits then return at
+// once, so a launch that lost its hand-offs runs to its end with an error
+// instead of waiting out every later wait.
+__device__ __forceinline__ bool launch_gave_up(const uint32_t* err) {
+  return (*(const volatile uint32_t*)err & kErrLookbackTimeout) != 0;
+}
+
 // Decoupled look-back over an additive 42-bit quantity, by one full warp.
 // Each lane reads LB_K predecessors per round trip (lane l, slot k holds the
 // tile at distance 1 + l + 32k), so a window covers 32*LB_K tiles: a tile whose
@@ -211,7 +218,7 @@ __device__ __forceinline__ uint64_t lookback_sum(const uint64_t* status, uint32_
     }
     if (wait) {
       __nanosleep(500);  // a predecessor is still working: leave the issue slots to the compute warps
-      if (++spins > kSpinLimit) {
+      if (++spins > kSpinLimit || ((spins & 63) == 0 && launch_gave_up(err))) {
         if (lane == 0) atomicOr(err, kErrLookbackTimeout);
         return 0;
       }

@@ -135,6 +135,7 @@ cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds,
 cudaError_t prepare_compress_batch();
 cudaError_t launch_rel_batch(const RelBatchArgs& a, uint32_t grid, cudaStream_t st);
 uint32_t rel_encode_host(float v);
+cudaError_t launch_wait_probe(uint64_t limit_ns, uint32_t* err, unsigned long long* waited, cudaStream_t st);
 cudaError_t launch_bitcount_probe(const uint32_t* in, uint8_t* out, uint64_t n, const BitcountTable& thr,
                                   cudaStream_t st);
 

@@ -13,17 +13,46 @@
 namespace szp {
 
 constexpr uint32_t kStopTile = 0xFFFFFFFFu;  // slot marker: no more tiles for this CTA
-constexpr uint32_t kWaitLimit = 1u << 24;    // mbarrier polls before a wait gives up
+constexpr uint32_t kWaitLimit = 1u << 24;    // polls of a shared-memory counter (with a 64 ns pause each)
+constexpr uint64_t kWaitNs = 2000000000ull;  // an mbarrier wait gives up after about two seconds
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for an mbarrier phase for at most `ns` nanoseconds; false if it did
+// not complete.
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, uint32_t parity, uint64_t ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (globaltimer_ns() - t0 < ns)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
 
 // Barrier over the 256 compute threads (warps 0-7) only.
 __device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-// Waits for an mbarrier phase; on timeout flags the launch and waits once more.
-__device__ __forceinline__ void mbar_wait_or_flag(uint64_t* bar, uint32_t parity, uint32_t* err) {
-  if (!mbar_wait_bounded(bar, parity, kWaitLimit)) {
-    atomicOr(err, kErrLookbackTimeout);
-    mbar_wait_bounded(bar, parity, kWaitLimit);
+// Waits for an mbarrier phase; after about two seconds flags the launch as
+// given up.  Once the launch is flagged, waits return after their first 256
+// polls.  The flag and the clock are read out of line, after 256 polls: a
+// read of the flag is a trip to L2, which would delay every short wait.
+static __device__ __noinline__ void mbar_wait_long(uint64_t* bar, uint32_t parity, uint32_t* err) {
+  if (launch_gave_up(err)) return;
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t i = 1;; i++) {
+    if (mbar_try_wait(bar, parity)) return;
+    if ((i & 255) == 0 && (launch_gave_up(err) || globaltimer_ns() - t0 > kWaitNs)) break;
   }
+  if (!launch_gave_up(err)) atomicOr(err, kErrLookbackTimeout);
+}
+__device__ __forceinline__ void mbar_wait_or_flag(uint64_t* bar, uint32_t parity, uint32_t* err) {
+#pragma unroll 1
+  for (int i = 0; i < 256; i++)
+    if (mbar_try_wait(bar, parity)) return;
+  mbar_wait_long(bar, parity, err);  // out of line: the clock and the flag stay off short waits
 }
 
 // A control warp's wait for slot phase `parity` of its k-th tile, or for the
@@ -31,15 +60,31 @@ __device__ __forceinline__ void mbar_wait_or_flag(uint64_t* bar, uint32_t parity
 __device__ __forceinline__ bool control_wait_full(uint64_t* full, uint32_t parity, uint32_t k,
                                                   const volatile uint32_t* s_stop_k, uint32_t* err) {
   bool got = false;
-  for (uint32_t i = 0; i < kWaitLimit; i++) {
-    if ((got = mbar_try_wait(full, parity))) break;
-    if (*s_stop_k <= k) break;
+  uint64_t t0 = 0;  // first read at the 256th poll
+  for (uint32_t i = 1; !(got = mbar_try_wait(full, parity)) && *s_stop_k > k; i++) {
+    if ((i & 255) == 0) {
+      if (launch_gave_up(err)) break;
+      const uint64_t t = globaltimer_ns();
+      if (t0 == 0) {
+        t0 = t;
+      } else if (t - t0 > kWaitNs) {
+        break;
+      }
+    }
   }
   if (!__all_sync(0xffffffffu, got)) {
     if ((threadIdx.x & 31) == 0 && *s_stop_k > k) atomicOr(err, kErrLookbackTimeout);
     return false;
   }
   return true;
+}
+
+// Called by a producer before it returns at position `k` (its stop): waits
+// until the bulk copies of its last NS positions have landed, so no copy
+// outlives the CTA even when a launch gave up its hand-offs.
+template <int NS>
+__device__ __forceinline__ void drain_copies(uint64_t* full, uint32_t k) {
+  for (uint32_t j = k >= (uint32_t)NS ? k - NS : 0u; j < k; j++) mbar_wait_ns(&full[j % NS], (j / NS) & 1, kWaitNs);
 }
 
 // Draws the next tile ticket for a persistent launch of `grid` CTAs over

@@ -38,13 +38,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait on an mbarrier phase; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
 // global -> shared bulk copy completing on bar (complete_tx of `bytes`).
 __device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
   asm volatile(

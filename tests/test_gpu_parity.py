@@ -143,6 +143,34 @@ def test_device_api(szp, port, torch):
     assert int(dsize.item()) == size
 
 
+def test_host_api_large_results(szp, port):
+    """Results above 32 MiB leave the device in pieces while host threads map
+    the malloc'd pages ahead: the bytes must be those of the oracle."""
+    rng = np.random.default_rng(81)
+    from szp_gb300.workloads import walk
+    n, T = 24_000_003, 16
+    x = walk(n, rng)
+    eb = float(np.float32(1e-7 * (x.max() - x.min())))
+    szp.set_segments(T)
+    s = szp.szp_compress(x, szp.ABS, eb, 0.0, 32, 1)
+    assert len(s) > 32 << 20
+    assert s == port.compress(x, eb, 32, T, 1)
+    y = szp.szp_decompress(s, n, 32, 1)
+    assert np.array_equal(bits(y), bits(port.decompress(s, n, 32, T, 1)))
+
+
+def test_bounded_wait_gives_up(szp, port):
+    """A device wait on a barrier that nothing completes gives up after its
+    limit and reports a timeout; the device stays usable."""
+    rc, waited = szp.wait_probe(50_000_000)
+    assert rc == szp.ETIMEOUT
+    assert 50_000_000 <= waited < 2_000_000_000
+    x = np.linspace(-1.0, 1.0, 100_000, dtype=np.float32)
+    szp.set_segments(4)
+    s = szp.szp_compress(x, szp.ABS, 1e-3, 0.0, 32, 1)
+    assert s == port.compress(x, 1e-3, 32, 4, 1)
+
+
 def test_empty_and_tiny(szp, port):
     for T in (1, 4):
         szp.set_segments(T)
