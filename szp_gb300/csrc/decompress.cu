@@ -976,16 +976,18 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
           bc = 0;
         }
       }
-      if (!FM2 && __all_sync(0xffffffffu, (m == L || m == 0) && bc <= 15)) {
+      constexpr uint32_t MF = FM2 ? L - 1 : L;  // values of a full block
+      if (__all_sync(0xffffffffu, (m == MF || m == 0) && bc <= 15)) {
         // every block of the round is full and has at most one byte plane:
         // the lane's plane and remainder bytes come from aligned word loads
+        // (fastmode2: L-1 values, the last lane's eighth is not one of them)
         if (bc) {
-          constexpr uint32_t NSB = L / 8;
+          constexpr uint32_t NSB = L / 8;  // sign bytes, ceil(MF / 8) either way
           const uint32_t B = bc >> 3, rr = bc & 7;
           const uint32_t ob = (uint32_t)(sp - s_slots) + off;  // the block in s_slots
           const uint32_t sb = s_slots[ob + 1 + sub];             // sign bits, szp_TypeManager.cc:820-844
           uint32_t lo, hi, plo = 0, phi = 0;
-          lds_le64(s_slots, ob + 1 + NSB + B * L + rr * sub, lo, hi);  // remainder, szp_TypeManager.cc:122-434
+          lds_le64(s_slots, ob + 1 + NSB + B * MF + rr * sub, lo, hi);  // remainder, szp_TypeManager.cc:122-434
           if (B) lds_le64(s_slots, ob + 1 + NSB + 8 * sub, plo, phi);  // byte plane, szp_TypeManager.cc:36-52
           const uint32_t t = __byte_perm(lo, 0, 0x0123);  // remainder bits 0..31, MSB first
           const uint32_t t2 = __funnelshift_l(__byte_perm(hi, 0, 0x0123), t, 4 * rr);  // bits 4rr..
@@ -997,7 +999,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
             const uint32_t h = __byte_perm(j < 4 ? plo : phi, 0, 0x4440 + (j & 3));
             const uint32_t v = h * pw + f;
             const uint32_t sg = (uint32_t)((sx << j) >> 31);
-            d[j] = (v ^ sg) - sg;
+            d[j] = (FM2 && j == 7 && sub == LPB - 1) ? 0u : (v ^ sg) - sg;
           }
         }
       } else if (m) {
