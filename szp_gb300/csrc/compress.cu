@@ -420,6 +420,9 @@ template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false>
 __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_constant__ CompressArgs a,
                                                                  uint32_t slot_bytes) {
   constexpr int NS = kPipeSlots, NC = kPipeControl;
+  // a control warp's next position must never share a slot phase it has not
+  // waited for (an mbarrier parity names one of two phases)
+  static_assert(NC <= NS, "more control warps than slots");
   constexpr uint32_t L = 8 * LPB;
   constexpr int BPR = 32 / LPB;
   constexpr uint32_t TB = 8 * ROUNDS * BPR;
