@@ -9,6 +9,7 @@
 #include <omp.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -147,6 +148,7 @@ struct Workspace {
   cudaEvent_t done = nullptr;
   DevBuf misc, rel_partial, status, in, stream, out, plan, walks, blkpos;
   uint8_t* h_small = nullptr;  // pinned: out_size (8) + err (4)
+  size_t last_stream = 0;      // size of this thread's last host-API stream
   // ring of event pairs per kernel slot: every launch is timed when timing
   // is on, and szp_gb300_kernel_time() sums the launches not yet read
   static constexpr int kRing = 1024;
@@ -530,6 +532,18 @@ void touch_pages(uint8_t* p, size_t bytes) {
   }
 }
 
+// Maps [p, p + bytes) with all OpenMP threads (1 MiB per task).
+void map_pages(uint8_t* p, size_t bytes) {
+  constexpr size_t kBatch = (size_t)1 << 20;
+  if (bytes < 8 * kBatch) {
+    touch_pages(p, bytes);
+    return;
+  }
+  const int64_t nb = (int64_t)((bytes + kBatch - 1) / kBatch);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t b = 0; b < nb; b++) touch_pages(p + b * kBatch, std::min(kBatch, bytes - (size_t)b * kBatch));
+}
+
 // Copies a device result into host memory that may be fresh (a malloc'd
 // result): worker threads map its pages ahead in address order while one
 // thread issues 16 MiB copies behind them, so the page faults overlap the
@@ -590,16 +604,29 @@ int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double
   CompressJob j{w->in.as<float>(), n, eb_mode, eb_abs, rel, L, T, fm, w->stream.as<uint8_t>(), cap, nullptr};
   rc = compress_launch(*w, j, st);
   if (rc) return rc;
+  // a malloc'd result is allocated while the GPU works, and as many of its
+  // pages as the previous stream of this thread had are mapped meanwhile (the
+  // stream's size is known only at the end)
+  uint8_t* dst = out_user;
+  if (!dst) {
+    const size_t alloc = std::max(cap, 4 + 4 * n);  // the reference hands out 4+4n bytes
+    dst = (uint8_t*)malloc(alloc);
+    if (!dst) {
+      finish_sync(*w, st, nullptr);
+      w->end(st);
+      return fail(SZP_GB300_ENOMEM, "malloc(%zu) failed", alloc);
+    }
+    map_pages(dst, std::min(w->last_stream, alloc));
+  }
   size_t sz = 0;
   rc = finish_sync(*w, st, &sz);
   w->end(st);
-  if (rc) return rc;
-  uint8_t* dst = out_user;
-  if (!dst) {
-    size_t alloc = sz > 4 + 4 * n ? sz : 4 + 4 * n;  // the reference hands out 4+4n bytes
-    dst = (uint8_t*)malloc(alloc);
-    if (!dst) return fail(SZP_GB300_ENOMEM, "malloc(%zu) failed", alloc);
-  } else if (sz > user_cap) {
+  if (rc) {
+    if (!out_user) free(dst);
+    return rc;
+  }
+  w->last_stream = sz;
+  if (out_user && sz > user_cap) {
     return fail(SZP_GB300_ECAPACITY, "stream of %zu bytes exceeds the %zu-byte output", sz, user_cap);
   }
   cudaError_t e = copy_to_host(dst, w->stream.p, sz, st);
