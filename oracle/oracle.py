@@ -1,6 +1,7 @@
 """Python handle on the oracle -- TEST INFRASTRUCTURE ONLY.
 
-Two CPU implementations of SZp's float32 fastmode1/fastmode2 codec live here:
+Two CPU implementations of SZp's fastmode1/fastmode2 codec (float32 and
+float64 data) live here:
 
 * ``Port``: the C restatement in ``oracle/szp_oracle.c`` (explicit segment
   count T, caller buffers).  The tests compare the CUDA library against it,
@@ -59,6 +60,16 @@ class Port:
         lib.szo_max_stream_bytes.restype = ctypes.c_size_t
         lib.szo_max_stream_bytes.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         lib.szo_max_threads.restype = ctypes.c_int
+        lib.szo_compress_d.restype = ctypes.c_int
+        lib.szo_compress_d.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, _c_size_p]
+        lib.szo_decompress_d.restype = ctypes.c_int
+        lib.szo_decompress_d.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        lib.szo_rel_bound_d.restype = ctypes.c_double
+        lib.szo_rel_bound_d.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double]
+        lib.szo_max_stream_bytes_d.restype = ctypes.c_size_t
+        lib.szo_max_stream_bytes_d.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         self.lib = lib
 
     def max_threads(self):
@@ -83,6 +94,30 @@ class Port:
         if rc != 0:
             raise RuntimeError("oracle decompress failed: %d" % rc)
         return y
+
+    def compress_d(self, x, eb, L=32, T=1, mode=1):
+        """Stream bytes for float64 x at absolute bound eb (double), T segments."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        cap = self.lib.szo_max_stream_bytes_d(x.size, L, T, mode)
+        out = np.empty(cap, dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        rc = self.lib.szo_compress_d(x.ctypes.data, x.size, float(eb), L, T, mode, out.ctypes.data, cap,
+                                     ctypes.byref(size))
+        if rc != 0:
+            raise RuntimeError("oracle compress_d failed: %d" % rc)
+        return out[: size.value].tobytes()
+
+    def decompress_d(self, stream, n, L=32, T=1, mode=1):
+        buf = np.frombuffer(stream, dtype=np.uint8)
+        y = np.empty(n, dtype=np.float64)
+        rc = self.lib.szo_decompress_d(buf.ctypes.data, buf.size, n, L, T, mode, y.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("oracle decompress_d failed: %d" % rc)
+        return y
+
+    def rel_bound_d(self, x, rel):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        return float(self.lib.szo_rel_bound_d(x.ctypes.data, x.size, rel))
 
     def rel_bound(self, x, rel):
         x = _f32(x)
@@ -131,24 +166,27 @@ class Reference:
         self.gomp.omp_set_num_threads(int(T))
 
     def compress(self, x, L=32, T=1, mode=1, eb_mode=0, abs_eb=0.0, rel=0.0):
-        """szp_compress(mode, SZ_FLOAT, ...) with T OpenMP threads."""
-        x = _f32(x)
+        """szp_compress(mode, SZ_FLOAT or SZ_DOUBLE (float64 x), ...) with T OpenMP threads."""
+        dbl = np.asarray(x).dtype == np.float64
+        x = np.ascontiguousarray(x, dtype=np.float64) if dbl else _f32(x)
         self.set_threads(T)
         size = ctypes.c_size_t(0)
-        p = self.lib.szp_compress(mode, 0, x.ctypes.data, ctypes.byref(size), eb_mode, abs_eb, rel, x.size, L)
+        p = self.lib.szp_compress(mode, 1 if dbl else 0, x.ctypes.data, ctypes.byref(size), eb_mode, abs_eb, rel,
+                                  x.size, L)
         if not p:
             raise RuntimeError("reference compress returned NULL")
         out = ctypes.string_at(p, size.value)
         self.libc.free(p)
         return out
 
-    def decompress(self, stream, n, L=32, T=1, mode=1):
+    def decompress(self, stream, n, L=32, T=1, mode=1, dtype=np.float32):
         self.set_threads(T)
+        dt = np.dtype(dtype)
         buf = np.frombuffer(stream, dtype=np.uint8).copy()
-        p = self.lib.szp_decompress(mode, 0, buf.ctypes.data, buf.size, n, L)
+        p = self.lib.szp_decompress(mode, 1 if dt == np.float64 else 0, buf.ctypes.data, buf.size, n, L)
         if not p and n:
             raise RuntimeError("reference decompress returned NULL")
-        y = np.frombuffer(ctypes.string_at(p, 4 * n), dtype=np.float32).copy() if n else np.empty(0, np.float32)
+        y = np.frombuffer(ctypes.string_at(p, dt.itemsize * n), dtype=dt).copy() if n else np.empty(0, dt)
         if p:
             self.libc.free(p)
         return y

@@ -28,6 +28,12 @@
  * fastmode2 (szp_float.cc:752-1076): segments as above, but every block starts
  * at lo + k*L and carries its own int32 seed; the diffs cover the m-1 elements
  * after the seed.
+ *
+ * float64 (SZp/src/szp_double.cc, szpd_double.cc): the same segments and
+ * blocks; eb is a big-endian double (8 bytes, szp_double.cc:164 and
+ * szp_CompressionToolkit.h:530-546), so the offsets start at byte 8;
+ * q = (int)(x * (1/eb)) with a double product (szp_double.cc:180,209,228)
+ * and x' = (double)q * eb (szpd_double.cc:67,86,112).
  */
 #include <math.h>
 #include <stdint.h>
@@ -65,6 +71,15 @@ static inline int32_t quantize(float x, double inv)
     return INT32_MIN;
 }
 
+/* q = (int)(x * inv) for double x, szp_double.cc:209,228: the double product
+ * rounds to nearest; out of range and NaN give INT32_MIN as above. */
+static inline int32_t quantize_d(double x, double inv)
+{
+    double p = x * inv;
+    if (p > -2147483649.0 && p < 2147483648.0) return (int32_t)p;
+    return INT32_MIN;
+}
+
 /* Float results that are NaN follow x86 SSE, the platform the reference's
  * fixtures were made on: a NaN operand propagates (quieted); an invalid
  * operation (0*inf, inf-inf) gives the default NaN 0xFFC00000.  aarch64 would
@@ -87,6 +102,40 @@ static inline float dequant(int32_t q, float eb)
 {
     float f = (float)q;
     return x86_nan_fix(f * eb, f, eb);
+}
+
+/* x86 SSE NaN rule for double results: a NaN operand propagates quieted, an
+ * invalid operation gives the default NaN 0xFFF8000000000000. */
+static inline double x86_nan_fix_d(double r, double a, double b)
+{
+    if (r == r) return r;
+    uint64_t u;
+    if (a != a) memcpy(&u, &a, 8);
+    else if (b != b) memcpy(&u, &b, 8);
+    else u = 0xFFF8000000000000ull;
+    u |= 0x0008000000000000ull;
+    memcpy(&r, &u, 8);
+    return r;
+}
+
+/* (double)q * eb, szpd_double.cc:67,86,112 */
+static inline double dequant_d(int32_t q, double eb)
+{
+    double f = (double)q;
+    return x86_nan_fix_d(f * eb, f, eb);
+}
+
+/* Element i of a float or double array, quantized. */
+static inline int32_t q_at(const void *x, int dbl, size_t i, double inv)
+{
+    return dbl ? quantize_d(((const double *)x)[i], inv) : quantize(((const float *)x)[i], inv);
+}
+
+/* y[i] = dequantized q, for a float or double output. */
+static inline void put_y(void *y, int dbl, size_t i, int32_t q, double eb)
+{
+    if (dbl) ((double *)y)[i] = dequant_d(q, eb);
+    else ((float *)y)[i] = dequant(q, (float)eb);
 }
 
 static inline void put_u32le(unsigned char *p, uint32_t v)
@@ -195,7 +244,7 @@ static inline void seg_bounds(size_t n, int T, int t, size_t *lo, size_t *hi)
     *hi = (t == T - 1) ? n : (size_t)(t + 1) * tsz;
 }
 
-/* Upper bound of the stream size for (n, L, T) in either mode. */
+/* Upper bound of the stream size for (n, L, T) in either mode (float). */
 size_t szo_max_stream_bytes(size_t n, int L, int T, int mode)
 {
     if (L <= 0 || T <= 0) return 0;
@@ -205,21 +254,28 @@ size_t szo_max_stream_bytes(size_t n, int L, int T, int mode)
     return 4 + 8 * (size_t)T + 4 * (size_t)T + nblk * (full + per);
 }
 
+/* The same for double data (8-byte eb). */
+size_t szo_max_stream_bytes_d(size_t n, int L, int T, int mode)
+{
+    size_t b = szo_max_stream_bytes(n, L, T, mode);
+    return b ? b + 4 : 0;
+}
+
 /* Encode segment [lo,hi) into o; returns bytes.  Fastmode1 loop,
  * szp_float.cc:206-275. */
-static size_t encode_segment_fm1(const float *x, size_t lo, size_t hi, double inv, size_t L,
+static size_t encode_segment_fm1(const void *x, int dbl, size_t lo, size_t hi, double inv, size_t L,
                                  unsigned char *o, uint32_t *v, unsigned char *s)
 {
     if (lo >= hi) return 0;
     size_t w = 0;
-    int32_t prior = quantize(x[lo], inv);
+    int32_t prior = q_at(x, dbl, lo, inv);
     put_u32le(o, (uint32_t)prior);
     w += 4;
     for (size_t i = lo + 1; i < hi; i += L) {
         size_t m = (i + L > hi) ? hi - i : L;
         uint32_t max = 0;
         for (size_t j = 0; j < m; j++) {
-            int32_t cur = quantize(x[i + j], inv);
+            int32_t cur = q_at(x, dbl, i + j, inv);
             uint32_t d = (uint32_t)cur - (uint32_t)prior; /* wrapping, as compiled x86 code does */
             prior = cur;
             s[j] = (int32_t)d < 0;
@@ -233,18 +289,18 @@ static size_t encode_segment_fm1(const float *x, size_t lo, size_t hi, double in
 
 /* Fastmode2 segment: every block restarts from its own seed,
  * szp_float.cc:812-864. */
-static size_t encode_segment_fm2(const float *x, size_t lo, size_t hi, double inv, size_t L,
+static size_t encode_segment_fm2(const void *x, int dbl, size_t lo, size_t hi, double inv, size_t L,
                                  unsigned char *o, uint32_t *v, unsigned char *s)
 {
     size_t w = 0;
     for (size_t i = lo; i < hi; i += L) {
         size_t m = (i + L > hi) ? hi - i : L;
-        int32_t prior = quantize(x[i], inv);
+        int32_t prior = q_at(x, dbl, i, inv);
         put_u32le(o + w, (uint32_t)prior);
         w += 4;
         uint32_t max = 0;
         for (size_t j = 0; j + 1 < m; j++) {
-            int32_t cur = quantize(x[i + j + 1], inv);
+            int32_t cur = q_at(x, dbl, i + j + 1, inv);
             uint32_t d = (uint32_t)cur - (uint32_t)prior;
             prior = cur;
             s[j] = (int32_t)d < 0;
@@ -256,20 +312,16 @@ static size_t encode_segment_fm2(const float *x, size_t lo, size_t hi, double in
     return w;
 }
 
-/* Full compressor with explicit segment count T (the reference's OpenMP
- * thread count).  mode 1 = fastmode1, 2 = fastmode2.  Writes into out
- * (capacity cap) and returns SZO_OK or an error. */
-int szo_compress(const float *x, size_t n, float eb, int L, int T, int mode,
-                 unsigned char *out, size_t cap, size_t *out_size)
+/* Compressor body for float (dbl = 0, eb header 4 bytes) or double data
+ * (dbl = 1, 8 bytes); inv and the header bytes come from the caller. */
+static int compress_any(const void *x, int dbl, size_t n, double inv, const unsigned char *ebb, int L, int T,
+                        int mode, unsigned char *out, size_t cap, size_t *out_size)
 {
     if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !out || !out_size) return SZO_ERR_ARG;
-    size_t head = 4 + 8 * (size_t)T;
+    const size_t hb = dbl ? 8 : 4;
+    size_t head = hb + 8 * (size_t)T;
     if (cap < head) return SZO_ERR_CAP;
-    /* float division stored in a double, szp_float.cc:185 */
-    double inv = (double)(1.0f / eb);
-    unsigned char ebb[4];
-    memcpy(ebb, &eb, 4);
-    out[0] = ebb[3]; out[1] = ebb[2]; out[2] = ebb[1]; out[3] = ebb[0];
+    memcpy(out, ebb, hb);
 
     size_t *sz = (size_t *)calloc((size_t)T, sizeof(size_t));
     unsigned char **buf = (unsigned char **)calloc((size_t)T, sizeof(unsigned char *));
@@ -289,9 +341,9 @@ int szo_compress(const float *x, size_t n, float eb, int L, int T, int mode,
 #pragma omp atomic write
             fail = 1;
         } else if (mode == 1) {
-            sz[t] = encode_segment_fm1(x, lo, hi, inv, (size_t)L, buf[t], v, s);
+            sz[t] = encode_segment_fm1(x, dbl, lo, hi, inv, (size_t)L, buf[t], v, s);
         } else {
-            sz[t] = encode_segment_fm2(x, lo, hi, inv, (size_t)L, buf[t], v, s);
+            sz[t] = encode_segment_fm2(x, dbl, lo, hi, inv, (size_t)L, buf[t], v, s);
         }
         free(v);
         free(s);
@@ -301,7 +353,7 @@ int szo_compress(const float *x, size_t n, float eb, int L, int T, int mode,
     size_t total = head;
     if (rc == SZO_OK) {
         size_t off = 0;
-        for (int t = 0; t < T; t++) { put_u64le(out + 4 + 8 * (size_t)t, off); off += sz[t]; }
+        for (int t = 0; t < T; t++) { put_u64le(out + hb + 8 * (size_t)t, off); off += sz[t]; }
         total = head + off;
         if (total > cap) rc = SZO_ERR_CAP;
     }
@@ -316,15 +368,41 @@ int szo_compress(const float *x, size_t n, float eb, int L, int T, int mode,
     return rc;
 }
 
+/* Full compressor with explicit segment count T (the reference's OpenMP
+ * thread count).  mode 1 = fastmode1, 2 = fastmode2.  Writes into out
+ * (capacity cap) and returns SZO_OK or an error. */
+int szo_compress(const float *x, size_t n, float eb, int L, int T, int mode,
+                 unsigned char *out, size_t cap, size_t *out_size)
+{
+    /* float division stored in a double, szp_float.cc:185 */
+    double inv = (double)(1.0f / eb);
+    unsigned char ebb[4], be[4];
+    memcpy(ebb, &eb, 4);
+    be[0] = ebb[3]; be[1] = ebb[2]; be[2] = ebb[1]; be[3] = ebb[0];
+    return compress_any(x, 0, n, inv, be, L, T, mode, out, cap, out_size);
+}
+
+/* Double compressor, szp_double.cc:149-309 (fastmode1), :759-920 (fastmode2):
+ * inv = 1/eb in double (szp_double.cc:180). */
+int szo_compress_d(const double *x, size_t n, double eb, int L, int T, int mode,
+                   unsigned char *out, size_t cap, size_t *out_size)
+{
+    double inv = 1.0 / eb;
+    unsigned char ebb[8], be[8];
+    memcpy(ebb, &eb, 8);
+    for (int i = 0; i < 8; i++) be[i] = ebb[7 - i];
+    return compress_any(x, 1, n, inv, be, L, T, mode, out, cap, out_size);
+}
+
 /* Decoder for one fastmode1 segment, szpd_float.cc:59-118. */
 static int decode_segment_fm1(const unsigned char *p, const unsigned char *end, size_t lo, size_t hi,
-                              float eb, size_t L, float *y, uint32_t *v, unsigned char *s)
+                              double eb, size_t L, void *y, int dbl, uint32_t *v, unsigned char *s)
 {
     if (lo >= hi) return SZO_OK;
     if (end - p < 4) return SZO_ERR_STREAM;
     int32_t prior = (int32_t)get_u32le(p);
     p += 4;
-    y[lo] = dequant(prior, eb);
+    put_y(y, dbl, lo, prior, eb);
     for (size_t i = lo + 1; i < hi; i += L) {
         size_t m = (i + L > hi) ? hi - i : L;
         size_t nb = get_block(p, end, v, s, m);
@@ -333,7 +411,7 @@ static int decode_segment_fm1(const unsigned char *p, const unsigned char *end, 
         for (size_t j = 0; j < m; j++) {
             uint32_t d = s[j] ? 0u - v[j] : v[j];
             prior = (int32_t)((uint32_t)prior + d);
-            y[i + j] = dequant(prior, eb);
+            put_y(y, dbl, i + j, prior, eb);
         }
     }
     return SZO_OK;
@@ -341,14 +419,14 @@ static int decode_segment_fm1(const unsigned char *p, const unsigned char *end, 
 
 /* Decoder for one fastmode2 segment, szpd_float.cc:425-637. */
 static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, size_t lo, size_t hi,
-                              float eb, size_t L, float *y, uint32_t *v, unsigned char *s)
+                              double eb, size_t L, void *y, int dbl, uint32_t *v, unsigned char *s)
 {
     for (size_t i = lo; i < hi; i += L) {
         size_t m = (i + L > hi) ? hi - i : L;
         if (end - p < 4) return SZO_ERR_STREAM;
         int32_t prior = (int32_t)get_u32le(p);
         p += 4;
-        y[i] = dequant(prior, eb);
+        put_y(y, dbl, i, prior, eb);
         /* a one-element block has no header byte on the decode side, although
          * the encoder wrote a 0 for it (szpd_float.cc:481 vs szp_float.cc:848);
          * it can only be the last block of a segment, so nothing shifts. */
@@ -359,22 +437,20 @@ static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, 
         for (size_t j = 0; j + 1 < m; j++) {
             uint32_t d = s[j] ? 0u - v[j] : v[j];
             prior = (int32_t)((uint32_t)prior + d);
-            y[i + j + 1] = dequant(prior, eb);
+            put_y(y, dbl, i + j + 1, prior, eb);
         }
     }
     return SZO_OK;
 }
 
-/* Full decompressor: stream (len bytes, including the 4-byte eb header),
- * explicit T.  Validates offsets against len. */
-int szo_decompress(const unsigned char *stream, size_t len, size_t n, int L, int T, int mode, float *y)
+/* Decompressor body: stream (len bytes, including the eb header of hb
+ * bytes), explicit T.  Validates offsets against len. */
+static int decompress_any(const unsigned char *stream, size_t len, size_t n, int L, int T, int mode, double eb,
+                          int dbl, void *y)
 {
-    if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !stream || (!y && n)) return SZO_ERR_ARG;
-    size_t head = 4 + 8 * (size_t)T;
+    const size_t hb = dbl ? 8 : 4;
+    size_t head = hb + 8 * (size_t)T;
     if (len < head) return SZO_ERR_STREAM;
-    unsigned char ebb[4] = {stream[3], stream[2], stream[1], stream[0]};
-    float eb;
-    memcpy(&eb, ebb, 4);
     const unsigned char *data = stream + head;
     const unsigned char *end = stream + len;
     int rc = SZO_OK;
@@ -382,15 +458,15 @@ int szo_decompress(const unsigned char *stream, size_t len, size_t n, int L, int
     for (int t = 0; t < T; t++) {
         size_t lo, hi;
         seg_bounds(n, T, t, &lo, &hi);
-        uint64_t off = get_u64le(stream + 4 + 8 * (size_t)t);
+        uint64_t off = get_u64le(stream + hb + 8 * (size_t)t);
         int r = SZO_OK;
         if (lo < hi && off > (uint64_t)(end - data)) r = SZO_ERR_STREAM;
         uint32_t *v = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)L);
         unsigned char *s = (unsigned char *)malloc((size_t)L);
         if (!v || !s) r = SZO_ERR_NOMEM;
         if (r == SZO_OK) {
-            if (mode == 1) r = decode_segment_fm1(data + off, end, lo, hi, eb, (size_t)L, y, v, s);
-            else r = decode_segment_fm2(data + off, end, lo, hi, eb, (size_t)L, y, v, s);
+            if (mode == 1) r = decode_segment_fm1(data + off, end, lo, hi, eb, (size_t)L, y, dbl, v, s);
+            else r = decode_segment_fm2(data + off, end, lo, hi, eb, (size_t)L, y, dbl, v, s);
         }
         free(v);
         free(s);
@@ -400,6 +476,30 @@ int szo_decompress(const unsigned char *stream, size_t len, size_t n, int L, int
         }
     }
     return rc;
+}
+
+/* Full decompressor: stream (len bytes, including the 4-byte eb header),
+ * explicit T.  Validates offsets against len. */
+int szo_decompress(const unsigned char *stream, size_t len, size_t n, int L, int T, int mode, float *y)
+{
+    if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !stream || (!y && n)) return SZO_ERR_ARG;
+    if (len < 4) return SZO_ERR_STREAM;
+    unsigned char ebb[4] = {stream[3], stream[2], stream[1], stream[0]};
+    float eb;
+    memcpy(&eb, ebb, 4);
+    return decompress_any(stream, len, n, L, T, mode, (double)eb, 0, y);
+}
+
+/* Double decompressor, szpd_double.cc:23-128 (fastmode1), :431-535 (fastmode2). */
+int szo_decompress_d(const unsigned char *stream, size_t len, size_t n, int L, int T, int mode, double *y)
+{
+    if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !stream || (!y && n)) return SZO_ERR_ARG;
+    if (len < 8) return SZO_ERR_STREAM;
+    unsigned char ebb[8];
+    for (int i = 0; i < 8; i++) ebb[i] = stream[7 - i];
+    double eb;
+    memcpy(&eb, ebb, 8);
+    return decompress_any(stream, len, n, L, T, mode, eb, 1, y);
 }
 
 /* REL bound: serial min/max and (max-min)*(float)rel in float,
@@ -416,6 +516,21 @@ float szo_rel_bound(const float *x, size_t n, double rel)
     float range = x86_nan_fix(mx - mn, mx, mn);
     float r = (float)rel;
     return x86_nan_fix(range * r, range, r);
+}
+
+/* REL bound for double data: serial min/max and (max-min)*rel in double,
+ * SZp/src/szp.cc:77-89. */
+double szo_rel_bound_d(const double *x, size_t n, double rel)
+{
+    if (n == 0) return 0.0;
+    double mn = x[0], mx = x[0];
+    for (size_t i = 0; i < n; i++) {
+        double v = x[i];
+        if (mn > v) mn = v;
+        else if (mx < v) mx = v;
+    }
+    double range = x86_nan_fix_d(mx - mn, mx, mn);
+    return x86_nan_fix_d(range * rel, range, rel);
 }
 
 /* The 34 bit-count thresholds: thr[k] = smallest m >= 1 with

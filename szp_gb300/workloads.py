@@ -80,7 +80,7 @@ def _pair(target):
     return -float(a), float(b), int(b) + int(a)
 
 
-def bitcount_sweep(rng, L=32):
+def bitcount_sweep(rng, L=32, dtype=np.float32):
     """Blocks whose max |delta| sweeps every bit count 0..33 (eb = 1)."""
     out = [0.0]
     targets = [0]
@@ -100,7 +100,26 @@ def bitcount_sweep(rng, L=32):
             blk[mask] = rng.integers(-3, 4, mask.sum())
         out.extend(blk.tolist())
     out.extend(rng.integers(-100, 100, 17).tolist())  # ragged tail
-    return np.array(out, dtype=np.float32)
+    return np.array(out, dtype=dtype)
+
+
+def walk64(n, rng):
+    """The walk in float64 (no rounding to float32)."""
+    steps = rng.normal(0.0, 0.01, n)
+    i = np.arange(n, dtype=np.float64)
+    return np.cumsum(steps) + np.sin(2 * np.pi * i / 4096.0)
+
+
+def specials64(rng, n=2000):
+    """float64 walk with NaN, +-inf, huge, denormal, -0.0, max-double entries and
+    values whose quantized product leaves the int32 range."""
+    x = walk64(n, rng) * 10.0
+    idx = rng.choice(np.arange(1, n), size=48, replace=False)
+    vals = [np.nan, np.inf, -np.inf, 3.0e9 * 1e-3, -3.0e9 * 1e-3, 4.9e-324, 1e-310, -0.0, 1.7e308, -1.7e308,
+            2147483.0, 2147483.6469]
+    for k, i in enumerate(idx):
+        x[i] = vals[k % len(vals)]
+    return x
 
 
 def specials(rng, n=2000):

@@ -43,6 +43,17 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_double():
+    path = os.path.join(ROOT, "tests", "golden", "golden_double.npz")
+    z = np.load(path)
+    meta = json.loads(bytes(z["meta"]).decode())
+    cases = []
+    for i, m in enumerate(meta):
+        cases.append(dict(m, x=z["x%d" % i], s=z["s%d" % i].tobytes(), y=z["y%d" % i]))
+    return cases
+
+
+@pytest.fixture(scope="session")
 def szp():
     import szp_gb300
     return szp_gb300
@@ -50,3 +61,7 @@ def szp():
 
 def eb_of(stream):
     return float(np.frombuffer(bytes(stream[:4])[::-1], dtype=np.float32)[0])
+
+
+def eb_of_double(stream):
+    return float(np.frombuffer(bytes(stream[:8])[::-1], dtype=np.float64)[0])

@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import eb_of
+from conftest import eb_of, eb_of_double
 
 
 def test_golden_streams(port, golden):
@@ -31,6 +31,27 @@ def test_golden_rel_bound(port, golden):
     assert rel
     for c in rel:
         assert port.rel_bound(c["x"], c["bound"]) == eb_of(c["s"]), c["name"]
+
+
+def test_golden_double_streams(port, golden_double):
+    """float64 (szp_double_* of the reference): streams byte for byte."""
+    assert len(golden_double) >= 50
+    for c in golden_double:
+        s = port.compress_d(c["x"], eb_of_double(c["s"]), c["L"], c["T"], c["mode"])
+        assert s == c["s"], c["name"]
+
+
+def test_golden_double_decompress(port, golden_double):
+    for c in golden_double:
+        y = port.decompress_d(c["s"], c["n"], c["L"], c["T"], c["mode"])
+        assert np.array_equal(y.view(np.uint64), c["y"].view(np.uint64)), c["name"]
+
+
+def test_golden_double_rel_bound(port, golden_double):
+    rel = [c for c in golden_double if c["eb_mode"] == 1]
+    assert rel
+    for c in rel:
+        assert port.rel_bound_d(c["x"], c["bound"]) == eb_of_double(c["s"]), c["name"]
 
 
 def test_bitcount_thresholds_exhaustive(port):
@@ -62,3 +83,19 @@ def test_live_reference_random(port, T, mode):
         assert port.compress(x, eb, 32, T, mode) == s_ref
         y_ref = reference_decompress_arg(ref, s_ref, n, 32, T, mode)
         assert np.array_equal(port.decompress(s_ref, n, 32, T, mode).view(np.uint32), y_ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_live_reference_random_double(port, mode):
+    from szp_gb300.workloads import walk64
+    ref = _reference()
+    rng = np.random.default_rng(2000 + mode)
+    for n, T in ((4096, 3), (50001, 6)):
+        x = walk64(n, rng) * rng.uniform(0.1, 100)
+        eb = 10 ** rng.uniform(-9, -3) * float(x.max() - x.min())
+        s = ref.compress(x, L=32, T=T, mode=mode, eb_mode=0, abs_eb=eb)
+        assert s == port.compress_d(x, eb, 32, T, mode)
+        y = ref.decompress(s, n, L=32, T=T, mode=mode, dtype=np.float64)
+        assert np.array_equal(y.view(np.uint64), port.decompress_d(s, n, 32, T, mode).view(np.uint64))
+        s = ref.compress(x, L=32, T=T, mode=mode, eb_mode=1, rel=1e-6)
+        assert s == port.compress_d(x, port.rel_bound_d(x, 1e-6), 32, T, mode)
