@@ -52,9 +52,11 @@ extern "C" {
 /* ---- reference entry points ------------------------------------------- */
 
 /* Replaces SZp/include/szp.h:33 (SZp/src/szp.cc:23-116).  fastMode 1 or 2,
- * dataType SZ_FLOAT, errBoundMode ABS or REL (REL: eb = (max-min)*(float)rel
- * over the data).  Returns a malloc'd stream the caller free()s; *outSize
- * gets its length.  NULL on error (SZ_DOUBLE is not provided). */
+ * dataType SZ_FLOAT (eb = (float)absErrBound, or REL: (max-min)*(float)rel)
+ * or SZ_DOUBLE (any other dataType, as in the reference: double data,
+ * eb = absErrBound or (max-min)*rel in double, an 8-byte eb header).  Returns
+ * a malloc'd stream the caller free()s; *outSize gets its length.  NULL on
+ * error. */
 unsigned char *szp_compress(int fastMode, int dataType, void *data, size_t *outSize, int errBoundMode,
                             double absErrBound, double relBoundRatio, size_t nbEle, int blockSize);
 
@@ -62,7 +64,8 @@ unsigned char *szp_compress(int fastMode, int dataType, void *data, size_t *outS
  * stream (eb header first).  byteLength, ignored by the reference, bounds
  * the bytes read here; a value smaller than the stream header makes the
  * library find the length by walking the last segment on the host.  Returns
- * a malloc'd float[nbEle] or NULL on error. */
+ * a malloc'd float[nbEle] (SZ_FLOAT) or double[nbEle] (any other dataType),
+ * or NULL on error. */
 void *szp_decompress(int fastMode, int dataType, unsigned char *bytes, size_t byteLength, size_t nbEle,
                      int blockSize);
 
@@ -121,6 +124,61 @@ float *szp_float_decompress_openmp_threadblock_randomaccess(size_t nbEle, float 
 void szp_float_decompress_openmp_threadblock_randomaccess_arg(float *newData, size_t nbEle, float absErrBound,
                                                               int blockSize, unsigned char *cmpBytes);
 
+/* float64 data (SZp/include/szp_double.h, szpd_double.h): the same streams
+ * with an 8-byte big-endian eb, q = (int)(x * (1/eb)) with a double product
+ * and x' = (double)q * eb.  The _arg compressors expect 8 + 8*nbEle bytes of
+ * output; the decompressors' cmpBytes points just past the 8-byte eb. */
+
+/* Replaces SZp/include/szp_double.h:30 (SZp/src/szp_double.cc:149-309). */
+unsigned char *szp_double_openmp_threadblock(double *oriData, size_t *outSize, double absErrBound, size_t nbEle,
+                                             int blockSize);
+
+/* Replaces SZp/include/szp_double.h:33 (SZp/src/szp_double.cc:320-484). */
+void szp_double_openmp_threadblock_arg(unsigned char *output, double *oriData, size_t *outSize,
+                                       double absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_double.h:36 (SZp/src/szp_double.cc:486-611): T = 1. */
+void szp_double_single_thread_arg(unsigned char *output, double *oriData, size_t *outSize, double absErrBound,
+                                  size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_double.h:39 (SZp/src/szp_double.cc:613-757);
+ * returns the bytes the GPU kernels moved. */
+size_t szp_double_single_thread_arg_record(unsigned char *output, double *oriData, size_t *outSize,
+                                           double absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_double.h:43 (SZp/src/szp_double.cc:759-920). */
+unsigned char *szp_double_openmp_threadblock_randomaccess(double *oriData, size_t *outSize, double absErrBound,
+                                                          size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szp_double.h:47 (SZp/src/szp_double.cc:922-1090). */
+void szp_double_openmp_threadblock_randomaccess_arg(unsigned char *output, double *oriData, size_t *outSize,
+                                                    double absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces SZp/include/szpd_double.h:21 (SZp/src/szpd_double.cc:23-128). */
+double *szp_double_decompress_openmp_threadblock(size_t nbEle, double absErrBound, int blockSize,
+                                                 unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_double.h:23 (SZp/src/szpd_double.cc:323-429). */
+void szp_double_decompress_openmp_threadblock_arg(double *newData, size_t nbEle, double absErrBound,
+                                                  int blockSize, unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_double.h:25 (SZp/src/szpd_double.cc:130-217). */
+void szp_double_decompress_single_thread_arg(double *newData, size_t nbEle, double absErrBound, int blockSize,
+                                             unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_double.h:27 (SZp/src/szpd_double.cc:219-321);
+ * returns the bytes the GPU kernels moved. */
+size_t szp_double_decompress_single_thread_arg_record(double *newData, size_t nbEle, double absErrBound,
+                                                      int blockSize, unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_double.h:29 (SZp/src/szpd_double.cc:431-534). */
+double *szp_double_decompress_openmp_threadblock_randomaccess(size_t nbEle, double absErrBound, int blockSize,
+                                                              unsigned char *cmpBytes);
+
+/* Replaces SZp/include/szpd_double.h:31 (SZp/src/szpd_double.cc:536-645). */
+void szp_double_decompress_openmp_threadblock_randomaccess_arg(double *newData, size_t nbEle, double absErrBound,
+                                                               int blockSize, unsigned char *cmpBytes);
+
 /* ---- extensions (no counterpart in the reference) ---------------------- */
 
 #define SZP_GB300_OK 0
@@ -158,6 +216,15 @@ int szp_gb300_compress_dev_async(int fastMode, const float *d_data, size_t nbEle
                                  double absErrBound, double relBoundRatio, int blockSize, int segments,
                                  unsigned char *d_out, size_t out_capacity, unsigned long long *d_outSize,
                                  void *stream);
+
+/* float64 device-pointer compressor (waits for the size) and decompressor
+ * (waits, returns the status); streams as szp_double_openmp_threadblock's. */
+size_t szp_gb300_max_stream_bytes_f64(size_t nbEle, int blockSize, int segments, int fastMode);
+int szp_gb300_compress_dev_f64(int fastMode, const double *d_data, size_t nbEle, int errBoundMode,
+                               double absErrBound, double relBoundRatio, int blockSize, int segments,
+                               unsigned char *d_out, size_t out_capacity, size_t *outSize, void *stream);
+int szp_gb300_decompress_dev_f64(int fastMode, const unsigned char *d_bytes, size_t byteLength, size_t nbEle,
+                                 int blockSize, int segments, double *d_out, void *stream);
 
 /* Device-pointer decompressor; asynchronous on stream.  d_bytes is a whole
  * stream of byteLength bytes in device memory. */

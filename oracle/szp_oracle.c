@@ -428,8 +428,10 @@ static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, 
         p += 4;
         put_y(y, dbl, i, prior, eb);
         /* a one-element block has no header byte on the decode side, although
-         * the encoder wrote a 0 for it (szpd_float.cc:481 vs szp_float.cc:848);
-         * it can only be the last block of a segment, so nothing shifts. */
+         * the encoder wrote a 0 for it (szpd_float.cc:483 vs szp_float.cc:848).
+         * With blockSize > 1 that is only a segment's last block, so nothing
+         * shifts; with blockSize 1 every block is one, and the reads fall one
+         * byte further behind per block, as in the reference. */
         if (m == 1) continue;
         size_t nb = get_block(p, end, v, s, m - 1);
         if (!nb) return SZO_ERR_STREAM;

@@ -63,6 +63,23 @@ _sig("szp_gb300_compress_dev_async", ctypes.c_int, [ctypes.c_int, _vp, _sz, ctyp
                                                     ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp, _sz, _vp,
                                                     _vp])
 _sig("szp_gb300_decompress_dev", ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, ctypes.c_int, ctypes.c_int, _vp, _vp])
+_sig("szp_gb300_max_stream_bytes_f64", _sz, [_sz, ctypes.c_int, ctypes.c_int, ctypes.c_int])
+_sig("szp_gb300_compress_dev_f64", ctypes.c_int, [ctypes.c_int, _vp, _sz, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp, _sz, _szp, _vp])
+_sig("szp_gb300_decompress_dev_f64", ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, ctypes.c_int, ctypes.c_int, _vp,
+                                                    _vp])
+for _n in ("szp_double_openmp_threadblock", "szp_double_openmp_threadblock_randomaccess"):
+    _sig(_n, _vp, [_vp, _szp, ctypes.c_double, _sz, ctypes.c_int])
+for _n in ("szp_double_openmp_threadblock_arg", "szp_double_single_thread_arg",
+           "szp_double_openmp_threadblock_randomaccess_arg"):
+    _sig(_n, None, [_vp, _vp, _szp, ctypes.c_double, _sz, ctypes.c_int])
+_sig("szp_double_single_thread_arg_record", _sz, [_vp, _vp, _szp, ctypes.c_double, _sz, ctypes.c_int])
+for _n in ("szp_double_decompress_openmp_threadblock", "szp_double_decompress_openmp_threadblock_randomaccess"):
+    _sig(_n, _vp, [_sz, ctypes.c_double, ctypes.c_int, _vp])
+for _n in ("szp_double_decompress_openmp_threadblock_arg", "szp_double_decompress_single_thread_arg",
+           "szp_double_decompress_openmp_threadblock_randomaccess_arg"):
+    _sig(_n, None, [_vp, _sz, ctypes.c_double, ctypes.c_int, _vp])
+_sig("szp_double_decompress_single_thread_arg_record", _sz, [_vp, _sz, ctypes.c_double, ctypes.c_int, _vp])
 _sig("szp_gb300_decompress_dev_async", ctypes.c_int, [ctypes.c_int, _vp, _sz, _vp, _sz, ctypes.c_int,
                                                       ctypes.c_int, _vp, _vp])
 _sig("szp_gb300_sync_status", ctypes.c_int, [_vp])
@@ -132,6 +149,16 @@ _sig("szp_gb300_wait_probe", ctypes.c_int, [ctypes.c_ulonglong, ctypes.POINTER(c
 _libc = ctypes.CDLL(None)
 _libc.free.argtypes = [_vp]
 _libc.free.restype = None
+
+
+def _owned_f64(p, n):
+    """float64 array over n doubles the library malloc'd at p, freed with the array (no copy)."""
+    if n == 0:
+        _libc.free(p)
+        return np.empty(0, np.float64)
+    buf = (ctypes.c_double * n).from_address(p)
+    weakref.finalize(buf, _libc.free, p)
+    return np.frombuffer(buf, dtype=np.float64)
 
 
 def _owned_f32(p, n):
@@ -208,8 +235,9 @@ def max_stream_bytes(n, block_size=32, segments=0, fast_mode=1):
 
 def szp_compress(data, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0, block_size=32,
                  fast_mode=SZP_NONRANDOMACCESS, data_type=SZ_FLOAT):
-    """szp_compress (SZp/include/szp.h:33) on a host float32 array -> bytes."""
-    x = _f32(data)
+    """szp_compress (SZp/include/szp.h:33) on a host array -> bytes: float32
+    (SZ_FLOAT) or float64 (SZ_DOUBLE)."""
+    x = np.ascontiguousarray(data, dtype=np.float64).ravel() if data_type == SZ_DOUBLE else _f32(data)
     size = ctypes.c_size_t(0)
     p = _lib.szp_compress(fast_mode, data_type, x.ctypes.data, ctypes.byref(size), err_bound_mode,
                           abs_err_bound, rel_bound_ratio, x.size, block_size)
@@ -222,14 +250,14 @@ def szp_compress(data, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.
 
 def szp_decompress(stream, n, block_size=32, fast_mode=SZP_NONRANDOMACCESS, data_type=SZ_FLOAT,
                    byte_length=None):
-    """szp_decompress (SZp/include/szp.h:36) -> float32 array of n values."""
+    """szp_decompress (SZp/include/szp.h:36) -> float32 (SZ_FLOAT) or float64
+    (SZ_DOUBLE) array of n values."""
     buf = np.frombuffer(stream, dtype=np.uint8)
     bl = buf.size if byte_length is None else byte_length
     p = _lib.szp_decompress(fast_mode, data_type, buf.ctypes.data, bl, n, block_size)
     if not p:
         _raise("szp_decompress")
-    y = _owned_f32(p, n)
-    return y
+    return _owned_f64(p, n) if data_type == SZ_DOUBLE else _owned_f32(p, n)
 
 
 def szp_float_openmp_threadblock(data, abs_err_bound, block_size=32):
@@ -322,6 +350,28 @@ def compress_dev_async(d_data, n, d_out, capacity, d_size, err_bound_mode=ABS, a
                                            block_size, segments, d_out, capacity, d_size, stream or None)
     if rc != 0:
         raise SzpError(rc, "compress_dev_async failed: %s" % last_error())
+
+
+def max_stream_bytes_f64(n, block_size=32, segments=0, fast_mode=1):
+    return _lib.szp_gb300_max_stream_bytes_f64(n, block_size, segments, fast_mode)
+
+
+def compress_dev_f64(d_data, n, d_out, capacity, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0,
+                     block_size=32, segments=0, fast_mode=1, stream=0):
+    """float64 device-pointer compressor; returns the stream size in bytes."""
+    size = ctypes.c_size_t(0)
+    rc = _lib.szp_gb300_compress_dev_f64(fast_mode, d_data, n, err_bound_mode, abs_err_bound, rel_bound_ratio,
+                                         block_size, segments, d_out, capacity, ctypes.byref(size), stream or None)
+    if rc != 0:
+        raise SzpError(rc, "compress_dev_f64 failed: %s" % last_error())
+    return size.value
+
+
+def decompress_dev_f64(d_stream, length, n, d_out, block_size=32, segments=0, fast_mode=1, stream=0):
+    rc = _lib.szp_gb300_decompress_dev_f64(fast_mode, d_stream, length, n, block_size, segments, d_out,
+                                           stream or None)
+    if rc != 0:
+        raise SzpError(rc, "decompress_dev_f64 failed: %s" % last_error())
 
 
 def decompress_dev(d_stream, length, n, d_out, block_size=32, segments=0, fast_mode=1, stream=0):

@@ -136,6 +136,7 @@ struct DevMisc {
   float eb;
   float pad;
   uint32_t verify[4];  // [0] locate repairs of the last launch
+  double ebd;          // REL bound of float64 data
 };
 constexpr int kRelMaxGrid = 1024;
 
@@ -164,7 +165,7 @@ struct Workspace {
     CU(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
     CU(misc.ensure(sizeof(DevMisc)));
     CU(cudaMemset(misc.p, 0, sizeof(DevMisc)));
-    CU(rel_partial.ensure(2 * sizeof(float) * kRelMaxGrid));
+    CU(rel_partial.ensure(2 * sizeof(double) * kRelMaxGrid));
     CU(cudaMallocHost((void**)&h_small, 64));
     for (int s = 0; s < kNumSlots; s++) {
       for (int i = 0; i < kRing; i++) {
@@ -263,12 +264,13 @@ void tile_counts(const Segments& s, bool fm2, uint32_t tb, uint64_t& per_seg, ui
   if (total == 0) total = 1;
 }
 
-size_t max_stream_bytes(size_t n, int L, int T, int fm) {
+// hb: bytes of the eb header, 4 (float) or 8 (double)
+size_t max_stream_bytes(size_t n, int L, int T, int fm, int hb = 4) {
   if (L <= 0 || T <= 0) return 0;
   Segments s = make_segments(n, T, L);
   bool fm2 = fm == 2;
   uint64_t per = fm2 ? (L == 1 ? 5 : 4 + block_bytes((uint32_t)L - 1, kMaxBitCount)) : max_block_bytes((uint32_t)L);
-  uint64_t total = 4 + 8ull * (uint64_t)T;
+  uint64_t total = (uint64_t)hb + 8ull * (uint64_t)T;
   for (uint32_t t = 0; t < (uint32_t)T; t++) {
     uint64_t len = s.len(t);
     if (!len) continue;
@@ -293,19 +295,23 @@ struct CompressJob {
   uint8_t* d_out;
   size_t cap;
   unsigned long long* d_size;  // optional: size copied here too
+  bool dbl = false;               // float64 data: d_xd and eb_abs_d, 8-byte eb header
+  const double* d_xd = nullptr;
+  double eb_abs_d = 0.0;
 };
 
 int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   if (j.L <= 0) return fail(SZP_GB300_EINVAL, "blockSize must be positive (got %d)", j.L);
   if (j.T <= 0) return fail(SZP_GB300_EINVAL, "segment count must be positive");
   if (j.fm != 1 && j.fm != 2) return fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2 (got %d)", j.fm);
-  if (j.n && !j.d_x) return fail(SZP_GB300_EINVAL, "null input");
-  const uint64_t head = 4 + 8ull * j.T;
+  const bool dbl = j.dbl;
+  if (j.n && !(dbl ? (const void*)j.d_xd : (const void*)j.d_x)) return fail(SZP_GB300_EINVAL, "null input");
+  const uint64_t head = (dbl ? 8 : 4) + 8ull * j.T;
   if (j.cap < head) return fail(SZP_GB300_ECAPACITY, "output buffer smaller than the stream header");
   const bool fm2 = j.fm == 2;
   Segments sg = make_segments(j.n, j.T, j.L);
   uint32_t bpw = 1;
-  uint32_t tb = compress_blocks_per_tile((uint32_t)j.L, bpw);
+  uint32_t tb = dbl ? compress_blocks_per_tile_f64((uint32_t)j.L, bpw) : compress_blocks_per_tile((uint32_t)j.L, bpw);
   uint64_t per_seg, ntiles;
   tile_counts(sg, fm2, tb, per_seg, ntiles);
   if (ntiles >= (1ull << 31) || per_seg >= (1ull << 31))
@@ -333,10 +339,31 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   a.nb_reg = sg.tsz ? seg_blocks_host(sg, 0, fm2) : 0;
   a.nb_last = seg_blocks_host(sg, sg.T - 1, fm2);
   a.thr = table();
+  a.xd = j.d_xd;
+  a.ebd = j.eb_abs_d;
 
   int launches = 0;
-  if (j.eb_mode == REL) {
+  if (j.eb_mode == REL && dbl) {
     RelArgs r;
+    memset(&r, 0, sizeof r);
+    r.xd = j.d_xd;
+    r.n = j.n;
+    r.rel_d = j.rel;
+    r.partial = w.rel_partial.as<float>();  // 2 doubles per CTA
+    r.counter = &dm->rel_counter;
+    r.ebd_out = &dm->ebd;
+    uint64_t want = (j.n / 4 + 255) / 256;
+    uint32_t grid = (uint32_t)(want < 1 ? 1 : want);
+    uint32_t lim = (uint32_t)(w.sm_count * 4 < kRelMaxGrid ? w.sm_count * 4 : kRelMaxGrid);
+    if (grid > lim) grid = lim;
+    w.mark(kSlotRel, 0, st);
+    CU(launch_rel_bound_f64(r, grid, st));
+    w.mark(kSlotRel, 1, st);
+    a.ebd_dev = &dm->ebd;
+    launches++;
+  } else if (j.eb_mode == REL) {
+    RelArgs r;
+    memset(&r, 0, sizeof r);
     r.x = j.d_x;
     r.n = j.n;
     r.rel = (float)j.rel;
@@ -353,10 +380,10 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     a.eb_dev = &dm->eb;
     launches++;
   }
-  size_t smem = compress_smem_bytes((uint32_t)j.L, tb);
+  size_t smem = dbl ? compress_smem_bytes_f64((uint32_t)j.L, tb) : compress_smem_bytes((uint32_t)j.L, tb);
   if (smem > 200 * 1024) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
   w.mark(kSlotCompress, 0, st);
-  CU(launch_compress(a, fm2, st));
+  CU(dbl ? launch_compress_f64(a, fm2, st) : launch_compress(a, fm2, st));
   w.mark(kSlotCompress, 1, st);
   launches++;
   if (j.d_size) CU(cudaMemcpyAsync(j.d_size, &dm->out_size, 8, cudaMemcpyDeviceToDevice, st));
@@ -387,15 +414,18 @@ struct DecompressJob {
   size_t n;
   int L, T, fm;
   float* d_y;
+  bool dbl = false;        // float64 stream: output of doubles in d_yd (8-byte eb header)
+  double* d_yd = nullptr;
 };
 
 int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   if (j.L <= 0) return fail(SZP_GB300_EINVAL, "blockSize must be positive (got %d)", j.L);
   if (j.T <= 0) return fail(SZP_GB300_EINVAL, "segment count must be positive");
   if (j.fm != 1 && j.fm != 2) return fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2 (got %d)", j.fm);
-  const uint64_t head = 4 + 8ull * j.T;
+  const bool dbl = j.dbl;
+  const uint64_t head = (dbl ? 8 : 4) + 8ull * j.T;
   if (j.len < head) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
-  if (j.n && !j.d_y) return fail(SZP_GB300_EINVAL, "null output");
+  if (j.n && !(dbl ? (void*)j.d_yd : (void*)j.d_y)) return fail(SZP_GB300_EINVAL, "null output");
   const bool fm2 = j.fm == 2;
   Segments sg = make_segments(j.n, j.T, j.L);
   const uint32_t maxsz = fm2 ? (j.L == 1 ? 5u : 4 + block_bytes((uint32_t)j.L - 1, kMaxBitCount))
@@ -405,7 +435,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   const uint32_t SC = locate_super_bytes(maxsz);
   const uint64_t nlocate = (j.len + SC - 1) / SC + (uint64_t)j.T + 1;
   uint32_t bpw = 1;
-  uint32_t tb = decode_blocks_per_tile((uint32_t)j.L, bpw);
+  uint32_t tb = dbl ? decode_blocks_per_tile_f64((uint32_t)j.L, bpw) : decode_blocks_per_tile((uint32_t)j.L, bpw);
   uint64_t per_seg, ntiles;
   tile_counts(sg, fm2, tb, per_seg, ntiles);
   uint64_t nblk_total = 0;
@@ -430,6 +460,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   f.len_dev = j.d_len;
   f.seg = sg;
   a.fm2 = fm2;
+  a.hb = dbl ? 8 : 4;
   uint8_t* pb = w.plan.as<uint8_t>();
   f.plan = reinterpret_cast<DecPlan*>(pb);
   f.reg0 = reinterpret_cast<uint64_t*>(pb + 64);
@@ -448,6 +479,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   f.blkpos = w.blkpos.as<uint32_t>();
   f.nblk_total = nblk_total;
   f.y = j.d_y;
+  f.yd = j.d_yd;
   f.ntiles = (uint32_t)ntiles;
   f.tiles_per_seg = (uint32_t)per_seg;
   f.tile_base = 0;
@@ -457,7 +489,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.tb = tb;
   a.bpw = bpw;
   a.nlocate_ctas = (uint32_t)nlocate;
-  if (decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024 ||
+  if ((!dbl && decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) ||
       locate_smem_bytes(SC, a.overlap, maxsz) > 200 * 1024)
     return fail(SZP_GB300_EINVAL, "blockSize too large");
   CU(cudaMemsetAsync(dm->verify, 0, sizeof(uint32_t), st));
@@ -469,7 +501,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   CU(launch_locate(a, st));
   w.mark(kSlotLocate, 1, st);
   w.mark(kSlotDecode, 0, st);
-  CU(launch_decode(a, st));
+  CU(dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
   w.mark(kSlotDecode, 1, st);
   count_launches(3);
   return SZP_GB300_OK;
@@ -477,13 +509,13 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
 
 // Host-side stream length: segment offsets give every segment's start; the
 // last one is walked block by block (the stream does not record its end).
-int host_stream_length(const uint8_t* stream, size_t n, int L, int T, int fm, size_t* len) {
+int host_stream_length(const uint8_t* stream, size_t n, int L, int T, int fm, size_t* len, int hb = 4) {
   if (L <= 0 || T <= 0) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
   Segments s = make_segments(n, T, L);
   const bool fm2 = fm == 2;
-  const uint64_t head = 4 + 8ull * T;
+  const uint64_t head = (uint64_t)hb + 8ull * T;
   uint64_t off = 0;
-  memcpy(&off, stream + 4 + 8ull * (T - 1), 8);
+  memcpy(&off, stream + hb + 8ull * (T - 1), 8);
   const uint8_t* p = stream + head + off;
   uint64_t seglen = s.len(T - 1);
   if (seglen == 0) {
@@ -589,19 +621,28 @@ cudaError_t copy_to_host(void* dst, const void* src, size_t bytes, cudaStream_t 
   return err == cudaSuccess ? cudaStreamSynchronize(st) : err;
 }
 
-int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double rel, int L, int T, int fm,
-                  uint8_t** out_malloc, uint8_t* out_user, size_t user_cap, size_t* out_size) {
+// Host-buffer compressor: float data (dbl false, eb_abs is the float bound)
+// or double data (dbl true, 8-byte eb header, szp_double.cc).
+int compress_host(const void* data, bool dbl, size_t n, int eb_mode, double eb_abs, double rel, int L, int T,
+                  int fm, uint8_t** out_malloc, uint8_t* out_user, size_t user_cap, size_t* out_size) {
   Workspace* w;
   int rc = get_ws(&w);
   if (rc) return rc;
   cudaStream_t st = w->begin_own();
   if (n && !data) return fail(SZP_GB300_EINVAL, "null input");
-  const size_t cap = max_stream_bytes(n, L, T, fm);
+  const size_t elem = dbl ? sizeof(double) : sizeof(float);
+  const size_t cap = max_stream_bytes(n, L, T, fm, (int)elem);
   if (!cap) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
-  CU(w->in.ensure(n * sizeof(float) + 16));
+  CU(w->in.ensure(n * elem + 16));
   CU(w->stream.ensure(cap));
-  if (n) CU(cudaMemcpyAsync(w->in.p, data, n * sizeof(float), cudaMemcpyHostToDevice, st));
-  CompressJob j{w->in.as<float>(), n, eb_mode, eb_abs, rel, L, T, fm, w->stream.as<uint8_t>(), cap, nullptr};
+  if (n) CU(cudaMemcpyAsync(w->in.p, data, n * elem, cudaMemcpyHostToDevice, st));
+  CompressJob j{dbl ? nullptr : w->in.as<float>(), n, eb_mode, (float)eb_abs, rel, L, T, fm,
+                w->stream.as<uint8_t>(), cap, nullptr};
+  if (dbl) {
+    j.dbl = true;
+    j.d_xd = w->in.as<double>();
+    j.eb_abs_d = eb_abs;
+  }
   rc = compress_launch(*w, j, st);
   if (rc) return rc;
   // a malloc'd result is allocated while the GPU works, and as many of its
@@ -609,7 +650,7 @@ int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double
   // stream's size is known only at the end)
   uint8_t* dst = out_user;
   if (!dst) {
-    const size_t alloc = std::max(cap, 4 + 4 * n);  // the reference hands out 4+4n bytes
+    const size_t alloc = std::max(cap, elem + elem * n);  // the reference hands out sizeof(T) * (1 + n)
     dst = (uint8_t*)malloc(alloc);
     if (!dst) {
       finish_sync(*w, st, nullptr);
@@ -639,48 +680,63 @@ int compress_host(const float* data, size_t n, int eb_mode, float eb_abs, double
   return SZP_GB300_OK;
 }
 
-// stream: whole stream (eb first) when eb_override is NaN; otherwise the
-// bytes after eb (the per-type entries) and eb is eb_override.
+// stream: whole stream (eb first) unless after_eb; then the bytes after eb
+// (the per-type entries) and eb is eb_value.  dbl: a float64 stream (8-byte
+// eb header, double output).
 int decompress_host(const uint8_t* bytes, size_t len, bool len_known, size_t n, int L, int T, int fm,
-                    bool after_eb, float eb_value, float** out_malloc, float* out_user) {
+                    bool after_eb, double eb_value, void** out_malloc, void* out_user, bool dbl = false) {
   Workspace* w;
   int rc = get_ws(&w);
   if (rc) return rc;
   if (!bytes) return fail(SZP_GB300_EINVAL, "null stream");
   if (L <= 0 || T <= 0) return fail(SZP_GB300_EINVAL, "bad blockSize/segments");
-  const uint64_t head = 4 + 8ull * T;
+  const int hb = dbl ? 8 : 4;
+  const size_t elem = dbl ? sizeof(double) : sizeof(float);
+  const uint64_t head = (uint64_t)hb + 8ull * T;
   // stream as seen from its eb header
-  const uint8_t* full = after_eb ? bytes - 4 : bytes;
+  const uint8_t* full = after_eb ? bytes - hb : bytes;
   size_t total = len;
   if (!len_known || total < head) {
-    // host_stream_length never reads the 4 eb bytes, so `full` may point
+    // host_stream_length never reads the eb bytes, so `full` may point
     // before the caller's buffer when only the bytes after eb were given
-    rc = host_stream_length(full, n, L, T, fm, &total);
+    rc = host_stream_length(full, n, L, T, fm, &total, hb);
     if (rc) return rc;
   } else {
-    size_t bound = max_stream_bytes(n, L, T, fm);
+    size_t bound = max_stream_bytes(n, L, T, fm, hb);
     if (total > bound) total = bound;
   }
   cudaStream_t st = w->begin_own();
   CU(w->stream.ensure(total + 16));
-  CU(w->out.ensure(n * sizeof(float) + 16));
+  CU(w->out.ensure(n * elem + 16));
   uint8_t* d_stream = w->stream.as<uint8_t>();
   if (after_eb) {
-    uint32_t b;
-    memcpy(&b, &eb_value, 4);
-    uint8_t be[4] = {(uint8_t)(b >> 24), (uint8_t)(b >> 16), (uint8_t)(b >> 8), (uint8_t)b};
-    memcpy(w->h_small + 16, be, 4);
-    CU(cudaMemcpyAsync(d_stream, w->h_small + 16, 4, cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_stream + 4, bytes, total - 4, cudaMemcpyHostToDevice, st));
+    uint8_t be[8];
+    if (dbl) {
+      uint64_t b;
+      memcpy(&b, &eb_value, 8);
+      for (int i = 0; i < 8; i++) be[i] = (uint8_t)(b >> (56 - 8 * i));
+    } else {
+      const float f = (float)eb_value;
+      uint32_t b;
+      memcpy(&b, &f, 4);
+      for (int i = 0; i < 4; i++) be[i] = (uint8_t)(b >> (24 - 8 * i));
+    }
+    memcpy(w->h_small + 16, be, hb);
+    CU(cudaMemcpyAsync(d_stream, w->h_small + 16, hb, cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_stream + hb, bytes, total - hb, cudaMemcpyHostToDevice, st));
   } else {
     CU(cudaMemcpyAsync(d_stream, bytes, total, cudaMemcpyHostToDevice, st));
   }
-  DecompressJob j{d_stream, total, nullptr, n, L, T, fm, w->out.as<float>()};
+  DecompressJob j{d_stream, total, nullptr, n, L, T, fm, dbl ? nullptr : w->out.as<float>()};
+  if (dbl) {
+    j.dbl = true;
+    j.d_yd = w->out.as<double>();
+  }
   rc = decompress_launch(*w, j, st);
   if (rc) return rc;
-  float* dst = out_user;
+  void* dst = out_user;
   if (!dst) {
-    dst = (float*)malloc(n ? n * sizeof(float) : 1);
+    dst = malloc(n ? n * elem : 1);
     if (!dst) {
       finish_sync(*w, st, nullptr);
       w->end(st);
@@ -691,7 +747,7 @@ int decompress_host(const uint8_t* bytes, size_t len, bool len_known, size_t n, 
   // and the first copies run); the status decides whether they are returned
   DevMisc* dm = w->dm();
   CU(cudaMemcpyAsync(w->h_small + 8, &dm->err, 4, cudaMemcpyDeviceToHost, st));
-  cudaError_t e = copy_to_host(dst, w->out.p, n * sizeof(float), st);
+  cudaError_t e = copy_to_host(dst, w->out.p, n * elem, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   w->end(st);
   if (e != cudaSuccess) {
@@ -744,46 +800,9 @@ void host_count_launches(int k) { count_launches(k); }
 }  // namespace szp
 
 // =============================================================== C ABI ====
-extern "C" {
-
-unsigned char* szp_compress(int fastMode, int dataType, void* data, size_t* outSize, int errBoundMode,
-                            double absErrBound, double relBoundRatio, size_t nbEle, int blockSize) {
-  clear_error();
-  if (outSize) *outSize = 0;
-  if (fastMode != SZP_NONRANDOMACCESS && fastMode != SZP_RANDOMACCESS) {
-    fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2");
-    return nullptr;
-  }
-  if (dataType != SZ_FLOAT) {
-    fail(SZP_GB300_EINVAL, "only SZ_FLOAT data is provided");
-    return nullptr;
-  }
-  if (!outSize) {
-    fail(SZP_GB300_EINVAL, "null outSize");
-    return nullptr;
-  }
-  uint8_t* out = nullptr;
-  int T = resolve_segments(0);
-  int rc = compress_host((const float*)data, nbEle, errBoundMode == REL ? REL : ABS, (float)absErrBound,
-                         relBoundRatio, blockSize, T, fastMode, &out, nullptr, 0, outSize);
-  return rc ? nullptr : out;
-}
-
-void* szp_decompress(int fastMode, int dataType, unsigned char* bytes, size_t byteLength, size_t nbEle,
-                     int blockSize) {
-  clear_error();
-  if (dataType != SZ_FLOAT) {
-    fail(SZP_GB300_EINVAL, "only SZ_FLOAT data is provided");
-    return nullptr;
-  }
-  int fm = fastMode == SZP_NONRANDOMACCESS ? 1 : 2;  // the reference treats any other mode as 2
-  int T = resolve_segments(0);
-  float* y = nullptr;
-  int rc = decompress_host(bytes, byteLength, true, nbEle, blockSize, T, fm, false, 0.0f, &y, nullptr);
-  return rc ? nullptr : y;
-}
-
-static unsigned char* fm_compress_alloc(float* x, size_t* outSize, float eb, size_t n, int L, int T, int fm) {
+// Per-type entry points (float or double), shared by the C ABI below.
+template <typename V>
+static unsigned char* fm_compress_alloc(V* x, size_t* outSize, V eb, size_t n, int L, int T, int fm) {
   clear_error();
   if (outSize) *outSize = 0;
   if (!outSize) {
@@ -791,12 +810,13 @@ static unsigned char* fm_compress_alloc(float* x, size_t* outSize, float eb, siz
     return nullptr;
   }
   uint8_t* out = nullptr;
-  int rc = compress_host(x, n, ABS, eb, 0.0, L, T, fm, &out, nullptr, 0, outSize);
+  int rc = compress_host(x, sizeof(V) == 8, n, ABS, (double)eb, 0.0, L, T, fm, &out, nullptr, 0, outSize);
   return rc ? nullptr : out;
 }
 
-static void fm_compress_arg(unsigned char* output, float* x, size_t* outSize, float eb, size_t n, int L, int T,
-                            int fm) {
+// The reference's callers size `output` as sizeof(V) * (1 + n) bytes (szp.cc:53).
+template <typename V>
+static void fm_compress_arg(unsigned char* output, V* x, size_t* outSize, V eb, size_t n, int L, int T, int fm) {
   clear_error();
   if (!outSize) {
     fail(SZP_GB300_EINVAL, "null outSize");
@@ -808,9 +828,66 @@ static void fm_compress_arg(unsigned char* output, float* x, size_t* outSize, fl
     return;
   }
   size_t sz = 0;
-  int rc = compress_host(x, n, ABS, eb, 0.0, L, T, fm, nullptr, output, 4 + 4 * n, &sz);
+  int rc = compress_host(x, sizeof(V) == 8, n, ABS, (double)eb, 0.0, L, T, fm, nullptr, output,
+                         sizeof(V) + sizeof(V) * n, &sz);
   if (!rc) *outSize = sz;
 }
+
+template <typename V>
+static V* fm_decompress_alloc(size_t n, V eb, int L, unsigned char* cmp, int T, int fm) {
+  clear_error();
+  void* y = nullptr;
+  int rc = decompress_host(cmp, 0, false, n, L, T, fm, true, (double)eb, &y, nullptr, sizeof(V) == 8);
+  return rc ? nullptr : static_cast<V*>(y);
+}
+
+template <typename V>
+static void fm_decompress_arg(V* out, size_t n, V eb, int L, unsigned char* cmp, int T, int fm) {
+  clear_error();
+  if (!out && n) {
+    fail(SZP_GB300_EINVAL, "null output");
+    return;
+  }
+  decompress_host(cmp, 0, false, n, L, T, fm, true, (double)eb, nullptr, out, sizeof(V) == 8);
+}
+
+extern "C" {
+
+unsigned char* szp_compress(int fastMode, int dataType, void* data, size_t* outSize, int errBoundMode,
+                            double absErrBound, double relBoundRatio, size_t nbEle, int blockSize) {
+  clear_error();
+  if (outSize) *outSize = 0;
+  if (fastMode != SZP_NONRANDOMACCESS && fastMode != SZP_RANDOMACCESS) {
+    fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2");
+    return nullptr;
+  }
+  if (!outSize) {
+    fail(SZP_GB300_EINVAL, "null outSize");
+    return nullptr;
+  }
+  uint8_t* out = nullptr;
+  int T = resolve_segments(0);
+  // any dataType but SZ_FLOAT is double data (szp.cc:71); the float bound is
+  // (float)absErrBound (szp.cc:31), the double one absErrBound itself (szp.cc:74)
+  const bool dbl = dataType != SZ_FLOAT;
+  int rc = compress_host(data, dbl, nbEle, errBoundMode == REL ? REL : ABS,
+                         dbl ? absErrBound : (double)(float)absErrBound, relBoundRatio, blockSize, T, fastMode,
+                         &out, nullptr, 0, outSize);
+  return rc ? nullptr : out;
+}
+
+void* szp_decompress(int fastMode, int dataType, unsigned char* bytes, size_t byteLength, size_t nbEle,
+                     int blockSize) {
+  clear_error();
+  int fm = fastMode == SZP_NONRANDOMACCESS ? 1 : 2;  // the reference treats any other mode as 2
+  int T = resolve_segments(0);
+  void* y = nullptr;
+  int rc = decompress_host(bytes, byteLength, true, nbEle, blockSize, T, fm, false, 0.0, &y, nullptr,
+                           dataType != SZ_FLOAT);
+  return rc ? nullptr : y;
+}
+
+
 
 unsigned char* szp_float_openmp_threadblock(float* oriData, size_t* outSize, float absErrBound, size_t nbEle,
                                             int blockSize) {
@@ -843,21 +920,39 @@ void szp_float_openmp_threadblock_randomaccess_arg(unsigned char* output, float*
   fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 2);
 }
 
-static float* fm_decompress_alloc(size_t n, float eb, int L, unsigned char* cmp, int T, int fm) {
-  clear_error();
-  float* y = nullptr;
-  int rc = decompress_host(cmp, 0, false, n, L, T, fm, true, eb, &y, nullptr);
-  return rc ? nullptr : y;
+// float64 compressors, SZp/include/szp_double.h (szp_double.cc:149-1090)
+unsigned char* szp_double_openmp_threadblock(double* oriData, size_t* outSize, double absErrBound, size_t nbEle,
+                                             int blockSize) {
+  return fm_compress_alloc(oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 1);
 }
 
-static void fm_decompress_arg(float* out, size_t n, float eb, int L, unsigned char* cmp, int T, int fm) {
-  clear_error();
-  if (!out && n) {
-    fail(SZP_GB300_EINVAL, "null output");
-    return;
-  }
-  decompress_host(cmp, 0, false, n, L, T, fm, true, eb, nullptr, out);
+void szp_double_openmp_threadblock_arg(unsigned char* output, double* oriData, size_t* outSize,
+                                       double absErrBound, size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 1);
 }
+
+void szp_double_single_thread_arg(unsigned char* output, double* oriData, size_t* outSize, double absErrBound,
+                                  size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, 1, 1);
+}
+
+size_t szp_double_single_thread_arg_record(unsigned char* output, double* oriData, size_t* outSize,
+                                           double absErrBound, size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, 1, 1);
+  return outSize && *outSize ? 8 * nbEle + *outSize : 0;
+}
+
+unsigned char* szp_double_openmp_threadblock_randomaccess(double* oriData, size_t* outSize, double absErrBound,
+                                                          size_t nbEle, int blockSize) {
+  return fm_compress_alloc(oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 2);
+}
+
+void szp_double_openmp_threadblock_randomaccess_arg(unsigned char* output, double* oriData, size_t* outSize,
+                                                    double absErrBound, size_t nbEle, int blockSize) {
+  fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, resolve_segments(0), 2);
+}
+
+
 
 float* szp_float_decompress_openmp_threadblock(size_t nbEle, float absErrBound, int blockSize,
                                                unsigned char* cmpBytes) {
@@ -890,6 +985,42 @@ float* szp_float_decompress_openmp_threadblock_randomaccess(size_t nbEle, float 
 
 void szp_float_decompress_openmp_threadblock_randomaccess_arg(float* newData, size_t nbEle, float absErrBound,
                                                               int blockSize, unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 2);
+}
+
+// float64 decompressors, SZp/include/szpd_double.h (szpd_double.cc:23-645);
+// cmpBytes points after the 8-byte eb
+double* szp_double_decompress_openmp_threadblock(size_t nbEle, double absErrBound, int blockSize,
+                                                 unsigned char* cmpBytes) {
+  return fm_decompress_alloc(nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 1);
+}
+
+void szp_double_decompress_openmp_threadblock_arg(double* newData, size_t nbEle, double absErrBound,
+                                                  int blockSize, unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 1);
+}
+
+void szp_double_decompress_single_thread_arg(double* newData, size_t nbEle, double absErrBound, int blockSize,
+                                             unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, 1, 1);
+}
+
+size_t szp_double_decompress_single_thread_arg_record(double* newData, size_t nbEle, double absErrBound,
+                                                      int blockSize, unsigned char* cmpBytes) {
+  fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, 1, 1);
+  if (t_status) return 0;
+  size_t len = 0;
+  if (host_stream_length(cmpBytes - 8, nbEle, blockSize, 1, 1, &len, 8)) return 0;
+  return len + 8 * nbEle;
+}
+
+double* szp_double_decompress_openmp_threadblock_randomaccess(size_t nbEle, double absErrBound, int blockSize,
+                                                              unsigned char* cmpBytes) {
+  return fm_decompress_alloc(nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 2);
+}
+
+void szp_double_decompress_openmp_threadblock_randomaccess_arg(double* newData, size_t nbEle, double absErrBound,
+                                                               int blockSize, unsigned char* cmpBytes) {
   fm_decompress_arg(newData, nbEle, absErrBound, blockSize, cmpBytes, resolve_segments(0), 2);
 }
 
@@ -943,6 +1074,54 @@ int szp_gb300_compress_dev(int fastMode, const float* d_data, size_t nbEle, int 
   rc = finish_sync(*w, st, &sz);
   w->end(st);
   if (outSize) *outSize = sz;
+  return rc;
+}
+
+size_t szp_gb300_max_stream_bytes_f64(size_t nbEle, int blockSize, int segments, int fastMode) {
+  return max_stream_bytes(nbEle, blockSize, resolve_segments(segments), fastMode == 2 ? 2 : 1, 8);
+}
+
+int szp_gb300_compress_dev_f64(int fastMode, const double* d_data, size_t nbEle, int errBoundMode,
+                               double absErrBound, double relBoundRatio, int blockSize, int segments,
+                               unsigned char* d_out, size_t out_capacity, size_t* outSize, void* stream) {
+  clear_error();
+  if (outSize) *outSize = 0;
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_out) return fail(SZP_GB300_EINVAL, "null output");
+  if (nbEle && !d_data) return fail(SZP_GB300_EINVAL, "null input");
+  cudaStream_t st = w->begin(stream);
+  CompressJob j{nullptr, nbEle, errBoundMode == REL ? REL : ABS, 0.0f, relBoundRatio, blockSize,
+                resolve_segments(segments), fastMode, d_out, out_capacity, nullptr};
+  j.dbl = true;
+  j.d_xd = d_data;
+  j.eb_abs_d = absErrBound;
+  rc = compress_launch(*w, j, st);
+  if (rc == SZP_GB300_OK) {
+    size_t sz = 0;
+    rc = finish_sync(*w, st, &sz);
+    if (outSize) *outSize = sz;
+  }
+  w->end(st);
+  return rc;
+}
+
+int szp_gb300_decompress_dev_f64(int fastMode, const unsigned char* d_bytes, size_t byteLength, size_t nbEle,
+                                 int blockSize, int segments, double* d_out, void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_bytes) return fail(SZP_GB300_EINVAL, "null stream");
+  if (nbEle && !d_out) return fail(SZP_GB300_EINVAL, "null output");
+  cudaStream_t st = w->begin(stream);
+  DecompressJob j{d_bytes, byteLength, nullptr, nbEle, blockSize, resolve_segments(segments), fastMode, nullptr};
+  j.dbl = true;
+  j.d_yd = d_out;
+  rc = decompress_launch(*w, j, st);
+  if (rc == SZP_GB300_OK) rc = finish_sync(*w, st, nullptr);
+  w->end(st);
   return rc;
 }
 

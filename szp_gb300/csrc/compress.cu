@@ -96,8 +96,20 @@ __device__ __forceinline__ void write_header_common(uint8_t* out, float eb, cons
   }
 }
 
-__device__ __forceinline__ void write_offset(uint8_t* out, uint32_t t, uint64_t off) {
-  uint8_t* p = out + 4 + 8ull * t;
+// eb as a big-endian double (szp_double.cc:164, szp_CompressionToolkit.h:539-546)
+// and the zero offsets of empty segments after it; float64 streams.
+__device__ __forceinline__ void write_header_common(uint8_t* out, double eb, const Segments& sg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(eb);
+  for (int i = threadIdx.x; i < 8; i += blockDim.x) out[i] = (uint8_t)(b >> (56 - 8 * i));
+  if (sg.tsz == 0) {
+    uint32_t nz = 8 * (sg.n == 0 ? sg.T : sg.T - 1);
+    for (uint32_t i = threadIdx.x; i < nz; i += blockDim.x) out[8 + i] = 0;
+  }
+}
+
+// Offset of segment t, after an eb header of hb bytes (4 float, 8 double).
+__device__ __forceinline__ void write_offset(uint8_t* out, uint32_t t, uint64_t off, uint32_t hb = 4) {
+  uint8_t* p = out + hb + 8ull * t;
   for (int i = 0; i < 8; i++) p[i] = (uint8_t)(off >> (8 * i));
 }
 
@@ -762,8 +774,12 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
 // 32*B bytes, 32*r bits = 4r bytes), so each piece packs like a 32-block.
 // fastmode2 (FM2) gives every block its own seed and L-1 deltas.
 // ---------------------------------------------------------------------------
-template <int WARPS, bool FM2>
+// V = float, or double for float64 data (szp_double.cc: 8-byte eb header,
+// q = (int)(x * (1/eb)) with a double product).
+template <int WARPS, bool FM2, typename V = float>
 __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
+  constexpr bool DBL = std::is_same<V, double>::value;
+  constexpr uint32_t HB = DBL ? 8 : 4;  // eb header bytes
   extern __shared__ __align__(16) uint8_t s_out[];
   __shared__ uint32_t s_tk[2];
   __shared__ uint32_t s_w[WARPS + 1];
@@ -775,13 +791,24 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
 
   const Segments sg = a.seg;
   const uint32_t L = sg.L;
+  uint32_t flags = 0;
   const uint32_t TB = WARPS * a.bpw;
-  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
-  const float inv = __fdiv_rn(1.0f, eb);
+  const V* __restrict__ xs = DBL ? reinterpret_cast<const V*>(a.xd) : reinterpret_cast<const V*>(a.x);
+  V eb, inv;
+  if constexpr (DBL) {
+    eb = a.ebd_dev ? *a.ebd_dev : a.ebd;
+    inv = __ddiv_rn(1.0, eb);  // 1/eb in double, szp_double.cc:180
+  } else {
+    eb = a.eb_dev ? *a.eb_dev : a.eb;
+    inv = __fdiv_rn(1.0f, eb);
+  }
+  auto qz = [&](V v) -> int32_t {
+    if constexpr (DBL) return quantize_d(v, inv, flags);
+    else return quantize(v, inv, flags);
+  };
   const TileInfo ti = tile_info(sg, tile, a.tiles_per_seg, TB, FM2);
   if (tile == 0) write_header_common(a.out, eb, sg);
   const uint64_t lo = sg.lo(ti.seg), hi = sg.hi(ti.seg);
-  uint32_t flags = 0;
 
   // block b of the segment: fastmode1 elements [lo+1+bL, ...), previous
   // element lo+bL; fastmode2 seed at lo+bL and deltas after it.
@@ -805,11 +832,11 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint64_t s = block_start(b);
     uint32_t m = block_len(b);
     uint32_t mx = 0;
-    int32_t prev = quantize(__ldg(a.x + s - 1), inv, flags);
+    int32_t prev = qz(__ldg(xs + s - 1));
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       bool valid = j < m;
-      int32_t q = valid ? quantize(__ldg(a.x + s + j), inv, flags) : 0;
+      int32_t q = valid ? qz(__ldg(xs + s + j)) : 0;
       int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
       if (lane == 0) qp = prev;
       prev = __shfl_sync(0xffffffffu, q, 31);
@@ -839,10 +866,10 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   }
   __syncthreads();
   const uint64_t base = s_base;
-  const uint64_t head = 4 + 8ull * sg.T;
+  const uint64_t head = HB + 8ull * sg.T;
   const uint64_t gpos = head + base;
   if (tile == a.ntiles - 1 && threadIdx.x == 0) *a.out_size = gpos + agg;
-  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, base);
+  if (ti.has_seg && ti.first && threadIdx.x == 0 && gpos + agg <= a.cap) write_offset(a.out, ti.seg, base, HB);
   if (gpos + agg > a.cap) {
     if (threadIdx.x == 0) atomicOr(a.err, kErrCapacity);
     return;
@@ -851,7 +878,7 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   const uint32_t align = (uint32_t)(((uintptr_t)a.out + gpos) & 15);
   uint8_t* s_tile = s_out + align;
   if (seed && warp == 0) {
-    int32_t sq = quantize(__ldg(a.x + lo), inv, flags);
+    int32_t sq = qz(__ldg(xs + lo));
     if (lane < 4) s_tile[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
   }
 
@@ -865,18 +892,18 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint32_t m = block_len(b);
     uint8_t* dst = s_tile + off;
     if (FM2) {
-      int32_t sq = quantize(__ldg(a.x + s - 1), inv, flags);
+      int32_t sq = qz(__ldg(xs + s - 1));
       if (lane < 4) dst[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
       dst += 4;
     }
     // recompute max (cheap, L1-resident) to know the bit count
     uint32_t mx = 0;
     {
-      int32_t prev = quantize(__ldg(a.x + s - 1), inv, flags);
+      int32_t prev = qz(__ldg(xs + s - 1));
       for (uint32_t p0 = 0; p0 < m; p0 += 32) {
         uint32_t j = p0 + lane;
         bool valid = j < m;
-        int32_t q = valid ? quantize(__ldg(a.x + s + j), inv, flags) : 0;
+        int32_t q = valid ? qz(__ldg(xs + s + j)) : 0;
         int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
         if (lane == 0) qp = prev;
         prev = __shfl_sync(0xffffffffu, q, 31);
@@ -895,12 +922,12 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint8_t* sgnp = dst + 1;
     uint8_t* bytp = sgnp + ns;
     uint8_t* remp = bytp + B * m;
-    int32_t prev = quantize(__ldg(a.x + s - 1), inv, flags);
+    int32_t prev = qz(__ldg(xs + s - 1));
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       bool valid = j < m;
       uint32_t pm = m - p0 < 32 ? m - p0 : 32;  // elements in this piece
-      int32_t q = valid ? quantize(__ldg(a.x + s + j), inv, flags) : 0;
+      int32_t q = valid ? qz(__ldg(xs + s + j)) : 0;
       int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
       if (lane == 0) qp = prev;
       prev = __shfl_sync(0xffffffffu, q, 31);
@@ -1042,6 +1069,99 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
     range = x86_nan_fix(__fsub_rn(mx, mn), mx, mn);
   }
   *a.eb_out = x86_nan_fix(__fmul_rn(range, a.rel), range, a.rel);
+}
+
+// REL bound of float64 data: min/max over x and eb = range * rel in double
+// (szp.cc:77-89), with the rules of rel_bound_kernel (NaNs skipped unless x[0]
+// is NaN; max == min gives range x - x).  Two loads of 16 bytes in flight per
+// thread; the last CTA reduces the per-CTA partials (2 doubles each).
+__global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
+  __shared__ double s_mn[8], s_mx[8];
+  __shared__ bool s_last;
+  double mn = INFINITY, mx = -INFINITY;
+  const double* x = a.xd;
+  const uint64_t n = a.n;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t headn = min(n, (uint64_t)((((uintptr_t)x & 15) >> 3)));  // one double to 16-byte alignment
+  for (uint64_t i = tid; i < headn; i += stride) {
+    mn = fmin(mn, x[i]);
+    mx = fmax(mx, x[i]);
+  }
+  const double2* x2 = reinterpret_cast<const double2*>(x + headn);
+  const uint64_t n2 = (n - headn) >> 1;
+  uint64_t i = tid;
+  for (; i + stride < n2; i += 2 * stride) {
+    const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + stride);
+    mn = fmin(mn, fmin(fmin(v0.x, v0.y), fmin(v1.x, v1.y)));
+    mx = fmax(mx, fmax(fmax(v0.x, v0.y), fmax(v1.x, v1.y)));
+  }
+  for (; i < n2; i += stride) {
+    const double2 v = __ldg(x2 + i);
+    mn = fmin(mn, fmin(v.x, v.y));
+    mx = fmax(mx, fmax(v.x, v.y));
+  }
+  for (uint64_t j = headn + 2 * n2 + tid; j < n; j += stride) {
+    mn = fmin(mn, x[j]);
+    mx = fmax(mx, x[j]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_mn[warp] = mn;
+    s_mx[warp] = mx;
+  }
+  __syncthreads();
+  double* part = reinterpret_cast<double*>(a.partial);
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      mn = fmin(mn, s_mn[w]);
+      mx = fmax(mx, s_mx[w]);
+    }
+    part[2 * blockIdx.x] = mn;
+    part[2 * blockIdx.x + 1] = mx;
+    __threadfence();
+    s_last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  mn = INFINITY;
+  mx = -INFINITY;
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    mn = fmin(mn, ((volatile double*)part)[2 * b]);
+    mx = fmax(mx, ((volatile double*)part)[2 * b + 1]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  __syncthreads();
+  if (lane == 0) {
+    s_mn[warp] = mn;
+    s_mx[warp] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+    mn = fmin(mn, s_mn[w]);
+    mx = fmax(mx, s_mx[w]);
+  }
+  *a.counter = 0;  // ready for the next launch
+  double range;
+  if (n == 0) {
+    range = 0.0;
+  } else if (isnan(x[0])) {
+    range = __longlong_as_double(__double_as_longlong(x[0]) | 0x0008000000000000ll);
+  } else if (mx == mn && isfinite(mx)) {
+    range = 0.0;
+  } else {
+    range = x86_nan_fix_d(__dsub_rn(mx, mn), mx, mn);
+  }
+  *a.ebd_out = x86_nan_fix_d(__dmul_rn(range, a.rel_d), range, a.rel_d);
 }
 
 // ---------------------------------------------------------------------------
@@ -1292,6 +1412,36 @@ cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds,
     case 4: return launch_lanes<4, true, 4>(a, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_rel_bound_f64(const RelArgs& a, uint32_t grid, cudaStream_t st) {
+  rel_bound_kernel_f64<<<grid, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+// float64 data: the one-warp-per-block kernel for every blockSize, tiles kept
+// near 16 KB of stream like the float kernel's.
+uint32_t compress_blocks_per_tile_f64(uint32_t L, uint32_t& bpw) {
+  const uint32_t mb = max_block_bytes(L) + 4;
+  const uint32_t b = (16384u / kGenWarps) / mb;
+  bpw = b < 1 ? 1 : (b > 8 ? 8 : b);
+  return kGenWarps * bpw;
+}
+
+size_t compress_smem_bytes_f64(uint32_t L, uint32_t tb) { return 16 + 8 + (size_t)tb * (max_block_bytes(L) + 4) + 32; }
+
+cudaError_t launch_compress_f64(const CompressArgs& a, bool fm2, cudaStream_t st) {
+  const size_t smem = compress_smem_bytes_f64(a.seg.L, a.tb);
+  if (fm2) {
+    auto k = compress_generic<kGenWarps, true, double>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
+  } else {
+    auto k = compress_generic<kGenWarps, false, double>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<a.ntiles, kGenWarps * 32, smem, st>>>(a);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st) {

@@ -32,6 +32,8 @@
 //                 the other blockSizes.
 #include <atomic>
 
+#include <type_traits>
+
 #include "szp_device.cuh"
 #include "szp_kernels.h"
 #include "szp_pipe.cuh"
@@ -86,7 +88,8 @@ __global__ void dec_setup_kernel(const __grid_constant__ DecArgs a) {
   const DecField& fd = BATCH ? a.fields[blockIdx.x] : a.f;
   const Segments sg = fd.seg;
   const uint32_t T = sg.T;
-  const uint64_t head = 4 + 8ull * T;
+  const uint32_t hb = a.hb == 8 ? 8u : 4u;  // eb header: float, or double (szpd_double.cc)
+  const uint64_t head = hb + 8ull * T;
   __shared__ uint32_t s_bad;
   uint64_t len = fd.len;
   if (fd.len_dev) {
@@ -98,8 +101,13 @@ __global__ void dec_setup_kernel(const __grid_constant__ DecArgs a) {
     if (!s_bad) {
       uint32_t b = ((uint32_t)fd.in[0] << 24) | ((uint32_t)fd.in[1] << 16) | ((uint32_t)fd.in[2] << 8) | fd.in[3];
       fd.plan->eb = __uint_as_float(b);
+      unsigned long long d = 0;
+      if (hb == 8)
+        for (int i = 0; i < 8; i++) d = (d << 8) | fd.in[i];
+      fd.plan->ebd = __longlong_as_double((long long)d);
     } else {
       fd.plan->eb = 0.0f;
+      fd.plan->ebd = 0.0;
     }
   }
   __syncthreads();
@@ -110,7 +118,7 @@ __global__ void dec_setup_kernel(const __grid_constant__ DecArgs a) {
     uint32_t nch = 0;
     bool bad = false;
     if (len_t > 0 && hdr_ok) {
-      uint64_t off = load_u64le(fd.in + 4 + 8ull * t);
+      uint64_t off = load_u64le(fd.in + hb + 8ull * t);
       uint64_t body = len - head;
       uint64_t end;
       if (off > body) {
@@ -118,7 +126,7 @@ __global__ void dec_setup_kernel(const __grid_constant__ DecArgs a) {
       } else {
         uint64_t start = head + off;
         if (t + 1 < T) {
-          uint64_t off2 = load_u64le(fd.in + 4 + 8ull * (t + 1));
+          uint64_t off2 = load_u64le(fd.in + hb + 8ull * (t + 1));
           if (off2 < off || off2 > body) bad = true;
           end = head + off2;
         } else {
@@ -591,6 +599,13 @@ __device__ __forceinline__ float dequant(uint32_t q, float eb, bool special = fa
   return special ? x86_nan_fix(r, f, eb) : r;
 }
 
+// (double)q * eb for float64 streams (szpd_double.cc:67,86,112).
+__device__ __forceinline__ double dequant(uint32_t q, double eb, bool special = false) {
+  const double f = (double)(int32_t)q;
+  const double r = __dmul_rn(f, eb);
+  return special ? x86_nan_fix_d(r, f, eb) : r;
+}
+
 template <int WARPS>
 __device__ __forceinline__ uint32_t scan_warps_u32(uint32_t* s_w, uint32_t mine, int warp, int lane,
                                                    uint32_t& excl) {
@@ -955,7 +970,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       seedv[r] = 0;
       if (FM2 && mblk) {
         // fastmode2: the block's 4-byte seed, then its header (a one-element
-        // block has no header on the decode side, szpd_float.cc:481)
+        // block has no header on the decode side, szpd_float.cc:483)
         const uint32_t b0 = bpos[bt] - span0;
         if (b0 + 4 > spanlen) {
           corrupt = true;
@@ -1152,8 +1167,10 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
 
 // Any blockSize, fastmode1 or fastmode2: one warp per block in 32-element
 // pieces.  fastmode1 decodes twice (totals, then values after the look-back).
-template <int WARPS, bool FM2>
+// V = float, or double for float64 streams (x' = (double)q * eb).
+template <int WARPS, bool FM2, typename V = float>
 __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_constant__ DecArgs a) {
+  constexpr bool DBL = std::is_same<V, double>::value;
   const DecField& fd = a.f;
   __shared__ uint32_t s_tk[2];
   __shared__ uint32_t s_w[WARPS + 1];
@@ -1167,8 +1184,11 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
   const uint32_t TB = WARPS * a.bpw;
   const DecTile dt = dec_tile(sg, tile, fd.tiles_per_seg, TB, FM2);
   if (!dt.any) return;
-  const float eb = fd.plan->eb;
+  V eb;
+  if constexpr (DBL) eb = fd.plan->ebd;
+  else eb = fd.plan->eb;
   const bool ebsp = !isfinite(eb);
+  V* __restrict__ yv = DBL ? reinterpret_cast<V*>(fd.yd) : reinterpret_cast<V*>(fd.y);
   const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
   const uint64_t R0 = fd.reg0[dt.seg], R1 = fd.reg1[dt.seg];
   const uint8_t* __restrict__ in = fd.in;
@@ -1187,7 +1207,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
   // block header pointer and validation; returns bc or 255 when corrupt
   auto blk_hdr = [&](uint64_t b, uint32_t m, uint64_t& hp) -> uint32_t {
     hp = R0 + __ldg(fd.blkpos + gb + b) + (FM2 ? 4 : 0);
-    if (FM2 && m == 0) return 0;  // one-element block: no header is read (szpd_float.cc:481)
+    if (FM2 && m == 0) return 0;  // one-element block: no header is read (szpd_float.cc:483)
     if (hp >= R1) return 255u;
     uint32_t bc = __ldg(in + hp);
     if (bc > 33 || hp + block_bytes(m, bc) > R1) return 255u;
@@ -1225,7 +1245,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
         excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
         if (lane == 0) {
           st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
-          fd.y[lo] = dequant(excl, eb, ebsp);
+          yv[lo] = dequant(excl, eb, ebsp);
         }
       } else {
         if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
@@ -1250,16 +1270,25 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
       bc = 0;
     }
     if (FM2) {
-      const uint8_t* sp = in + hp - 4;
-      q0 = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
-           ((uint32_t)__ldg(sp + 3) << 24);
-      if (lane == 0) fd.y[s - 1] = dequant(q0, eb, ebsp);
+      // blockSize 1: the reference's decoder reads no header byte for a
+      // one-value block and so steps 4 bytes per block where its encoder
+      // wrote 5 (szpd_float.cc:483, szpd_double.cc:487); results follow it
+      const uint64_t so = L == 1 ? R0 + 4 * b : hp - 4;
+      if (so + 4 > R1) {
+        corrupt = true;
+        q0 = 0;
+      } else {
+        const uint8_t* sp = in + so;
+        q0 = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
+             ((uint32_t)__ldg(sp + 3) << 24);
+      }
+      if (lane == 0) yv[s - 1] = dequant(q0, eb, ebsp);
     }
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       uint32_t d = (bc && j < m) ? decode_delta(in + hp, m, bc, j) : 0u;
       uint32_t sc = warp_incl_scan(d, lane);
-      if (j < m) fd.y[s + j] = dequant(q0 + sc, eb, ebsp);
+      if (j < m) yv[s + j] = dequant(q0 + sc, eb, ebsp);
       q0 += __shfl_sync(0xffffffffu, sc, 31);
     }
   }
@@ -1358,6 +1387,21 @@ static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
   const uint32_t grid = a.ntiles < cap ? a.ntiles : cap;
   if (grid == 0) return cudaSuccess;
   k<<<grid, kDecPipeThreads, smem, st>>>(a, slot);
+  return cudaGetLastError();
+}
+
+uint32_t decode_blocks_per_tile_f64(uint32_t L, uint32_t& bpw) {
+  const uint32_t b = 2048u / (L < 32 ? 32u : L);
+  bpw = b < 1 ? 1 : (b > 8 ? 8 : b);
+  return kDecWarps * bpw;
+}
+
+cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st) {
+  if (a.fm2) {
+    decode_generic<kDecWarps, true, double><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
+  } else {
+    decode_generic<kDecWarps, false, double><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -57,6 +57,16 @@ __device__ __forceinline__ int32_t quantize(float x, float inv, uint32_t& flags)
   return quantize_slow(x, inv, flags);
 }
 
+// q = (int)(x * inv) for float64 data (szp_double.cc:209,228): the double
+// product rounds to nearest, the conversion truncates; out of range and NaN
+// give INT32_MIN like x86's cvttsd2si, and raise kErrQuantRange.
+__device__ __forceinline__ int32_t quantize_d(double x, double inv, uint32_t& flags) {
+  const double p = __dmul_rn(x, inv);
+  if (p > -2147483649.0 && p < 2147483648.0) return __double2int_rz(p);
+  flags |= kErrQuantRange;
+  return INT32_MIN;
+}
+
 // NaN results follow x86 SSE, where the reference's fixtures come from: a NaN
 // operand propagates (quieted), an invalid operation (0*inf, inf-inf) gives
 // the default NaN 0xFFC00000.  The GPU would return 0x7FFFFFFF.
@@ -64,6 +74,14 @@ __device__ __forceinline__ float x86_nan_fix(float r, float a, float b) {
   if (r == r) return r;
   uint32_t u = (a != a) ? __float_as_uint(a) : ((b != b) ? __float_as_uint(b) : 0xFFC00000u);
   return __uint_as_float(u | 0x00400000u);
+}
+// The same rule for double results (default NaN 0xFFF8000000000000).
+__device__ __forceinline__ double x86_nan_fix_d(double r, double a, double b) {
+  if (r == r) return r;
+  const unsigned long long u = (a != a) ? (unsigned long long)__double_as_longlong(a)
+                                        : ((b != b) ? (unsigned long long)__double_as_longlong(b)
+                                                    : 0xFFF8000000000000ull);
+  return __longlong_as_double((long long)(u | 0x0008000000000000ull));
 }
 
 // Byte size of an encoded block of m elements (1 <= m) with bit count bc.

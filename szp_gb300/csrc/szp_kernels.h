@@ -47,6 +47,11 @@ struct CompressArgs {
   // batched launches: tiles of all fields, field of each tile
   const CompressField* fields;
   const uint32_t* tile_field;
+  // float64 data (compress_generic<.., double>): input, bound and where a REL
+  // range pass left it; the stream's eb header is then 8 bytes
+  const double* xd;
+  double ebd;
+  const double* ebd_dev;
 };
 
 // Per-field state of the batched range pass: order-preserving encodings of
@@ -70,9 +75,13 @@ struct RelArgs {
   const float* x;
   uint64_t n;
   float rel;        // (float)relBoundRatio
-  float* partial;   // 2 floats per CTA
+  float* partial;   // 2 floats per CTA (2 doubles for float64 data)
   uint32_t* counter;
   float* eb_out;
+  // float64 data: (max - min) * rel in double (szp.cc:77-89)
+  const double* xd;
+  double rel_d;
+  double* ebd_out;
 };
 
 // Decompression plan, filled on the device from the stream header.
@@ -81,6 +90,7 @@ struct DecPlan {
   uint32_t nchunks;      // total chunks over all segments
   uint32_t bad;          // header failed validation
   uint32_t pad;
+  double ebd;            // float64 streams: the 8-byte eb
   // followed in memory by: uint32 chunk_base[T+1]; uint64 reg0[T]; uint64 reg1[T]
 };
 
@@ -97,6 +107,7 @@ struct DecField {
   uint32_t* blkpos;         // per block: header offset relative to its segment's region start
   uint64_t nblk_total;
   float* y;                 // output
+  double* yd;               // output of a float64 stream (decode_generic<.., double>)
   uint32_t ntiles;          // decode tiles of this field
   uint32_t tiles_per_seg;
   uint32_t tile_base;       // its first decode tile in the launch
@@ -108,6 +119,7 @@ struct DecField {
 struct DecArgs {
   DecField f;            // the field of a single-field launch
   bool fm2;
+  uint32_t hb;           // bytes of the stream's eb header: 4 (float) or 8 (double)
   uint32_t chunk;        // bytes per locate thread
   uint32_t super_chunk;  // bytes per locate CTA (chunk * threads)
   uint32_t overlap;      // bytes walked before a CTA's region to find the header chain
@@ -130,6 +142,11 @@ struct DecArgs {
 uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw);
 size_t compress_smem_bytes(uint32_t L, uint32_t tb);
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st);
+// float64 data: every blockSize on the one-warp-per-block kernels
+uint32_t compress_blocks_per_tile_f64(uint32_t L, uint32_t& bpw);
+size_t compress_smem_bytes_f64(uint32_t L, uint32_t tb);
+cudaError_t launch_compress_f64(const CompressArgs& a, bool fm2, cudaStream_t st);
+cudaError_t launch_rel_bound_f64(const RelArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds, cudaStream_t st);
 cudaError_t prepare_compress_batch();
@@ -149,6 +166,8 @@ size_t decode_smem_bytes(uint32_t L, uint32_t tb, bool fm2);
 cudaError_t launch_dec_setup(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_locate(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st);
+uint32_t decode_blocks_per_tile_f64(uint32_t L, uint32_t& bpw);
+cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st);
 // batched decompression (fastmode1, blockSize 32)
 cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStream_t st);
 cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st);

@@ -249,7 +249,9 @@ def test_bad_arguments(szp):
     with pytest.raises(szp.SzpError):
         szp.szp_compress(x, szp.ABS, 1e-3, 0.0, 32, 3)
     with pytest.raises(szp.SzpError):
-        szp.szp_compress(x, szp.ABS, 1e-3, 0.0, 32, 1, data_type=szp.SZ_DOUBLE)
+        szp.szp_compress(x, szp.ABS, 1e-3, 0.0, 0, 1, data_type=szp.SZ_DOUBLE)
+    with pytest.raises(szp.SzpError):  # segment offsets past the stream's end
+        szp.szp_decompress(b"\xff" * 400, 10, 32, 1, data_type=szp.SZ_DOUBLE)
 
 
 @pytest.mark.parametrize("overlap", [0, 3, 40])
