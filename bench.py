@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-fm2", action="store_true")
+    ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-window", type=float, default=0.2, help="seconds of arrivals per rate")
     ap.add_argument("--batched-fields", type=int, default=1024)
@@ -606,6 +607,37 @@ def main():
                "kernels_ms": {k: round(v, 4) for k, v in avg.items()}}
         del d_s2
 
+    # float64 data (szp_double_*): 2^26 doubles (512 MiB) of the field, REL 1e-6
+    f64 = None
+    if not args.no_f64:
+        nd = min(n, 1 << 26)
+        xd = x[:nd].double()
+        capd = szp.max_stream_bytes_f64(nd, L, T, 1)
+        d_sd = torch.empty(capd, dtype=torch.uint8, device=dev)
+        yd = torch.empty_like(xd)
+        szp.set_timing(True)
+        for i in range(4):
+            szd = szp.compress_dev_f64(xd.data_ptr(), nd, d_sd.data_ptr(), capd, szp.REL, 0.0, 1e-6, L, T, 1, st)
+            szp.decompress_dev_f64(d_sd.data_ptr(), szd, nd, yd.data_ptr(), L, T, 1, st)
+            if i == 0:
+                torch.cuda.synchronize()
+                for slot in range(5):
+                    szp.kernel_time(slot)  # drop the first round trip
+        torch.cuda.synchronize()
+        kt = {name: szp.kernel_time(slot) for slot, name in
+              enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
+        szp.set_timing(False)
+        avg = {k: v[0] / v[1] for k, v in kt.items() if v[1]}
+        ebd = 1e-6 * float(xd.max() - xd.min())
+        errd = float((xd - yd).abs().max())
+        assert errd <= ebd * (1 + 1e-9), "float64 round trip exceeds the bound"
+        f64 = {"n": nd, "rel": 1e-6, "ratio": round(8.0 * nd / szd, 3),
+               "compress_gbs": round(8.0 * nd / ((avg["rel_range"] + avg["compress"]) / 1e3) / 1e9, 2),
+               "decompress_gbs": round(8.0 * nd / ((avg["dec_setup"] + avg["locate"] + avg["decode"]) / 1e3) / 1e9,
+                                       2),
+               "kernels_ms": {k: round(v, 4) for k, v in avg.items()}}
+        del xd, yd, d_sd
+
     batched = None
     if not args.no_batched:
         batched = batched_workload(szp, torch, dev, T, args.batched_fields)
@@ -644,6 +676,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "fastmode2": fm2,
+            "float64": f64,
             "batched": batched,
             "serving": serving,
             "gpu_launches": int(launches),

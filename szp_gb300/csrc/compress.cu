@@ -822,9 +822,21 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   };
   const uint32_t per_blk_extra = FM2 ? 4u : 0u;  // fastmode2 seed
 
-  // pass 1: bit counts and sizes
+  // pass 1: bit counts and sizes.  With blockSize <= 32 (one piece per block)
+  // every lane keeps its block's value before, its own value and the bit
+  // count in registers (at most KC blocks per warp), so pass 2 quantizes
+  // nothing again (FP64 products are expensive on this GPU).
+  constexpr int KC = 8;
+  const bool cache = L <= 32 && a.bpw <= (uint32_t)KC;
+  int32_t cprev[KC], cq[KC];
+  uint32_t cbc[KC];
   uint32_t wbytes = 0;
   const uint32_t wfirst = warp * a.bpw;
+#pragma unroll
+  for (int k = 0; k < KC; k++) {
+    cprev[k] = cq[k] = 0;
+    cbc[k] = 0;
+  }
   for (uint32_t k = 0; k < a.bpw; k++) {
     uint32_t bi = wfirst + k;
     if (bi >= ti.nblk) break;
@@ -833,10 +845,12 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint32_t m = block_len(b);
     uint32_t mx = 0;
     int32_t prev = qz(__ldg(xs + s - 1));
+    const int32_t prev0 = prev;
+    int32_t q = 0;
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       bool valid = j < m;
-      int32_t q = valid ? qz(__ldg(xs + s + j)) : 0;
+      q = valid ? qz(__ldg(xs + s + j)) : 0;
       int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
       if (lane == 0) qp = prev;
       prev = __shfl_sync(0xffffffffu, q, 31);
@@ -846,6 +860,15 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     }
     uint32_t bc = bitcount_from_table(mx, a.thr.thr);
     wbytes += per_blk_extra + (m ? block_bytes(m, bc) : 1u);
+    if (cache) {
+#pragma unroll
+      for (int c = 0; c < KC; c++)
+        if ((uint32_t)c == k) {
+          cprev[c] = prev0;
+          cq[c] = q;
+          cbc[c] = bc;
+        }
+    }
   }
   if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
 
@@ -891,14 +914,25 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint64_t s = block_start(b);
     uint32_t m = block_len(b);
     uint8_t* dst = s_tile + off;
+    int32_t kprev = 0, kq = 0;
+    uint32_t kbc = 0;
+    if (cache) {
+#pragma unroll
+      for (int c = 0; c < KC; c++)
+        if ((uint32_t)c == k) {
+          kprev = cprev[c];
+          kq = cq[c];
+          kbc = cbc[c];
+        }
+    }
     if (FM2) {
-      int32_t sq = qz(__ldg(xs + s - 1));
+      int32_t sq = cache ? kprev : qz(__ldg(xs + s - 1));
       if (lane < 4) dst[lane] = (uint8_t)((uint32_t)sq >> (8 * lane));
       dst += 4;
     }
-    // recompute max (cheap, L1-resident) to know the bit count
+    // without the cache: recompute the max (L1-resident) to know the bit count
     uint32_t mx = 0;
-    {
+    if (!cache) {
       int32_t prev = qz(__ldg(xs + s - 1));
       for (uint32_t p0 = 0; p0 < m; p0 += 32) {
         uint32_t j = p0 + lane;
@@ -912,7 +946,7 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
         mx = max(mx, __reduce_max_sync(0xffffffffu, v));
       }
     }
-    const uint32_t bc = bitcount_from_table(mx, a.thr.thr);
+    const uint32_t bc = cache ? kbc : bitcount_from_table(mx, a.thr.thr);
     if (lane == 0) dst[0] = (uint8_t)bc;
     if (m == 0 || bc == 0) {
       off += per_blk_extra + 1;
@@ -922,12 +956,12 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint8_t* sgnp = dst + 1;
     uint8_t* bytp = sgnp + ns;
     uint8_t* remp = bytp + B * m;
-    int32_t prev = qz(__ldg(xs + s - 1));
+    int32_t prev = cache ? kprev : qz(__ldg(xs + s - 1));
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       bool valid = j < m;
       uint32_t pm = m - p0 < 32 ? m - p0 : 32;  // elements in this piece
-      int32_t q = valid ? qz(__ldg(xs + s + j)) : 0;
+      int32_t q = cache ? kq : (valid ? qz(__ldg(xs + s + j)) : 0);
       int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
       if (lane == 0) qp = prev;
       prev = __shfl_sync(0xffffffffu, q, 31);
@@ -1071,43 +1105,57 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
   *a.eb_out = x86_nan_fix(__fmul_rn(range, a.rel), range, a.rel);
 }
 
+// Order-preserving key of a double (larger value, larger key); NaNs get key
+// 0, below every number's (the reduction uses 0 as "nothing seen" too).
+__device__ __forceinline__ uint64_t f64_key(double v) {
+  const uint64_t u = (uint64_t)__double_as_longlong(v);
+  if ((u & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return 0;  // NaN: skipped, as the reference's compares do
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double f64_unkey(uint64_t k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
 // REL bound of float64 data: min/max over x and eb = range * rel in double
 // (szp.cc:77-89), with the rules of rel_bound_kernel (NaNs skipped unless x[0]
-// is NaN; max == min gives range x - x).  Two loads of 16 bytes in flight per
-// thread; the last CTA reduces the per-CTA partials (2 doubles each).
+// is NaN; max == min gives range x - x).  The min/max run on integer keys
+// (FP64 min/max would take the GPU's narrow FP64 pipe); the last CTA reduces
+// the per-CTA partials (2 keys each) and does the FP64 arithmetic once.
 __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
-  __shared__ double s_mn[8], s_mx[8];
+  __shared__ uint64_t s_mn[8], s_mx[8];
   __shared__ bool s_last;
-  double mn = INFINITY, mx = -INFINITY;
+  uint64_t mn = ~0ull, mx = 0;  // keys; 0 also stands for "none" (NaN keys never count)
   const double* x = a.xd;
   const uint64_t n = a.n;
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  auto take = [&](double v) {
+    const uint64_t k = f64_key(v);
+    if (k) {
+      mn = min(mn, k);
+      mx = max(mx, k);
+    }
+  };
   const uint64_t headn = min(n, (uint64_t)((((uintptr_t)x & 15) >> 3)));  // one double to 16-byte alignment
-  for (uint64_t i = tid; i < headn; i += stride) {
-    mn = fmin(mn, x[i]);
-    mx = fmax(mx, x[i]);
-  }
+  for (uint64_t i = tid; i < headn; i += stride) take(x[i]);
   const double2* x2 = reinterpret_cast<const double2*>(x + headn);
   const uint64_t n2 = (n - headn) >> 1;
   uint64_t i = tid;
-  for (; i + stride < n2; i += 2 * stride) {
+  for (; i + 3 * stride < n2; i += 4 * stride) {
     const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + stride);
-    mn = fmin(mn, fmin(fmin(v0.x, v0.y), fmin(v1.x, v1.y)));
-    mx = fmax(mx, fmax(fmax(v0.x, v0.y), fmax(v1.x, v1.y)));
+    const double2 v2 = __ldg(x2 + i + 2 * stride), v3 = __ldg(x2 + i + 3 * stride);
+    take(v0.x); take(v0.y); take(v1.x); take(v1.y);
+    take(v2.x); take(v2.y); take(v3.x); take(v3.y);
   }
   for (; i < n2; i += stride) {
     const double2 v = __ldg(x2 + i);
-    mn = fmin(mn, fmin(v.x, v.y));
-    mx = fmax(mx, fmax(v.x, v.y));
+    take(v.x);
+    take(v.y);
   }
-  for (uint64_t j = headn + 2 * n2 + tid; j < n; j += stride) {
-    mn = fmin(mn, x[j]);
-    mx = fmax(mx, x[j]);
-  }
+  for (uint64_t j = headn + 2 * n2 + tid; j < n; j += stride) take(x[j]);
   for (int o = 16; o > 0; o >>= 1) {
-    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mn = min(mn, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mn, o));
+    mx = max(mx, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mx, o));
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
@@ -1115,11 +1163,11 @@ __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
     s_mx[warp] = mx;
   }
   __syncthreads();
-  double* part = reinterpret_cast<double*>(a.partial);
+  uint64_t* part = reinterpret_cast<uint64_t*>(a.partial);
   if (threadIdx.x == 0) {
     for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-      mn = fmin(mn, s_mn[w]);
-      mx = fmax(mx, s_mx[w]);
+      mn = min(mn, s_mn[w]);
+      mx = max(mx, s_mx[w]);
     }
     part[2 * blockIdx.x] = mn;
     part[2 * blockIdx.x + 1] = mx;
@@ -1129,15 +1177,15 @@ __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  mn = INFINITY;
-  mx = -INFINITY;
+  mn = ~0ull;
+  mx = 0;
   for (uint32_t b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-    mn = fmin(mn, ((volatile double*)part)[2 * b]);
-    mx = fmax(mx, ((volatile double*)part)[2 * b + 1]);
+    mn = min(mn, ((volatile uint64_t*)part)[2 * b]);
+    mx = max(mx, ((volatile uint64_t*)part)[2 * b + 1]);
   }
   for (int o = 16; o > 0; o >>= 1) {
-    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mn = min(mn, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mn, o));
+    mx = max(mx, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mx, o));
   }
   __syncthreads();
   if (lane == 0) {
@@ -1147,8 +1195,8 @@ __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
   __syncthreads();
   if (threadIdx.x != 0) return;
   for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-    mn = fmin(mn, s_mn[w]);
-    mx = fmax(mx, s_mx[w]);
+    mn = min(mn, s_mn[w]);
+    mx = max(mx, s_mx[w]);
   }
   *a.counter = 0;  // ready for the next launch
   double range;
@@ -1156,10 +1204,9 @@ __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
     range = 0.0;
   } else if (isnan(x[0])) {
     range = __longlong_as_double(__double_as_longlong(x[0]) | 0x0008000000000000ll);
-  } else if (mx == mn && isfinite(mx)) {
-    range = 0.0;
   } else {
-    range = x86_nan_fix_d(__dsub_rn(mx, mn), mx, mn);
+    const double fmn = f64_unkey(mn), fmx = f64_unkey(mx);  // x[0] is a number, so both were seen
+    range = (fmx == fmn && isfinite(fmx)) ? 0.0 : x86_nan_fix_d(__dsub_rn(fmx, fmn), fmx, fmn);
   }
   *a.ebd_out = x86_nan_fix_d(__dmul_rn(range, a.rel_d), range, a.rel_d);
 }

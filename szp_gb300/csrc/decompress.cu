@@ -1214,6 +1214,14 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
     return bc;
   };
 
+  // fastmode1 decodes every delta twice (the warp's total, then the values
+  // once its base is known); with blockSize <= 32 (one piece per block) each
+  // lane keeps its deltas of up to KC blocks in registers instead
+  constexpr int KC = 8;
+  const bool cache = !FM2 && L <= 32 && a.bpw <= (uint32_t)KC;
+  uint32_t cd[KC];
+#pragma unroll
+  for (int c = 0; c < KC; c++) cd[c] = 0;
   uint32_t q0 = 0;
   if (!FM2) {
     uint32_t wtot = 0;
@@ -1231,6 +1239,11 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
       for (uint32_t p0 = 0; p0 < m; p0 += 32) {
         uint32_t j = p0 + lane;
         uint32_t d = j < m ? decode_delta(in + hp, m, bc, j) : 0u;
+        if (cache) {
+#pragma unroll
+          for (int c = 0; c < KC; c++)
+            if ((uint32_t)c == k) cd[c] = d;
+        }
         for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         wtot += d;
       }
@@ -1284,9 +1297,15 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
       }
       if (lane == 0) yv[s - 1] = dequant(q0, eb, ebsp);
     }
+    uint32_t dk = 0;
+    if (cache) {
+#pragma unroll
+      for (int c = 0; c < KC; c++)
+        if ((uint32_t)c == k) dk = cd[c];
+    }
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
-      uint32_t d = (bc && j < m) ? decode_delta(in + hp, m, bc, j) : 0u;
+      uint32_t d = cache ? dk : ((bc && j < m) ? decode_delta(in + hp, m, bc, j) : 0u);
       uint32_t sc = warp_incl_scan(d, lane);
       if (j < m) yv[s + j] = dequant(q0 + sc, eb, ebsp);
       q0 += __shfl_sync(0xffffffffu, sc, 31);
