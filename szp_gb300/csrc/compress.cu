@@ -18,6 +18,7 @@
 #include <type_traits>
 
 #include "szp_device.cuh"
+#include "szp_f64.h"
 #include "szp_kernels.h"
 #include "szp_pipe.cuh"
 #include "szp_tma.cuh"
@@ -802,9 +803,17 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     eb = a.eb_dev ? *a.eb_dev : a.eb;
     inv = __fdiv_rn(1.0f, eb);
   }
+  f64i::Operand invo{};  // 1/eb's fields for the integer float64 quantizer
+  if constexpr (DBL) invo = f64i::unpack(f64i::bits_of(inv));
   auto qz = [&](V v) -> int32_t {
-    if constexpr (DBL) return quantize_d(v, inv, flags);
-    else return quantize(v, inv, flags);
+    if constexpr (DBL) {
+      bool bad = false;
+      const int32_t q = f64i::quantize(f64i::bits_of(v), invo, bad);
+      if (bad) flags |= kErrQuantRange;
+      return q;
+    } else {
+      return quantize(v, inv, flags);
+    }
   };
   const TileInfo ti = tile_info(sg, tile, a.tiles_per_seg, TB, FM2);
   if (tile == 0) write_header_common(a.out, eb, sg);
@@ -823,21 +832,53 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   const uint32_t per_blk_extra = FM2 ? 4u : 0u;  // fastmode2 seed
 
   // pass 1: bit counts and sizes.  With blockSize <= 32 (one piece per block)
-  // every lane keeps its block's value before, its own value and the bit
-  // count in registers (at most KC blocks per warp), so pass 2 quantizes
-  // nothing again (FP64 products are expensive on this GPU).
+  // and at most KC blocks per warp, the warp loads all its values at once,
+  // lane c quantizes the value before block c (its seed in fastmode2), and
+  // every lane keeps its quantized value and the blocks' bit counts in
+  // registers, so pass 2 loads and quantizes nothing again.
   constexpr int KC = 8;
   const bool cache = L <= 32 && a.bpw <= (uint32_t)KC;
-  int32_t cprev[KC], cq[KC];
+  int32_t cq[KC];
   uint32_t cbc[KC];
+  int32_t pq = 0;  // lane c: the quantized value before block c
   uint32_t wbytes = 0;
   const uint32_t wfirst = warp * a.bpw;
 #pragma unroll
   for (int k = 0; k < KC; k++) {
-    cprev[k] = cq[k] = 0;
+    cq[k] = 0;
     cbc[k] = 0;
   }
-  for (uint32_t k = 0; k < a.bpw; k++) {
+  if (cache) {
+    V xv[KC];
+    V xp = V(0);
+#pragma unroll
+    for (int c = 0; c < KC; c++) {
+      xv[c] = V(0);
+      const uint32_t bi = wfirst + c;
+      if ((uint32_t)c < a.bpw && bi < ti.nblk && (uint32_t)lane < block_len(ti.blk0 + bi))
+        xv[c] = __ldg(xs + block_start(ti.blk0 + bi) + lane);
+    }
+    if ((uint32_t)lane < a.bpw && wfirst + lane < ti.nblk) xp = __ldg(xs + block_start(ti.blk0 + wfirst + lane) - 1);
+    pq = qz(xp);
+#pragma unroll
+    for (int c = 0; c < KC; c++) {
+      const uint32_t bi = wfirst + c;
+      if ((uint32_t)c >= a.bpw || bi >= ti.nblk) break;
+      const uint32_t m = block_len(ti.blk0 + bi);
+      const bool valid = (uint32_t)lane < m;
+      const int32_t q = valid ? qz(xv[c]) : 0;
+      int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
+      const int32_t p0 = __shfl_sync(0xffffffffu, pq, c);
+      if (lane == 0) qp = p0;
+      const uint32_t d = (uint32_t)q - (uint32_t)qp;
+      const uint32_t v = valid ? (((int32_t)d < 0) ? 0u - d : d) : 0u;
+      const uint32_t bc = bitcount_from_table(__reduce_max_sync(0xffffffffu, v), a.thr.thr);
+      wbytes += per_blk_extra + (m ? block_bytes(m, bc) : 1u);
+      cq[c] = q;
+      cbc[c] = bc;
+    }
+  }
+  for (uint32_t k = 0; !cache && k < a.bpw; k++) {
     uint32_t bi = wfirst + k;
     if (bi >= ti.nblk) break;
     uint64_t b = ti.blk0 + bi;
@@ -845,12 +886,10 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint32_t m = block_len(b);
     uint32_t mx = 0;
     int32_t prev = qz(__ldg(xs + s - 1));
-    const int32_t prev0 = prev;
-    int32_t q = 0;
     for (uint32_t p0 = 0; p0 < m; p0 += 32) {
       uint32_t j = p0 + lane;
       bool valid = j < m;
-      q = valid ? qz(__ldg(xs + s + j)) : 0;
+      int32_t q = valid ? qz(__ldg(xs + s + j)) : 0;
       int32_t qp = __shfl_up_sync(0xffffffffu, q, 1);
       if (lane == 0) qp = prev;
       prev = __shfl_sync(0xffffffffu, q, 31);
@@ -860,15 +899,6 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     }
     uint32_t bc = bitcount_from_table(mx, a.thr.thr);
     wbytes += per_blk_extra + (m ? block_bytes(m, bc) : 1u);
-    if (cache) {
-#pragma unroll
-      for (int c = 0; c < KC; c++)
-        if ((uint32_t)c == k) {
-          cprev[c] = prev0;
-          cq[c] = q;
-          cbc[c] = bc;
-        }
-    }
   }
   if (__any_sync(0xffffffffu, flags != 0) && lane == 0) atomicOr(a.err, kErrQuantRange);
 
@@ -914,13 +944,13 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     uint64_t s = block_start(b);
     uint32_t m = block_len(b);
     uint8_t* dst = s_tile + off;
-    int32_t kprev = 0, kq = 0;
+    int32_t kq = 0;
     uint32_t kbc = 0;
+    const int32_t kprev = __shfl_sync(0xffffffffu, pq, k & 31);
     if (cache) {
 #pragma unroll
       for (int c = 0; c < KC; c++)
         if ((uint32_t)c == k) {
-          kprev = cprev[c];
           kq = cq[c];
           kbc = cbc[c];
         }

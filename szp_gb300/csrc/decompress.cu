@@ -35,6 +35,7 @@
 #include <type_traits>
 
 #include "szp_device.cuh"
+#include "szp_f64.h"
 #include "szp_kernels.h"
 #include "szp_pipe.cuh"
 #include "szp_tma.cuh"
@@ -1188,6 +1189,24 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
   if constexpr (DBL) eb = fd.plan->ebd;
   else eb = fd.plan->eb;
   const bool ebsp = !isfinite(eb);
+  // float64: (double)q * eb in integer arithmetic for every eb whose
+  // products stay normal (FP64 instructions are slow on this GPU)
+  bool fastdq = false;
+  uint64_t ebm = 0, ebs = 0;
+  uint32_t ebe = 0;
+  if constexpr (DBL) {
+    const uint64_t u = f64i::bits_of(eb);
+    fastdq = f64i::dequant_fast_ok(u);
+    ebm = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    ebe = (uint32_t)(u >> 52) & 0x7FFu;
+    ebs = u & 0x8000000000000000ull;
+  }
+  auto dq = [&](uint32_t q) -> V {
+    if constexpr (DBL) {
+      if (fastdq) return f64i::double_of(f64i::dequant_bits((int32_t)q, ebm, ebe, ebs));
+    }
+    return dequant(q, eb, ebsp);
+  };
   V* __restrict__ yv = DBL ? reinterpret_cast<V*>(fd.yd) : reinterpret_cast<V*>(fd.y);
   const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
   const uint64_t R0 = fd.reg0[dt.seg], R1 = fd.reg1[dt.seg];
@@ -1215,8 +1234,10 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
   };
 
   // fastmode1 decodes every delta twice (the warp's total, then the values
-  // once its base is known); with blockSize <= 32 (one piece per block) each
-  // lane keeps its deltas of up to KC blocks in registers instead
+  // once its base is known); with blockSize <= 32 (one piece per block) and
+  // at most KC blocks per warp, lane c fetches block c's position and header
+  // byte, the deltas of all the warp's blocks are decoded with their loads
+  // in flight together, and each lane keeps its deltas in registers
   constexpr int KC = 8;
   const bool cache = !FM2 && L <= 32 && a.bpw <= (uint32_t)KC;
   uint32_t cd[KC];
@@ -1225,7 +1246,30 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
   uint32_t q0 = 0;
   if (!FM2) {
     uint32_t wtot = 0;
-    for (uint32_t k = 0; k < a.bpw; k++) {
+    if (cache) {
+      uint64_t hpl = 0;
+      uint32_t bcl = 0, ml = 0;
+      if ((uint32_t)lane < a.bpw && wfirst + lane < dt.nblk) {
+        ml = blk_len(dt.blk0 + wfirst + lane);
+        bcl = blk_hdr(dt.blk0 + wfirst + lane, ml, hpl);
+        if (bcl == 255u) {
+          corrupt = true;
+          bcl = 0;
+        }
+      }
+      uint32_t lsum = 0;
+#pragma unroll
+      for (int c = 0; c < KC; c++) {
+        if ((uint32_t)c >= a.bpw || wfirst + c >= dt.nblk) break;
+        const uint32_t bc = __shfl_sync(0xffffffffu, bcl, c), m = __shfl_sync(0xffffffffu, ml, c);
+        const uint64_t hp = __shfl_sync(0xffffffffu, (unsigned long long)hpl, c);
+        cd[c] = (bc && (uint32_t)lane < m) ? decode_delta(in + hp, m, bc, lane) : 0u;
+        lsum += cd[c];
+      }
+      for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+      wtot = lsum;
+    }
+    for (uint32_t k = 0; !cache && k < a.bpw; k++) {
       uint32_t bi = wfirst + k;
       if (bi >= dt.nblk) break;
       uint64_t b = dt.blk0 + bi, hp;
@@ -1239,11 +1283,6 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
       for (uint32_t p0 = 0; p0 < m; p0 += 32) {
         uint32_t j = p0 + lane;
         uint32_t d = j < m ? decode_delta(in + hp, m, bc, j) : 0u;
-        if (cache) {
-#pragma unroll
-          for (int c = 0; c < KC; c++)
-            if ((uint32_t)c == k) cd[c] = d;
-        }
         for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         wtot += d;
       }
@@ -1258,7 +1297,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
         excl = (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
         if (lane == 0) {
           st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, (uint32_t)(excl + agg)));
-          yv[lo] = dequant(excl, eb, ebsp);
+          yv[lo] = dq(excl);
         }
       } else {
         if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagAggregate, agg));
@@ -1277,7 +1316,8 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
     uint64_t b = dt.blk0 + bi, hp;
     uint64_t s = blk_start(b);
     uint32_t m = blk_len(b);
-    uint32_t bc = blk_hdr(b, m, hp);
+    hp = 0;
+    uint32_t bc = cache ? 0u : blk_hdr(b, m, hp);  // the cache holds the deltas
     if (bc == 255u) {
       corrupt = true;
       bc = 0;
@@ -1295,7 +1335,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
         q0 = (uint32_t)__ldg(sp) | ((uint32_t)__ldg(sp + 1) << 8) | ((uint32_t)__ldg(sp + 2) << 16) |
              ((uint32_t)__ldg(sp + 3) << 24);
       }
-      if (lane == 0) yv[s - 1] = dequant(q0, eb, ebsp);
+      if (lane == 0) yv[s - 1] = dq(q0);
     }
     uint32_t dk = 0;
     if (cache) {
@@ -1307,7 +1347,7 @@ __global__ void __launch_bounds__(WARPS * 32) decode_generic(const __grid_consta
       uint32_t j = p0 + lane;
       uint32_t d = cache ? dk : ((bc && j < m) ? decode_delta(in + hp, m, bc, j) : 0u);
       uint32_t sc = warp_incl_scan(d, lane);
-      if (j < m) yv[s + j] = dequant(q0 + sc, eb, ebsp);
+      if (j < m) yv[s + j] = dq(q0 + sc);
       q0 += __shfl_sync(0xffffffffu, sc, 31);
     }
   }
