@@ -137,6 +137,7 @@ struct DevMisc {
   float pad;
   uint32_t verify[4];  // [0] locate repairs of the last launch
   double ebd;          // REL bound of float64 data
+  double invd;         // and its inverse
 };
 constexpr int kRelMaxGrid = 1024;
 
@@ -148,6 +149,7 @@ struct Workspace {
   cudaStream_t last = nullptr;
   cudaEvent_t done = nullptr;
   DevBuf misc, rel_partial, status, in, stream, out, plan, walks, blkpos;
+  DevBuf qbuf;  // int32 q of float64 data between a pipeline and its pass
   uint8_t* h_small = nullptr;  // pinned: out_size (8) + err (4)
   size_t last_stream = 0;      // size of this thread's last host-API stream
   // ring of event pairs per kernel slot: every launch is timed when timing
@@ -305,13 +307,19 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   if (j.T <= 0) return fail(SZP_GB300_EINVAL, "segment count must be positive");
   if (j.fm != 1 && j.fm != 2) return fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2 (got %d)", j.fm);
   const bool dbl = j.dbl;
-  if (j.n && !(dbl ? (const void*)j.d_xd : (const void*)j.d_x)) return fail(SZP_GB300_EINVAL, "null input");
+  const void* xin = dbl ? (const void*)j.d_xd : (const void*)j.d_x;
+  if (j.n && !xin) return fail(SZP_GB300_EINVAL, "null input");
+  if ((uintptr_t)xin & (dbl ? 7 : 3)) return fail(SZP_GB300_EINVAL, "input not aligned to its element size");
   const uint64_t head = (dbl ? 8 : 4) + 8ull * j.T;
   if (j.cap < head) return fail(SZP_GB300_ECAPACITY, "output buffer smaller than the stream header");
   const bool fm2 = j.fm == 2;
+  // float64 data on blockSizes the pipelines take: a quantization pass, then
+  // the pipeline over int32 q
+  const bool qpipe = dbl && f64_pipe_supported((uint32_t)j.L);
   Segments sg = make_segments(j.n, j.T, j.L);
   uint32_t bpw = 1;
-  uint32_t tb = dbl ? compress_blocks_per_tile_f64((uint32_t)j.L, bpw) : compress_blocks_per_tile((uint32_t)j.L, bpw);
+  uint32_t tb = dbl && !qpipe ? compress_blocks_per_tile_f64((uint32_t)j.L, bpw)
+                              : compress_blocks_per_tile((uint32_t)j.L, bpw);
   uint64_t per_seg, ntiles;
   tile_counts(sg, fm2, tb, per_seg, ntiles);
   if (ntiles >= (1ull << 31) || per_seg >= (1ull << 31))
@@ -341,6 +349,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   a.thr = table();
   a.xd = j.d_xd;
   a.ebd = j.eb_abs_d;
+  a.invd = dbl ? 1.0 / j.eb_abs_d : 0.0;  // binary64 division, as the reference's inverse
 
   int launches = 0;
   if (j.eb_mode == REL && dbl) {
@@ -352,6 +361,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     r.partial = w.rel_partial.as<float>();  // 2 doubles per CTA
     r.counter = &dm->rel_counter;
     r.ebd_out = &dm->ebd;
+    r.invd_out = &dm->invd;
     uint64_t want = (j.n / 4 + 255) / 256;
     uint32_t grid = (uint32_t)(want < 1 ? 1 : want);
     uint32_t lim = (uint32_t)(w.sm_count * 4 < kRelMaxGrid ? w.sm_count * 4 : kRelMaxGrid);
@@ -360,6 +370,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     CU(launch_rel_bound_f64(r, grid, st));
     w.mark(kSlotRel, 1, st);
     a.ebd_dev = &dm->ebd;
+    a.invd_dev = &dm->invd;
     launches++;
   } else if (j.eb_mode == REL) {
     RelArgs r;
@@ -380,10 +391,22 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     a.eb_dev = &dm->eb;
     launches++;
   }
-  size_t smem = dbl ? compress_smem_bytes_f64((uint32_t)j.L, tb) : compress_smem_bytes((uint32_t)j.L, tb);
+  size_t smem = dbl && !qpipe ? compress_smem_bytes_f64((uint32_t)j.L, tb) : compress_smem_bytes((uint32_t)j.L, tb);
   if (smem > 200 * 1024) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
+  int32_t* q = nullptr;
+  if (qpipe) {
+    CU(w.qbuf.ensure((j.n + 4) * sizeof(int32_t)));
+    q = f64_q_view(w.qbuf.p, j.d_xd);
+  }
   w.mark(kSlotCompress, 0, st);
-  CU(dbl ? launch_compress_f64(a, fm2, st) : launch_compress(a, fm2, st));
+  if (qpipe) {
+    CU(launch_quantize_f64(j.d_xd, q, j.n, a.invd, a.invd_dev, a.err, (uint32_t)w.sm_count, st));
+    a.x = reinterpret_cast<const float*>(q);
+    CU(launch_compress_q(a, fm2, st));
+    launches++;
+  } else {
+    CU(dbl ? launch_compress_f64(a, fm2, st) : launch_compress(a, fm2, st));
+  }
   w.mark(kSlotCompress, 1, st);
   launches++;
   if (j.d_size) CU(cudaMemcpyAsync(j.d_size, &dm->out_size, 8, cudaMemcpyDeviceToDevice, st));
@@ -425,8 +448,11 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   const bool dbl = j.dbl;
   const uint64_t head = (dbl ? 8 : 4) + 8ull * j.T;
   if (j.len < head) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
-  if (j.n && !(dbl ? (void*)j.d_yd : (void*)j.d_y)) return fail(SZP_GB300_EINVAL, "null output");
+  void* yout = dbl ? (void*)j.d_yd : (void*)j.d_y;
+  if (j.n && !yout) return fail(SZP_GB300_EINVAL, "null output");
+  if ((uintptr_t)yout & (dbl ? 7 : 3)) return fail(SZP_GB300_EINVAL, "output not aligned to its element size");
   const bool fm2 = j.fm == 2;
+  const bool qpipe = dbl && f64_pipe_supported((uint32_t)j.L);  // pipeline to int32 q, then a pass
   Segments sg = make_segments(j.n, j.T, j.L);
   const uint32_t maxsz = fm2 ? (j.L == 1 ? 5u : 4 + block_bytes((uint32_t)j.L - 1, kMaxBitCount))
                              : max_block_bytes((uint32_t)j.L);
@@ -435,7 +461,8 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   const uint32_t SC = locate_super_bytes(maxsz);
   const uint64_t nlocate = (j.len + SC - 1) / SC + (uint64_t)j.T + 1;
   uint32_t bpw = 1;
-  uint32_t tb = dbl ? decode_blocks_per_tile_f64((uint32_t)j.L, bpw) : decode_blocks_per_tile((uint32_t)j.L, bpw);
+  uint32_t tb = dbl && !qpipe ? decode_blocks_per_tile_f64((uint32_t)j.L, bpw)
+                              : decode_blocks_per_tile((uint32_t)j.L, bpw);
   uint64_t per_seg, ntiles;
   tile_counts(sg, fm2, tb, per_seg, ntiles);
   uint64_t nblk_total = 0;
@@ -489,9 +516,15 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.tb = tb;
   a.bpw = bpw;
   a.nlocate_ctas = (uint32_t)nlocate;
-  if ((!dbl && decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) ||
+  if (((!dbl || qpipe) && decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) ||
       locate_smem_bytes(SC, a.overlap, maxsz) > 200 * 1024)
     return fail(SZP_GB300_EINVAL, "blockSize too large");
+  int32_t* q = nullptr;
+  if (qpipe) {
+    CU(w.qbuf.ensure((j.n + 4) * sizeof(int32_t)));
+    q = f64_q_view(w.qbuf.p, j.d_yd);
+    f.y = reinterpret_cast<float*>(q);
+  }
   CU(cudaMemsetAsync(dm->verify, 0, sizeof(uint32_t), st));
 
   w.mark(kSlotSetup, 0, st);
@@ -501,9 +534,14 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   CU(launch_locate(a, st));
   w.mark(kSlotLocate, 1, st);
   w.mark(kSlotDecode, 0, st);
-  CU(dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
+  if (qpipe) {
+    CU(launch_decode_q(a, st));
+    CU(launch_dequant_f64(q, j.d_yd, j.n, f.plan, (uint32_t)w.sm_count, st));
+  } else {
+    CU(dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
+  }
   w.mark(kSlotDecode, 1, st);
-  count_launches(3);
+  count_launches(qpipe ? 4 : 3);
   return SZP_GB300_OK;
 }
 

@@ -231,6 +231,16 @@ __device__ __forceinline__ void write_header_warp(uint8_t* out, float eb, const 
   }
 }
 
+// The float64 stream's header: eb as 8 big-endian bytes, zero offsets as above.
+__device__ __forceinline__ void write_header_warp(uint8_t* out, double eb, const Segments& sg, int lane) {
+  const uint64_t b = (uint64_t)__double_as_longlong(eb);
+  if (lane < 8) out[lane] = (uint8_t)(b >> (56 - 8 * lane));
+  if (sg.tsz == 0) {
+    const uint32_t nz = 8 * (sg.n == 0 ? sg.T : sg.T - 1);
+    for (uint32_t i = lane; i < nz; i += 32) out[8 + i] = 0;
+  }
+}
+
 // One warp copies len bytes from shared memory src (16-byte aligned, readable
 // for len + 16 bytes) to global dst (any alignment): 16-byte stores for the
 // aligned middle, the bytes shifted into place with funnel shifts; byte
@@ -388,7 +398,7 @@ __device__ __forceinline__ void pipe_producer(const CompressArgs& a, uint8_t* sl
 }
 
 // Control warp c: tiles c, c + kPipeControl, ... of this CTA.
-template <int NS, int NC>
+template <int NS, int NC, bool QI = false>
 __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const uint8_t* slots,
                                              uint32_t slot_bytes, const SlotMeta* meta, const uint32_t* s_agg,
                                              uint64_t* full, uint64_t* aggb, uint64_t* packed, uint64_t* empty,
@@ -409,17 +419,22 @@ __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const
     const uint32_t agg = s_agg[s];
     const uint32_t epoch = *s_epoch;
     uint64_t excl = 0;
+    constexpr uint32_t HB = QI ? 8 : 4;  // eb header bytes: float64 streams carry a double
     if (lt == 0) {
-      write_header_warp(out, m.eb, m.seg, lane);
+      if (QI) {
+        write_header_warp(out, a.ebd_dev ? *a.ebd_dev : a.ebd, m.seg, lane);
+      } else {
+        write_header_warp(out, m.eb, m.seg, lane);
+      }
     } else {
       excl = lookback_sum(a.status, tile, m.tile_base, epoch, a.err);
       if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
-    const uint64_t gpos = 4 + 8ull * m.seg.T + excl;
+    const uint64_t gpos = HB + 8ull * m.seg.T + excl;
     const bool fits = gpos + agg <= cap;
     if (lane == 0) {
       if (lt == m.ntiles - 1) *m.out_size = gpos + agg;
-      if (first_of_seg && fits) write_offset(out, seg, excl);
+      if (first_of_seg && fits) write_offset(out, seg, excl, HB);
       if (!fits) atomicOr(m.err, kErrCapacity);
     }
     mbar_wait_or_flag(&packed[s], par, a.err);
@@ -429,7 +444,9 @@ __device__ __forceinline__ void pipe_control(int c, const CompressArgs& a, const
   }
 }
 
-template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false>
+// QI: the input is float64 data already quantized to int32 (four bytes per
+// element like a float), packed into a stream with an 8-byte eb header.
+template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false, bool QI = false>
 __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_constant__ CompressArgs a,
                                                                  uint32_t slot_bytes) {
   constexpr int NS = kPipeSlots, NC = kPipeControl;
@@ -471,8 +488,8 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
     return;
   }
   if (warp >= 8) {
-    pipe_control<NS, NC>(warp - 8, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_packed, s_empty,
-                         &s_epoch, &s_stop_k);
+    pipe_control<NS, NC, QI>(warp - 8, a, s_slots, slot_bytes, s_meta, s_agg, s_full, s_aggb, s_packed, s_empty,
+                             &s_epoch, &s_stop_k);
     return;
   }
 
@@ -492,7 +509,8 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
     const bool seed = !FM2 && g.has_seg && g.first && g.hi > g.lo;  // the segment's seed (fastmode1)
     int32_t seedv = 0;
     uint32_t flags = 0;
-    if (seed && threadIdx.x == 0) seedv = quantize(sx[g.d], inv, flags);  // x[lo] = window element 0
+    if (seed && threadIdx.x == 0)  // x[lo] = window element 0
+      seedv = QI ? __float_as_int(sx[g.d]) : quantize(sx[g.d], inv, flags);
 
     // ---- analysis: q, deltas, signs, block max, bit count, block size ----
     uint32_t vv[ROUNDS][8];
@@ -543,7 +561,10 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
         for (int j = 0; j < 8; j++) xv[j] = (uint32_t)j < ml ? sx[i + j] : 0.0f;
       }
       int32_t q[8];
-      if (EXACT) {
+      if (QI) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) q[j] = __float_as_int(xv[j]);
+      } else if (EXACT) {
 #pragma unroll
         for (int j = 0; j < 8; j++) q[j] = quantize_lean(xv[j], inv, flags);
       } else {
@@ -557,7 +578,9 @@ __global__ void __launch_bounds__(kPipeThreads, 2) compress_pipe(const __grid_co
       int32_t prev = __shfl_up_sync(0xffffffffu, q[7], 1);
       if (FM2 ? sub == 0 : lane == 0) {  // the element before the lane's first: fastmode2 the block's seed
         const float xp = bt < g.nblk ? sx[i - 1] : 0.0f;  // past the tile's blocks the slot holds no input
-        if (EXACT) {
+        if (QI) {
+          prev = __float_as_int(xp);
+        } else if (EXACT) {
           prev = quantize_lean(xp, inv, flags);
         } else {
           const float pp = __fmul_rz(xp, inv);
@@ -798,7 +821,7 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   V eb, inv;
   if constexpr (DBL) {
     eb = a.ebd_dev ? *a.ebd_dev : a.ebd;
-    inv = __ddiv_rn(1.0, eb);  // 1/eb in double, szp_double.cc:180
+    inv = a.invd_dev ? *a.invd_dev : a.invd;  // 1/eb in double, szp_double.cc:180
   } else {
     eb = a.eb_dev ? *a.eb_dev : a.eb;
     inv = __fdiv_rn(1.0f, eb);
@@ -1238,7 +1261,9 @@ __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
     const double fmn = f64_unkey(mn), fmx = f64_unkey(mx);  // x[0] is a number, so both were seen
     range = (fmx == fmn && isfinite(fmx)) ? 0.0 : x86_nan_fix_d(__dsub_rn(fmx, fmn), fmx, fmn);
   }
-  *a.ebd_out = x86_nan_fix_d(__dmul_rn(range, a.rel_d), range, a.rel_d);
+  const double eb = x86_nan_fix_d(__dmul_rn(range, a.rel_d), range, a.rel_d);
+  *a.ebd_out = eb;
+  *a.invd_out = x86_nan_fix_d(__ddiv_rn(1.0, eb), 1.0, eb);  // once, for every quantizing thread
 }
 
 // ---------------------------------------------------------------------------
@@ -1297,9 +1322,9 @@ static uint32_t pipe_slot_bytes(uint32_t L, uint32_t tb, bool fm2) {
   return (uint32_t)(((out > in ? out : in) + 15) & ~(size_t)15);
 }
 
-template <int LPB, bool BATCH = false, int ROUNDS = kRounds, bool FM2 = false>
+template <int LPB, bool BATCH = false, int ROUNDS = kRounds, bool FM2 = false, bool QI = false>
 static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
-  auto k = compress_pipe<LPB, BATCH, ROUNDS, FM2>;
+  auto k = compress_pipe<LPB, BATCH, ROUNDS, FM2, QI>;
   const uint32_t slot = pipe_slot_bytes(a.seg.L, a.tb, FM2);
   const size_t smem = (size_t)kPipeSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
@@ -1494,6 +1519,79 @@ cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds,
 cudaError_t launch_rel_bound_f64(const RelArgs& a, uint32_t grid, cudaStream_t st) {
   rel_bound_kernel_f64<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
+}
+
+// float64 quantization pass (szp_double.cc:180-230's q = (int)(x * inver)):
+// q[i] from x[i] in integer arithmetic, four elements per step (two 16-byte
+// loads, one 16-byte store; x + h and q + h are 16-byte aligned, h the
+// elements before x's first 16-byte boundary).  Range errors set the
+// quantization flag, as the compress kernels do.
+__global__ void __launch_bounds__(256) quantize_f64_kernel(const double* __restrict__ x, int32_t* __restrict__ q,
+                                                           uint64_t n, double invd, const double* invd_dev,
+                                                           uint32_t* err) {
+  const f64i::Operand io = f64i::unpack(f64i::bits_of(invd_dev ? *invd_dev : invd));
+  bool bad = false;
+  const uint64_t h = min(n, (uint64_t)((((uintptr_t)x & 15) >> 3)));
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (tid < h) q[tid] = f64i::quantize(f64i::bits_of(x[tid]), io, bad);
+  const double2* x2 = reinterpret_cast<const double2*>(x + h);
+  int4* q4 = reinterpret_cast<int4*>(q + h);
+  const uint64_t n4 = (n - h) >> 2;
+  for (uint64_t i = tid; i < n4; i += stride) {
+    const double2 u = __ldcs(x2 + 2 * i), v = __ldcs(x2 + 2 * i + 1);
+    int4 r;
+    r.x = f64i::quantize(f64i::bits_of(u.x), io, bad);
+    r.y = f64i::quantize(f64i::bits_of(u.y), io, bad);
+    r.z = f64i::quantize(f64i::bits_of(v.x), io, bad);
+    r.w = f64i::quantize(f64i::bits_of(v.y), io, bad);
+    q4[i] = r;
+  }
+  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) q[i] = f64i::quantize(f64i::bits_of(x[i]), io, bad);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, kErrQuantRange);
+}
+
+bool f64_pipe_supported(uint32_t L) { return lanes_per_block(L) != 0; }
+
+// qbuf holds n + 4 int32; the view starts 0-3 elements in so that the q of
+// element i shares its 16-byte phase with x[i] (doubles: phase 0 or 8 bytes).
+int32_t* f64_q_view(void* qbuf, const void* xy) {
+  const uint32_t h = ((uintptr_t)xy & 15) ? 1u : 0u;  // elements before the first 16-byte boundary
+  return reinterpret_cast<int32_t*>(qbuf) + ((4 - h) & 3);
+}
+
+cudaError_t launch_quantize_f64(const double* x, int32_t* q, uint64_t n, double invd, const double* invd_dev,
+                                uint32_t* err, uint32_t sm_count, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const uint64_t want = (n / 4 + 255) / 256;
+  const uint64_t lim = (uint64_t)(sm_count ? sm_count : 1) * 8;
+  const uint32_t grid = (uint32_t)(want < 1 ? 1 : (want > lim ? lim : want));
+  quantize_f64_kernel<<<grid, 256, 0, st>>>(x, q, n, invd, invd_dev, err);
+  return cudaGetLastError();
+}
+
+// The fastmode pipelines over int32 q of float64 data (8-byte eb header).
+cudaError_t launch_compress_q(const CompressArgs& a, bool fm2, cudaStream_t st) {
+  if (fm2) {
+    switch (lanes_per_block(a.seg.L)) {
+      case 1: return launch_lanes<1, false, kRounds, true, true>(a, st);
+      case 2: return launch_lanes<2, false, kRounds, true, true>(a, st);
+      case 4: return launch_lanes<4, false, kRounds, true, true>(a, st);
+      case 8: return launch_lanes<8, false, kRounds, true, true>(a, st);
+      case 16: return launch_lanes<16, false, kRounds, true, true>(a, st);
+      case 32: return launch_lanes<32, false, kRounds, true, true>(a, st);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  switch (lanes_per_block(a.seg.L)) {
+    case 1: return launch_lanes<1, false, kRounds, false, true>(a, st);
+    case 2: return launch_lanes<2, false, kRounds, false, true>(a, st);
+    case 4: return launch_lanes<4, false, kRounds, false, true>(a, st);
+    case 8: return launch_lanes<8, false, kRounds, false, true>(a, st);
+    case 16: return launch_lanes<16, false, kRounds, false, true>(a, st);
+    case 32: return launch_lanes<32, false, kRounds, false, true>(a, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 // float64 data: the one-warp-per-block kernel for every blockSize, tiles kept

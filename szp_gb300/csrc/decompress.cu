@@ -792,8 +792,11 @@ __device__ __forceinline__ void lds_le64(const uint8_t* b, uint32_t o, uint32_t&
 // tile's nel elements starting at dst = y + e0; 16-byte stores for the aligned
 // middle, the words picked from two aligned shared-memory lines when dst is not
 // 16-byte aligned.  stage is 16-byte aligned and readable for nel + 4 words.
+// QO: the q themselves are stored (as their bits), for a float64 pass to finish.
+template <bool QO = false>
 __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
                                                   uint32_t nel, uint32_t base, float eb, bool ebsp) {
+  auto dq = [eb, ebsp](uint32_t q) -> float { return QO ? __uint_as_float(q) : dequant(q, eb, ebsp); };
   const uint32_t tid = threadIdx.x;
   if (nel == 0) return;
   const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 2) & 3);
@@ -801,12 +804,12 @@ __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const
   const uint32_t end = ph + nel;
   const uint32_t c0 = (ph + 3) >> 2, c1 = end >> 2;  // whole float4 chunks [c0, c1)
   if (c0 >= c1) {
-    if (tid < nel) g0[ph + tid] = dequant(base + stage[tid], eb, ebsp);
+    if (tid < nel) g0[ph + tid] = dq(base + stage[tid]);
     return;
   }
-  if (tid < 4 * c0 - ph) g0[ph + tid] = dequant(base + stage[tid], eb, ebsp);
+  if (tid < 4 * c0 - ph) g0[ph + tid] = dq(base + stage[tid]);
   if (tid >= 32 && tid - 32 < end - 4 * c1)
-    g0[4 * c1 + tid - 32] = dequant(base + stage[4 * c1 + tid - 32 - ph], eb, ebsp);
+    g0[4 * c1 + tid - 32] = dq(base + stage[4 * c1 + tid - 32 - ph]);
   const uint4* s4 = reinterpret_cast<const uint4*>(stage);
   // four chunks per thread per pass: their shared-memory loads are in flight together
   constexpr int U = 4;
@@ -829,10 +832,10 @@ __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const
       const uint32_t c = cb + tid + 256 * u;
       if (c < c1) {
         float4 o;
-        o.x = dequant(base + w[u].x, eb, ebsp);
-        o.y = dequant(base + w[u].y, eb, ebsp);
-        o.z = dequant(base + w[u].z, eb, ebsp);
-        o.w = dequant(base + w[u].w, eb, ebsp);
+        o.x = dq(base + w[u].x);
+        o.y = dq(base + w[u].y);
+        o.z = dq(base + w[u].z);
+        o.w = dq(base + w[u].w);
         reinterpret_cast<float4*>(g0)[c] = o;
       }
     }
@@ -842,7 +845,7 @@ __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const
 // Control warp c: tiles c, c + kDecControl, ... of this CTA.  Finds each
 // tile's base q (the segment's seed plus the deltas of the tiles before it) and
 // hands it to the compute warps, which finish the tile.
-template <int NS, int NC>
+template <int NS, int NC, bool QO = false>
 __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSlot* meta, const uint32_t* s_agg,
                                             uint32_t* s_base, uint64_t* full, uint64_t* aggb, uint64_t* based,
                                             const uint32_t* s_epoch, const volatile uint32_t* s_stop_k) {
@@ -862,7 +865,7 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
       base = meta[s].seed;
       if (lane == 0) {
         const float eb = meta[s].eb;
-        meta[s].y[meta[s].e0 - 1] = dequant(base, eb, !isfinite(eb));
+        meta[s].y[meta[s].e0 - 1] = QO ? __uint_as_float(base) : dequant(base, eb, !isfinite(eb));
       }
     } else {
       base = (uint32_t)lookback_sum(a.status, tile, meta[s].seg_tile0, epoch, a.err);
@@ -876,7 +879,8 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
   }
 }
 
-template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false>
+// QO: y receives int32 q (float64 streams; a pass turns them into doubles).
+template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false, bool QO = false>
 __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_constant__ DecArgs a,
                                                                   uint32_t slot_bytes) {
   constexpr int NS = kDecSlots, NC = kDecControl, WARPS = 8;
@@ -918,7 +922,8 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
   }
   if (warp >= WARPS) {
     // fastmode2 blocks carry their own seeds: no look-back, nothing to control
-    if (!FM2) dec_control<NS, NC>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
+    if (!FM2)
+      dec_control<NS, NC, QO>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
     return;
   }
 
@@ -932,7 +937,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
     mbar_wait_or_flag(&s_based[sp_], (kp / NS) & 1, a.err);
     const float ebp = s_meta[sp_].eb;
     const uint32_t* stage = reinterpret_cast<const uint32_t*>(s_slots + (size_t)sp_ * slot_bytes + PB);
-    cta_dequant_store(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp));
+    cta_dequant_store<QO>(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp));
     compute_sync();  // every read of the slot is done
     if (threadIdx.x == 0) mbar_arrive(&s_empty[sp_]);
   };
@@ -1098,7 +1103,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       }
       compute_sync();
       const float ebp = s_meta[s].eb;
-      cta_dequant_store(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
+      cta_dequant_store<QO>(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
       compute_sync();  // every read of the slot is done
       if (threadIdx.x == 0) mbar_arrive(&s_empty[s]);
       continue;
@@ -1420,9 +1425,9 @@ static uint32_t dec_slot_bytes(uint32_t L, uint32_t tb, uint32_t maxsz) {
   return (uint32_t)((dec_pos_bytes(tb) + (span > stage ? span : stage) + 15) & ~(size_t)15);
 }
 
-template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds, bool FM2 = false>
+template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds, bool FM2 = false, bool QO = false>
 static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
-  auto k = decode_pipe<LPB, BATCH, ROUNDS, FM2>;
+  auto k = decode_pipe<LPB, BATCH, ROUNDS, FM2, QO>;
   const uint32_t slot = dec_slot_bytes(8 * LPB, a.tb, a.maxsz);
   const size_t smem = (size_t)kDecSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
@@ -1461,6 +1466,70 @@ cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st) {
   } else {
     decode_generic<kDecWarps, false, double><<<a.ntiles, kDecWarps * 32, 0, st>>>(a);
   }
+  return cudaGetLastError();
+}
+
+// The fastmode pipelines to int32 q (float64 streams, blockSize 8..256).
+cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st) {
+  if (a.fm2) {
+    switch (dec_lanes_per_block(a.f.seg.L)) {
+      case 1: return launch_dec_lanes<1, false, kDecRounds, true, true>(a, st);
+      case 2: return launch_dec_lanes<2, false, kDecRounds, true, true>(a, st);
+      case 4: return launch_dec_lanes<4, false, kDecRounds, true, true>(a, st);
+      case 8: return launch_dec_lanes<8, false, kDecRounds, true, true>(a, st);
+      case 16: return launch_dec_lanes<16, false, kDecRounds, true, true>(a, st);
+      case 32: return launch_dec_lanes<32, false, kDecRounds, true, true>(a, st);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  switch (dec_lanes_per_block(a.f.seg.L)) {
+    case 1: return launch_dec_lanes<1, false, kDecRounds, false, true>(a, st);
+    case 2: return launch_dec_lanes<2, false, kDecRounds, false, true>(a, st);
+    case 4: return launch_dec_lanes<4, false, kDecRounds, false, true>(a, st);
+    case 8: return launch_dec_lanes<8, false, kDecRounds, false, true>(a, st);
+    case 16: return launch_dec_lanes<16, false, kDecRounds, false, true>(a, st);
+    case 32: return launch_dec_lanes<32, false, kDecRounds, false, true>(a, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// float64 dequantization pass (szpd_double.cc:67,86,112's (double)q * eb):
+// y[i] from int32 q[i], four elements per step (one 16-byte load, two 16-byte
+// stores; y + h and q + h 16-byte aligned).  Integer arithmetic for every eb
+// whose products stay normal, the FP64 multiply (x86 NaN rules) otherwise.
+__global__ void __launch_bounds__(256) dequant_f64_kernel(const int32_t* __restrict__ q, double* __restrict__ y,
+                                                          uint64_t n, const DecPlan* __restrict__ plan) {
+  if (plan->bad) return;
+  const double eb = plan->ebd;
+  const uint64_t u = f64i::bits_of(eb);
+  const bool fast = f64i::dequant_fast_ok(u), ebsp = !isfinite(eb);
+  const uint64_t ebm = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52), ebs = u & 0x8000000000000000ull;
+  const uint32_t ebe = (uint32_t)(u >> 52) & 0x7FFu;
+  auto dq = [&](int32_t v) -> double {
+    return fast ? f64i::double_of(f64i::dequant_bits(v, ebm, ebe, ebs)) : dequant((uint32_t)v, eb, ebsp);
+  };
+  const uint64_t h = min(n, (uint64_t)((((uintptr_t)y & 15) >> 3)));
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  if (tid < h) y[tid] = dq(q[tid]);
+  const int4* q4 = reinterpret_cast<const int4*>(q + h);
+  double2* y2 = reinterpret_cast<double2*>(y + h);
+  const uint64_t n4 = (n - h) >> 2;
+  for (uint64_t i = tid; i < n4; i += stride) {
+    const int4 v = __ldcs(q4 + i);
+    __stcs(y2 + 2 * i, make_double2(dq(v.x), dq(v.y)));
+    __stcs(y2 + 2 * i + 1, make_double2(dq(v.z), dq(v.w)));
+  }
+  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) y[i] = dq(q[i]);
+}
+
+cudaError_t launch_dequant_f64(const int32_t* q, double* y, uint64_t n, const DecPlan* plan, uint32_t sm_count,
+                               cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const uint64_t want = (n / 4 + 255) / 256;
+  const uint64_t lim = (uint64_t)(sm_count ? sm_count : 1) * 8;
+  const uint32_t grid = (uint32_t)(want < 1 ? 1 : (want > lim ? lim : want));
+  dequant_f64_kernel<<<grid, 256, 0, st>>>(q, y, n, plan);
   return cudaGetLastError();
 }
 

@@ -132,3 +132,42 @@ def test_double_host_api_tiny_and_empty(szp, port):
         assert s == port.compress_d(x, 1e-3, 32, 4, 1), n
         y = szp.szp_decompress(s, n, 32, 1, szp.SZ_DOUBLE)
         assert np.array_equal(bits(y), bits(port.decompress_d(s, n, 32, 4, 1))), n
+
+
+@pytest.mark.parametrize("L", [8, 32, 256, 24])
+@pytest.mark.parametrize("mode", [1, 2])
+def test_double_views_off_16_byte_boundaries(szp, port, torch, L, mode):
+    """Input and output one double past a 16-byte boundary (the quantization
+    and dequantization passes' ragged heads), for the pipeline blockSizes and
+    the one-warp-per-block kernels alike."""
+    from szp_gb300.workloads import walk64
+    rng = np.random.default_rng(500 + L + mode)
+    n, T = 300_007, 5
+    x = walk64(n + 1, rng)
+    dx = torch.from_numpy(x).cuda()[1:]
+    assert dx.data_ptr() % 16 == 8
+    xs = x[1:].copy()
+    st = torch.cuda.current_stream().cuda_stream
+    cap = szp.max_stream_bytes_f64(n, L, T, mode)
+    dout = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    size = szp.compress_dev_f64(dx.data_ptr(), n, dout.data_ptr(), cap, szp.REL, 0.0, 1e-5, L, T, mode, st)
+    s = dout[:size].cpu().numpy().tobytes()
+    assert s == port.compress_d(xs, port.rel_bound_d(xs, 1e-5), L, T, mode)
+    dy = torch.full((n + 1,), 7.0, dtype=torch.float64, device="cuda")
+    szp.decompress_dev_f64(dout.data_ptr(), size, n, dy[1:].data_ptr(), L, T, mode, st)
+    y = dy.cpu().numpy()
+    assert y[0] == 7.0
+    assert np.array_equal(bits(y[1:]), bits(port.decompress_d(s, n, L, T, mode)))
+
+
+def test_double_misaligned_pointers_rejected(szp, torch):
+    """A double pointer off its 8-byte alignment is refused before any launch."""
+    dx = torch.zeros(1024, dtype=torch.float64, device="cuda")
+    cap = szp.max_stream_bytes_f64(1000, 32, 4, 1)
+    dout = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    with pytest.raises(szp.SzpError):
+        szp.compress_dev_f64(dx.data_ptr() + 4, 1000, dout.data_ptr(), cap, szp.ABS, 1e-3, 0.0, 32, 4, 1, st)
+    size = szp.compress_dev_f64(dx.data_ptr(), 1000, dout.data_ptr(), cap, szp.ABS, 1e-3, 0.0, 32, 4, 1, st)
+    with pytest.raises(szp.SzpError):
+        szp.decompress_dev_f64(dout.data_ptr(), size, 1000, dx.data_ptr() + 4, 32, 4, 1, st)
