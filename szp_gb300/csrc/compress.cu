@@ -817,7 +817,9 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   const uint32_t L = sg.L;
   uint32_t flags = 0;
   const uint32_t TB = WARPS * a.bpw;
-  const V* __restrict__ xs = DBL ? reinterpret_cast<const V*>(a.xd) : reinterpret_cast<const V*>(a.x);
+  // float64 values are loaded as their bits (see f64_key)
+  using LT = typename std::conditional<DBL, unsigned long long, float>::type;
+  const LT* __restrict__ xs = DBL ? reinterpret_cast<const LT*>(a.xd) : reinterpret_cast<const LT*>(a.x);
   V eb, inv;
   if constexpr (DBL) {
     eb = a.ebd_dev ? *a.ebd_dev : a.ebd;
@@ -828,10 +830,10 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
   }
   f64i::Operand invo{};  // 1/eb's fields for the integer float64 quantizer
   if constexpr (DBL) invo = f64i::unpack(f64i::bits_of(inv));
-  auto qz = [&](V v) -> int32_t {
+  auto qz = [&](LT v) -> int32_t {
     if constexpr (DBL) {
       bool bad = false;
-      const int32_t q = f64i::quantize(f64i::bits_of(v), invo, bad);
+      const int32_t q = f64i::quantize(v, invo, bad);
       if (bad) flags |= kErrQuantRange;
       return q;
     } else {
@@ -872,11 +874,11 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     cbc[k] = 0;
   }
   if (cache) {
-    V xv[KC];
-    V xp = V(0);
+    LT xv[KC];
+    LT xp = LT(0);
 #pragma unroll
     for (int c = 0; c < KC; c++) {
-      xv[c] = V(0);
+      xv[c] = LT(0);
       const uint32_t bi = wfirst + c;
       if ((uint32_t)c < a.bpw && bi < ti.nblk && (uint32_t)lane < block_len(ti.blk0 + bi))
         xv[c] = __ldg(xs + block_start(ti.blk0 + bi) + lane);
@@ -1158,10 +1160,12 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
   *a.eb_out = x86_nan_fix(__fmul_rn(range, a.rel), range, a.rel);
 }
 
-// Order-preserving key of a double (larger value, larger key); NaNs get key
-// 0, below every number's (the reduction uses 0 as "nothing seen" too).
-__device__ __forceinline__ uint64_t f64_key(double v) {
-  const uint64_t u = (uint64_t)__double_as_longlong(v);
+// Order-preserving key of a double's bits (larger value, larger key); NaNs
+// get key 0, below every number's (the reduction uses 0 as "nothing seen"
+// too).  The float64 passes load their data as 64-bit integers: on bits
+// taken from a double the compiler turns these tests back into FP64 compares,
+// which run on this GPU's narrow FP64 pipe.
+__device__ __forceinline__ uint64_t f64_key(uint64_t u) {
   if ((u & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull) return 0;  // NaN: skipped, as the reference's compares do
   return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
@@ -1179,33 +1183,34 @@ __global__ void __launch_bounds__(256) rel_bound_kernel_f64(RelArgs a) {
   __shared__ bool s_last;
   uint64_t mn = ~0ull, mx = 0;  // keys; 0 also stands for "none" (NaN keys never count)
   const double* x = a.xd;
+  const unsigned long long* xb = reinterpret_cast<const unsigned long long*>(x);  // the doubles' bits
   const uint64_t n = a.n;
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  auto take = [&](double v) {
-    const uint64_t k = f64_key(v);
+  auto take = [&](uint64_t u) {
+    const uint64_t k = f64_key(u);
     if (k) {
       mn = min(mn, k);
       mx = max(mx, k);
     }
   };
   const uint64_t headn = min(n, (uint64_t)((((uintptr_t)x & 15) >> 3)));  // one double to 16-byte alignment
-  for (uint64_t i = tid; i < headn; i += stride) take(x[i]);
-  const double2* x2 = reinterpret_cast<const double2*>(x + headn);
+  for (uint64_t i = tid; i < headn; i += stride) take(xb[i]);
+  const ulonglong2* x2 = reinterpret_cast<const ulonglong2*>(xb + headn);
   const uint64_t n2 = (n - headn) >> 1;
   uint64_t i = tid;
   for (; i + 3 * stride < n2; i += 4 * stride) {
-    const double2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + stride);
-    const double2 v2 = __ldg(x2 + i + 2 * stride), v3 = __ldg(x2 + i + 3 * stride);
+    const ulonglong2 v0 = __ldg(x2 + i), v1 = __ldg(x2 + i + stride);
+    const ulonglong2 v2 = __ldg(x2 + i + 2 * stride), v3 = __ldg(x2 + i + 3 * stride);
     take(v0.x); take(v0.y); take(v1.x); take(v1.y);
     take(v2.x); take(v2.y); take(v3.x); take(v3.y);
   }
   for (; i < n2; i += stride) {
-    const double2 v = __ldg(x2 + i);
+    const ulonglong2 v = __ldg(x2 + i);
     take(v.x);
     take(v.y);
   }
-  for (uint64_t j = headn + 2 * n2 + tid; j < n; j += stride) take(x[j]);
+  for (uint64_t j = headn + 2 * n2 + tid; j < n; j += stride) take(xb[j]);
   for (int o = 16; o > 0; o >>= 1) {
     mn = min(mn, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mn, o));
     mx = max(mx, (uint64_t)__shfl_xor_sync(0xffffffffu, (unsigned long long)mx, o));
@@ -1534,20 +1539,21 @@ __global__ void __launch_bounds__(256) quantize_f64_kernel(const double* __restr
   const uint64_t h = min(n, (uint64_t)((((uintptr_t)x & 15) >> 3)));
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  if (tid < h) q[tid] = f64i::quantize(f64i::bits_of(x[tid]), io, bad);
-  const double2* x2 = reinterpret_cast<const double2*>(x + h);
+  const unsigned long long* xb = reinterpret_cast<const unsigned long long*>(x);  // bits, see f64_key
+  if (tid < h) q[tid] = f64i::quantize(xb[tid], io, bad);
+  const ulonglong2* x2 = reinterpret_cast<const ulonglong2*>(xb + h);
   int4* q4 = reinterpret_cast<int4*>(q + h);
   const uint64_t n4 = (n - h) >> 2;
   for (uint64_t i = tid; i < n4; i += stride) {
-    const double2 u = __ldcs(x2 + 2 * i), v = __ldcs(x2 + 2 * i + 1);
+    const ulonglong2 u = __ldcs(x2 + 2 * i), v = __ldcs(x2 + 2 * i + 1);
     int4 r;
-    r.x = f64i::quantize(f64i::bits_of(u.x), io, bad);
-    r.y = f64i::quantize(f64i::bits_of(u.y), io, bad);
-    r.z = f64i::quantize(f64i::bits_of(v.x), io, bad);
-    r.w = f64i::quantize(f64i::bits_of(v.y), io, bad);
+    r.x = f64i::quantize(u.x, io, bad);
+    r.y = f64i::quantize(u.y, io, bad);
+    r.z = f64i::quantize(v.x, io, bad);
+    r.w = f64i::quantize(v.y, io, bad);
     q4[i] = r;
   }
-  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) q[i] = f64i::quantize(f64i::bits_of(x[i]), io, bad);
+  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) q[i] = f64i::quantize(xb[i], io, bad);
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, kErrQuantRange);
 }
 

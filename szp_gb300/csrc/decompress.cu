@@ -1505,22 +1505,25 @@ __global__ void __launch_bounds__(256) dequant_f64_kernel(const int32_t* __restr
   const bool fast = f64i::dequant_fast_ok(u), ebsp = !isfinite(eb);
   const uint64_t ebm = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52), ebs = u & 0x8000000000000000ull;
   const uint32_t ebe = (uint32_t)(u >> 52) & 0x7FFu;
-  auto dq = [&](int32_t v) -> double {
-    return fast ? f64i::double_of(f64i::dequant_bits(v, ebm, ebe, ebs)) : dequant((uint32_t)v, eb, ebsp);
+  // the results as bits (integers end to end, no FP64 instruction on the
+  // fast path), or the FP64 multiply
+  auto dq = [&](int32_t v) -> unsigned long long {
+    return fast ? f64i::dequant_bits(v, ebm, ebe, ebs) : f64i::bits_of(dequant((uint32_t)v, eb, ebsp));
   };
+  unsigned long long* yb = reinterpret_cast<unsigned long long*>(y);
   const uint64_t h = min(n, (uint64_t)((((uintptr_t)y & 15) >> 3)));
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  if (tid < h) y[tid] = dq(q[tid]);
+  if (tid < h) yb[tid] = dq(q[tid]);
   const int4* q4 = reinterpret_cast<const int4*>(q + h);
-  double2* y2 = reinterpret_cast<double2*>(y + h);
+  ulonglong2* y2 = reinterpret_cast<ulonglong2*>(yb + h);
   const uint64_t n4 = (n - h) >> 2;
   for (uint64_t i = tid; i < n4; i += stride) {
     const int4 v = __ldcs(q4 + i);
-    __stcs(y2 + 2 * i, make_double2(dq(v.x), dq(v.y)));
-    __stcs(y2 + 2 * i + 1, make_double2(dq(v.z), dq(v.w)));
+    __stcs(y2 + 2 * i, make_ulonglong2(dq(v.x), dq(v.y)));
+    __stcs(y2 + 2 * i + 1, make_ulonglong2(dq(v.z), dq(v.w)));
   }
-  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) y[i] = dq(q[i]);
+  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) yb[i] = dq(q[i]);
 }
 
 cudaError_t launch_dequant_f64(const int32_t* q, double* y, uint64_t n, const DecPlan* plan, uint32_t sm_count,
