@@ -828,12 +828,12 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
     eb = a.eb_dev ? *a.eb_dev : a.eb;
     inv = __fdiv_rn(1.0f, eb);
   }
-  f64i::Operand invo{};  // 1/eb's fields for the integer float64 quantizer
-  if constexpr (DBL) invo = f64i::unpack(f64i::bits_of(inv));
+  f64i::Inverse invo{};  // 1/eb's fields for the integer float64 quantizer
+  if constexpr (DBL) invo = f64i::prepare_inverse(f64i::bits_of(inv));
   auto qz = [&](LT v) -> int32_t {
     if constexpr (DBL) {
       bool bad = false;
-      const int32_t q = f64i::quantize(v, invo, bad);
+      const int32_t q = f64i::quantize_fast(v, invo, bad);
       if (bad) flags |= kErrQuantRange;
       return q;
     } else {
@@ -1534,26 +1534,26 @@ cudaError_t launch_rel_bound_f64(const RelArgs& a, uint32_t grid, cudaStream_t s
 __global__ void __launch_bounds__(256) quantize_f64_kernel(const double* __restrict__ x, int32_t* __restrict__ q,
                                                            uint64_t n, double invd, const double* invd_dev,
                                                            uint32_t* err) {
-  const f64i::Operand io = f64i::unpack(f64i::bits_of(invd_dev ? *invd_dev : invd));
+  const f64i::Inverse io = f64i::prepare_inverse(f64i::bits_of(invd_dev ? *invd_dev : invd));
   bool bad = false;
   const uint64_t h = min(n, (uint64_t)((((uintptr_t)x & 15) >> 3)));
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const unsigned long long* xb = reinterpret_cast<const unsigned long long*>(x);  // bits, see f64_key
-  if (tid < h) q[tid] = f64i::quantize(xb[tid], io, bad);
+  if (tid < h) q[tid] = f64i::quantize_fast(xb[tid], io, bad);
   const ulonglong2* x2 = reinterpret_cast<const ulonglong2*>(xb + h);
   int4* q4 = reinterpret_cast<int4*>(q + h);
   const uint64_t n4 = (n - h) >> 2;
   for (uint64_t i = tid; i < n4; i += stride) {
     const ulonglong2 u = __ldcs(x2 + 2 * i), v = __ldcs(x2 + 2 * i + 1);
     int4 r;
-    r.x = f64i::quantize(u.x, io, bad);
-    r.y = f64i::quantize(u.y, io, bad);
-    r.z = f64i::quantize(v.x, io, bad);
-    r.w = f64i::quantize(v.y, io, bad);
+    r.x = f64i::quantize_fast(u.x, io, bad);
+    r.y = f64i::quantize_fast(u.y, io, bad);
+    r.z = f64i::quantize_fast(v.x, io, bad);
+    r.w = f64i::quantize_fast(v.y, io, bad);
     q4[i] = r;
   }
-  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) q[i] = f64i::quantize(xb[i], io, bad);
+  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) q[i] = f64i::quantize_fast(xb[i], io, bad);
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, kErrQuantRange);
 }
 

@@ -139,6 +139,55 @@ SZP_F64_FN int32_t quantize(uint64_t xb, const Operand& inv, bool& bad) {
   return (int32_t)(neg ? 0u - (uint32_t)i : (uint32_t)i);
 }
 
+// 1/eb prepared for quantize_fast: significand, exponent field, sign, and
+// whether it is normal (quantize_fast needs that; otherwise quantize()).
+struct Inverse {
+  Operand op;  // for quantize()
+  uint64_t m;
+  uint32_t ef, sign;
+  bool normal;
+};
+
+SZP_F64_FN Inverse prepare_inverse(uint64_t u) {
+  Inverse v;
+  v.op = unpack(u);
+  v.m = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  v.ef = (uint32_t)(u >> 52) & 0x7FFu;
+  v.sign = (uint32_t)(u >> 63);
+  v.normal = v.ef >= 1 && v.ef <= 2046;
+  return v;
+}
+
+// quantize() in fewer steps for a normal x and a normal inverse (others take
+// quantize()).  With P = mx * mi in [2^104, 2^106) and p = P * 2^E, rounding
+// to 53 bits is adding half an ulp at bit sh (52 + [P >= 2^105]) and
+// truncating there (ties up, which as quantize() notes never moves the
+// truncated value), and truncating again at -E >= 64 composes with it:
+// trunc(RN(p)) = (P + 2^(sh-1)) >> -E, which reads only the high word of the
+// sum.
+SZP_F64_FN int32_t quantize_fast(uint64_t xb, const Inverse& inv, bool& bad) {
+  const uint32_t xh = (uint32_t)(xb >> 32);
+  const uint32_t ex = (xh >> 20) & 0x7FFu;
+  if (ex - 1u >= 0x7FEu || !inv.normal) return quantize(xb, inv.op, bad);  // zero, subnormal, inf, NaN
+  uint64_t hi, lo;
+  mul_53x53((xb & 0xFFFFFFFFFFFFFull) | (1ull << 52), inv.m, hi, lo);
+  const uint64_t half = 1ull << (51 + (uint32_t)(hi >> 41));
+  const uint64_t lo2 = lo + half;
+  const uint64_t hi2 = hi + (lo2 < lo ? 1u : 0u);
+  const int32_t k = 2086 - (int32_t)ex - (int32_t)inv.ef;  // -E - 64
+  const uint32_t neg = (xh >> 31) ^ inv.sign;
+  if (k < 0) {  // |p| >= 2^40
+    bad = true;
+    return INT32_MIN;
+  }
+  const uint64_t i = k >= 64 ? 0 : hi2 >> (uint32_t)k;
+  if (i > 0x7FFFFFFFull + neg) {
+    bad = true;
+    return INT32_MIN;
+  }
+  return (int32_t)(neg ? 0u - (uint32_t)i : (uint32_t)i);
+}
+
 // Whether dequant_bits applies to eb: eb normal and small enough that no
 // product |q| * eb with |q| <= 2^31 leaves the normal range.
 SZP_F64_FN bool dequant_fast_ok(uint64_t ebb) {
@@ -155,16 +204,18 @@ SZP_F64_FN uint64_t dequant_bits(int32_t q, uint64_t mb, uint32_t ef, uint64_t s
   uint32_t a = q < 0 ? 0u - (uint32_t)q : (uint32_t)q;  // |q| in [1, 2^31]
   const int c = clz32(a);
   a <<= c;  // [2^31, 2^32)
-  uint64_t hi, lo;
-  mul_32x53(a, mb, hi, lo);                 // P in [2^83, 2^85)
-  const uint32_t t = (uint32_t)(hi >> 20);  // P >= 2^84
-  const uint32_t sh = 31 + t;
-  uint64_t s = (hi << (33 - t)) | (lo >> sh);
-  const uint64_t r = lo & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-  s += (r > half || (r == half && (s & 1))) ? 1u : 0u;  // s in [2^52, 2^53]
-  // |q| * eb = s * 2^(sh - c + ef - 1075): biased exponent ef + sh - c; a
-  // rounded-up s = 2^53 carries into the exponent field
-  const uint64_t e = (uint64_t)(ef + sh - (uint32_t)c);
+  // P = a * mb in [2^83, 2^85) as w * 2^32 + l, w in [2^51, 2^53)
+  const uint64_t p0 = (uint64_t)a * (uint32_t)mb;
+  const uint64_t w = (uint64_t)a * (uint32_t)(mb >> 32) + (p0 >> 32);
+  const uint32_t l = (uint32_t)p0;
+  const uint32_t t = (uint32_t)(w >> 52);  // P >= 2^84: round at bit 32, else at bit 31
+  // the 53 kept bits, and the dropped bits scaled to 32 (their half is 2^31)
+  uint64_t s = t ? w : ((w << 1) | (l >> 31));
+  const uint32_t r = t ? l : (l << 1);
+  s += (r > 0x80000000u || (r == 0x80000000u && (s & 1))) ? 1u : 0u;  // s in [2^52, 2^53]
+  // |q| * eb = s * 2^(31 + t - c + ef - 1075): biased exponent ef + 31 + t - c;
+  // a rounded-up s = 2^53 carries into the exponent field
+  const uint64_t e = (uint64_t)(ef + 31 + t - (uint32_t)c);
   return sg | (((e - 1) << 52) + s);
 }
 

@@ -81,6 +81,7 @@ int main(int argc, char** argv) {
     // quantizer: one inverse per few hundred values, like one eb per field
     const double inv = rand_inv();
     const Operand io = unpack(bits_of(inv));
+    const Inverse iv = prepare_inverse(bits_of(inv));
     for (int k = 0; k < 8; k++, cases++) {
       double x = rand_double_any();
       if (k == 7) {  // a product within a few ulps of a boundary (integer or half-integer)
@@ -94,11 +95,13 @@ int main(int argc, char** argv) {
         u += (uint64_t)d;
         x = double_of(u);
       }
-      bool b1 = false, b2 = false;
+      bool b1 = false, b2 = false, b3 = false;
       const int32_t r = quantize_ref(x, inv, b1);
       const int32_t g = quantize(bits_of(x), io, b2);
-      if (r != g || b1 != b2) {
-        printf("quantize mismatch x=%a inv=%a ref=%d(%d) got=%d(%d)\n", x, inv, r, (int)b1, g, (int)b2);
+      const int32_t f = quantize_fast(bits_of(x), iv, b3);
+      if (r != g || b1 != b2 || r != f || b1 != b3) {
+        printf("quantize mismatch x=%a inv=%a ref=%d(%d) got=%d(%d) fast=%d(%d)\n", x, inv, r, (int)b1, g, (int)b2, f,
+               (int)b3);
         return 1;
       }
     }
