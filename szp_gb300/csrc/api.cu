@@ -452,7 +452,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   if (j.n && !yout) return fail(SZP_GB300_EINVAL, "null output");
   if ((uintptr_t)yout & (dbl ? 7 : 3)) return fail(SZP_GB300_EINVAL, "output not aligned to its element size");
   const bool fm2 = j.fm == 2;
-  const bool qpipe = dbl && f64_pipe_supported((uint32_t)j.L);  // pipeline to int32 q, then a pass
+  const bool qpipe = dbl && f64_pipe_supported((uint32_t)j.L);  // the pipeline, writing doubles
   Segments sg = make_segments(j.n, j.T, j.L);
   const uint32_t maxsz = fm2 ? (j.L == 1 ? 5u : 4 + block_bytes((uint32_t)j.L - 1, kMaxBitCount))
                              : max_block_bytes((uint32_t)j.L);
@@ -519,12 +519,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   if (((!dbl || qpipe) && decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) ||
       locate_smem_bytes(SC, a.overlap, maxsz) > 200 * 1024)
     return fail(SZP_GB300_EINVAL, "blockSize too large");
-  int32_t* q = nullptr;
-  if (qpipe) {
-    CU(w.qbuf.ensure((j.n + 4) * sizeof(int32_t)));
-    q = f64_q_view(w.qbuf.p, j.d_yd);
-    f.y = reinterpret_cast<float*>(q);
-  }
+  if (qpipe) f.y = reinterpret_cast<float*>(j.d_yd);  // the pipeline's output slot; it writes doubles
   CU(cudaMemsetAsync(dm->verify, 0, sizeof(uint32_t), st));
 
   w.mark(kSlotSetup, 0, st);
@@ -534,14 +529,9 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   CU(launch_locate(a, st));
   w.mark(kSlotLocate, 1, st);
   w.mark(kSlotDecode, 0, st);
-  if (qpipe) {
-    CU(launch_decode_q(a, st));
-    CU(launch_dequant_f64(q, j.d_yd, j.n, f.plan, (uint32_t)w.sm_count, st));
-  } else {
-    CU(dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
-  }
+  CU(qpipe ? launch_decode_q(a, st) : dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
   w.mark(kSlotDecode, 1, st);
-  count_launches(qpipe ? 4 : 3);
+  count_launches(3);
   return SZP_GB300_OK;
 }
 

@@ -688,7 +688,8 @@ struct DecSlot {
   uint32_t pofs;     // slot word offset of the tile's first block offset
   uint32_t seg_tile0;  // launch tile of its segment's first tile (the look-back stops there)
   float eb;          // the field's bound
-  float* y;          // the field's output
+  double ebd;        // float64 streams: the bound
+  float* y;          // the field's output (float64 streams: its doubles)
   uint32_t* err;     // the field's error word
 };
 
@@ -731,6 +732,7 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     m.seg = dt.seg;
     m.seg_tile0 = fd.tile_base + (fd.tiles_per_seg ? dt.seg * fd.tiles_per_seg : 0u);
     m.eb = fd.plan->eb;
+    m.ebd = fd.plan->ebd;
     m.y = fd.y;
     m.err = fd.err;
     m.nblk = dt.nblk;
@@ -792,11 +794,9 @@ __device__ __forceinline__ void lds_le64(const uint8_t* b, uint32_t o, uint32_t&
 // tile's nel elements starting at dst = y + e0; 16-byte stores for the aligned
 // middle, the words picked from two aligned shared-memory lines when dst is not
 // 16-byte aligned.  stage is 16-byte aligned and readable for nel + 4 words.
-// QO: the q themselves are stored (as their bits), for a float64 pass to finish.
-template <bool QO = false>
 __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
                                                   uint32_t nel, uint32_t base, float eb, bool ebsp) {
-  auto dq = [eb, ebsp](uint32_t q) -> float { return QO ? __uint_as_float(q) : dequant(q, eb, ebsp); };
+  auto dq = [eb, ebsp](uint32_t q) -> float { return dequant(q, eb, ebsp); };
   const uint32_t tid = threadIdx.x;
   if (nel == 0) return;
   const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 2) & 3);
@@ -842,6 +842,47 @@ __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const
   }
 }
 
+// (double)q * eb of float64 data as bits: integer arithmetic for every eb
+// whose products stay normal (szp_f64.h), the FP64 multiply otherwise.
+struct DequantD {
+  uint64_t m, sgn;
+  uint32_t ef;
+  bool fast, special;
+  double eb;
+  __device__ __forceinline__ explicit DequantD(double e) : eb(e) {
+    const uint64_t u = f64i::bits_of(e);
+    fast = f64i::dequant_fast_ok(u);
+    special = !isfinite(e);
+    m = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    ef = (uint32_t)(u >> 52) & 0x7FFu;
+    sgn = u & 0x8000000000000000ull;
+  }
+  __device__ __forceinline__ unsigned long long operator()(uint32_t q) const {
+    return fast ? f64i::dequant_bits((int32_t)q, m, ef, sgn) : f64i::bits_of(dequant(q, eb, special));
+  }
+};
+
+// cta_dequant_store for float64 data: y[e] = (double)(base + stage[e - e0]) * eb
+// for the tile's nel elements from dst = y + e0, 16-byte stores of two
+// results (the first result alone when dst is 8 bytes past a 16-byte
+// boundary), written as bits.
+__device__ __forceinline__ void cta_dequant_store_d(double* __restrict__ dst, const uint32_t* __restrict__ stage,
+                                                    uint32_t nel, uint32_t base, double eb) {
+  if (nel == 0) return;
+  const DequantD dq(eb);
+  const uint32_t tid = threadIdx.x;
+  unsigned long long* g = reinterpret_cast<unsigned long long*>(dst);
+  const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 3) & 1);  // results before the first 16-byte boundary
+  if (ph && tid == 0) g[0] = dq(base + stage[0]);
+  const uint32_t n2 = (nel - ph) >> 1;
+  ulonglong2* g2 = reinterpret_cast<ulonglong2*>(g + ph);
+  for (uint32_t c = tid; c < n2; c += 256) {
+    const uint32_t e = ph + 2 * c;
+    g2[c] = make_ulonglong2(dq(base + stage[e]), dq(base + stage[e + 1]));
+  }
+  if (((nel - ph) & 1) && tid == 32) g[nel - 1] = dq(base + stage[nel - 1]);
+}
+
 // Control warp c: tiles c, c + kDecControl, ... of this CTA.  Finds each
 // tile's base q (the segment's seed plus the deltas of the tiles before it) and
 // hands it to the compute warps, which finish the tile.
@@ -865,7 +906,11 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
       base = meta[s].seed;
       if (lane == 0) {
         const float eb = meta[s].eb;
-        meta[s].y[meta[s].e0 - 1] = QO ? __uint_as_float(base) : dequant(base, eb, !isfinite(eb));
+        if (QO) {
+          reinterpret_cast<unsigned long long*>(meta[s].y)[meta[s].e0 - 1] = DequantD(meta[s].ebd)(base);
+        } else {
+          meta[s].y[meta[s].e0 - 1] = dequant(base, eb, !isfinite(eb));
+        }
       }
     } else {
       base = (uint32_t)lookback_sum(a.status, tile, meta[s].seg_tile0, epoch, a.err);
@@ -879,7 +924,8 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
   }
 }
 
-// QO: y receives int32 q (float64 streams; a pass turns them into doubles).
+// QO: float64 streams; y is an array of doubles (dequantized in integer
+// arithmetic, see DequantD).
 template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false, bool QO = false>
 __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_constant__ DecArgs a,
                                                                   uint32_t slot_bytes) {
@@ -937,7 +983,12 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
     mbar_wait_or_flag(&s_based[sp_], (kp / NS) & 1, a.err);
     const float ebp = s_meta[sp_].eb;
     const uint32_t* stage = reinterpret_cast<const uint32_t*>(s_slots + (size_t)sp_ * slot_bytes + PB);
-    cta_dequant_store<QO>(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp));
+    if (QO) {
+      cta_dequant_store_d(reinterpret_cast<double*>(s_meta[sp_].y) + s_meta[sp_].e0, stage, s_meta[sp_].nel,
+                          s_base[sp_], s_meta[sp_].ebd);
+    } else {
+      cta_dequant_store(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp));
+    }
     compute_sync();  // every read of the slot is done
     if (threadIdx.x == 0) mbar_arrive(&s_empty[sp_]);
   };
@@ -1103,7 +1154,11 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       }
       compute_sync();
       const float ebp = s_meta[s].eb;
-      cta_dequant_store<QO>(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
+      if (QO) {
+        cta_dequant_store_d(reinterpret_cast<double*>(s_meta[s].y) + s_meta[s].e0, stage, nel, 0u, s_meta[s].ebd);
+      } else {
+        cta_dequant_store(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
+      }
       compute_sync();  // every read of the slot is done
       if (threadIdx.x == 0) mbar_arrive(&s_empty[s]);
       continue;
@@ -1469,7 +1524,8 @@ cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// The fastmode pipelines to int32 q (float64 streams, blockSize 8..256).
+// The fastmode pipelines for float64 streams (blockSize 8..256): a.f.y is the
+// output array of doubles.
 cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st) {
   if (a.fm2) {
     switch (dec_lanes_per_block(a.f.seg.L)) {
@@ -1491,49 +1547,6 @@ cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st) {
     case 32: return launch_dec_lanes<32, false, kDecRounds, false, true>(a, st);
     default: return cudaErrorInvalidValue;
   }
-}
-
-// float64 dequantization pass (szpd_double.cc:67,86,112's (double)q * eb):
-// y[i] from int32 q[i], four elements per step (one 16-byte load, two 16-byte
-// stores; y + h and q + h 16-byte aligned).  Integer arithmetic for every eb
-// whose products stay normal, the FP64 multiply (x86 NaN rules) otherwise.
-__global__ void __launch_bounds__(256) dequant_f64_kernel(const int32_t* __restrict__ q, double* __restrict__ y,
-                                                          uint64_t n, const DecPlan* __restrict__ plan) {
-  if (plan->bad) return;
-  const double eb = plan->ebd;
-  const uint64_t u = f64i::bits_of(eb);
-  const bool fast = f64i::dequant_fast_ok(u), ebsp = !isfinite(eb);
-  const uint64_t ebm = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52), ebs = u & 0x8000000000000000ull;
-  const uint32_t ebe = (uint32_t)(u >> 52) & 0x7FFu;
-  // the results as bits (integers end to end, no FP64 instruction on the
-  // fast path), or the FP64 multiply
-  auto dq = [&](int32_t v) -> unsigned long long {
-    return fast ? f64i::dequant_bits(v, ebm, ebe, ebs) : f64i::bits_of(dequant((uint32_t)v, eb, ebsp));
-  };
-  unsigned long long* yb = reinterpret_cast<unsigned long long*>(y);
-  const uint64_t h = min(n, (uint64_t)((((uintptr_t)y & 15) >> 3)));
-  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  if (tid < h) yb[tid] = dq(q[tid]);
-  const int4* q4 = reinterpret_cast<const int4*>(q + h);
-  ulonglong2* y2 = reinterpret_cast<ulonglong2*>(yb + h);
-  const uint64_t n4 = (n - h) >> 2;
-  for (uint64_t i = tid; i < n4; i += stride) {
-    const int4 v = __ldcs(q4 + i);
-    __stcs(y2 + 2 * i, make_ulonglong2(dq(v.x), dq(v.y)));
-    __stcs(y2 + 2 * i + 1, make_ulonglong2(dq(v.z), dq(v.w)));
-  }
-  for (uint64_t i = h + 4 * n4 + tid; i < n; i += stride) yb[i] = dq(q[i]);
-}
-
-cudaError_t launch_dequant_f64(const int32_t* q, double* y, uint64_t n, const DecPlan* plan, uint32_t sm_count,
-                               cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  const uint64_t want = (n / 4 + 255) / 256;
-  const uint64_t lim = (uint64_t)(sm_count ? sm_count : 1) * 8;
-  const uint32_t grid = (uint32_t)(want < 1 ? 1 : (want > lim ? lim : want));
-  dequant_f64_kernel<<<grid, 256, 0, st>>>(q, y, n, plan);
-  return cudaGetLastError();
 }
 
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {

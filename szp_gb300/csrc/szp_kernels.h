@@ -154,8 +154,8 @@ cudaError_t launch_compress_f64(const CompressArgs& a, bool fm2, cudaStream_t st
 cudaError_t launch_rel_bound_f64(const RelArgs& a, uint32_t grid, cudaStream_t st);
 // float64 data on the fastmode pipelines (blockSize 8..256): a pass turns x
 // into int32 q, the pipeline packs q into a stream with an 8-byte eb header
-// (a.x = q, a.ebd/a.ebd_dev the header's eb).  Decoding runs the pipeline to
-// int32 q and a pass turns q into doubles.
+// (a.x = q, a.ebd/a.ebd_dev the header's eb).  The decode pipeline writes the
+// doubles itself.
 bool f64_pipe_supported(uint32_t L);
 int32_t* f64_q_view(void* qbuf, const void* x_or_y);  // q array aligned with x (or y) on 16 bytes
 cudaError_t launch_quantize_f64(const double* x, int32_t* q, uint64_t n, double invd, const double* invd_dev,
@@ -182,9 +182,7 @@ cudaError_t launch_locate(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st);
 uint32_t decode_blocks_per_tile_f64(uint32_t L, uint32_t& bpw);
 cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st);
-cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st);  // a.f.y receives int32 q
-cudaError_t launch_dequant_f64(const int32_t* q, double* y, uint64_t n, const DecPlan* plan, uint32_t sm_count,
-                               cudaStream_t st);
+cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st);  // a.f.y: the output doubles
 // batched decompression (fastmode1, blockSize 32)
 cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStream_t st);
 cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st);
