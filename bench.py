@@ -418,11 +418,11 @@ def run_reference(args, rank, world, pg):
         "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32->int32",
-        "data": "synthetic (seeded 512^3 Fourier field, first 2^25 values)",
-        "config": {"workload": "fourier512^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip",
+        "data": "synthetic (seeded %d^3 Fourier field, first 2^25 values)" % args.side,
+        "config": {"workload": "fourier%d^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip" % args.side,
                    "n": int(xs.size), "segments": T, "block_size": L, "l2": "inputs > L2"},
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": T, "kind": "port",
-                         "sample": "2^25 floats of the 512^3 field, compress+decompress per step"},
+                         "sample": "2^25 floats of the %d^3 field, compress+decompress per step" % args.side},
         "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -662,10 +662,11 @@ def main():
             "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32->int32",
-            "data": "synthetic (seeded 512^3 Fourier field generated in HBM)",
-            "config": {"workload": "fourier512^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip",
+            "data": "synthetic (seeded %d^3 Fourier field generated in HBM)" % args.side,
+            "config": {"workload": "fourier%d^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip" % args.side,
                        "n": n, "segments": T, "block_size": L, "parallelism": "replicas",
-                       "l2": "inputs larger than L2 (512 MiB)",
+                       "l2": "inputs %s than L2 (%d MiB)" % ("larger" if 4 * n > 129e6 else "smaller",
+                                                            4 * n >> 20),
                        "ratio": {str(r): round(4.0 * n / sizes[r], 3) for r in RELS}},
             "compress_gbs": round(world * 4.0 * n / (kern["compress"]["avg_ms"] / 1e3 +
                                                     kern.get("rel_range", {"avg_ms": 0})["avg_ms"] / 1e3) / 1e9, 2),
