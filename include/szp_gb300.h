@@ -226,6 +226,19 @@ int szp_gb300_compress_dev_f64(int fastMode, const double *d_data, size_t nbEle,
 int szp_gb300_decompress_dev_f64(int fastMode, const unsigned char *d_bytes, size_t byteLength, size_t nbEle,
                                  int blockSize, int segments, double *d_out, void *stream);
 
+/* Homomorphic sum of two device streams (the hZCCL use of fZ-light streams;
+ * no reference entry point): both compressed from nbEle values with the same
+ * error bound (identical eb header bytes), blockSize (8..256), segments and
+ * fastMode, of dataType SZ_FLOAT or SZ_DOUBLE.  Writes to d_out the stream
+ * whose quantization codes are the sums of a's and b's (wrapping int32; a
+ * wrap is a notice, szp_gb300_last_notices), under the same header: it
+ * decompresses to (q_a + q_b) * eb, within 2 * eb of the sum of the two
+ * original fields.  Waits; stores the size in *outSize.  Streams with
+ * different bounds give SZP_GB300_EINVAL. */
+int szp_gb300_reduce_sum_dev(int fastMode, int dataType, const unsigned char *d_a, size_t lenA,
+                             const unsigned char *d_b, size_t lenB, size_t nbEle, int blockSize, int segments,
+                             unsigned char *d_out, size_t out_capacity, size_t *outSize, void *stream);
+
 /* Device-pointer decompressor; asynchronous on stream.  d_bytes is a whole
  * stream of byteLength bytes in device memory. */
 int szp_gb300_decompress_dev(int fastMode, const unsigned char *d_bytes, size_t byteLength, size_t nbEle,

@@ -70,6 +70,10 @@ class Port:
         lib.szo_rel_bound_d.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double]
         lib.szo_max_stream_bytes_d.restype = ctypes.c_size_t
         lib.szo_max_stream_bytes_d.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        lib.szo_reduce_sum.restype = ctypes.c_int
+        lib.szo_reduce_sum.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_size_t, _c_size_p]
         self.lib = lib
 
     def max_threads(self):
@@ -114,6 +118,21 @@ class Port:
         if rc != 0:
             raise RuntimeError("oracle decompress_d failed: %d" % rc)
         return y
+
+    def reduce_sum(self, a, b, n, L=32, T=1, mode=1, hb=4):
+        """The stream of the summed quantization codes of streams a and b
+        (same eb header, blockSize, T, mode); hb 4 for float streams, 8 for
+        double streams."""
+        ba = np.frombuffer(a, dtype=np.uint8)
+        bb = np.frombuffer(b, dtype=np.uint8)
+        cap = (self.lib.szo_max_stream_bytes_d if hb == 8 else self.lib.szo_max_stream_bytes)(n, L, T, mode)
+        out = np.empty(cap, dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        rc = self.lib.szo_reduce_sum(ba.ctypes.data, ba.size, bb.ctypes.data, bb.size, n, L, T, mode, hb,
+                                     out.ctypes.data, cap, ctypes.byref(size))
+        if rc != 0:
+            raise RuntimeError("oracle reduce_sum failed: %d" % rc)
+        return out[: size.value].tobytes()
 
     def rel_bound_d(self, x, rel):
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -125,17 +125,26 @@ static inline double dequant_d(int32_t q, double eb)
     return x86_nan_fix_d(f * eb, f, eb);
 }
 
-/* Element i of a float or double array, quantized. */
-static inline int32_t q_at(const void *x, int dbl, size_t i, double inv)
+/* Array kinds of the codec bodies: float data, double data, or the int32
+ * quantization codes themselves (the reduction below) under a float or a
+ * double stream header. */
+enum { KIND_FLOAT = 0, KIND_DOUBLE = 1, KIND_Q_F = 2, KIND_Q_D = 3 };
+static inline size_t kind_hb(int kind) { return (kind == KIND_DOUBLE || kind == KIND_Q_D) ? 8 : 4; }
+
+/* Element i of the input, quantized (codes are taken as they are). */
+static inline int32_t q_at(const void *x, int kind, size_t i, double inv)
 {
-    return dbl ? quantize_d(((const double *)x)[i], inv) : quantize(((const float *)x)[i], inv);
+    if (kind == KIND_DOUBLE) return quantize_d(((const double *)x)[i], inv);
+    if (kind == KIND_FLOAT) return quantize(((const float *)x)[i], inv);
+    return ((const int32_t *)x)[i];
 }
 
-/* y[i] = dequantized q, for a float or double output. */
-static inline void put_y(void *y, int dbl, size_t i, int32_t q, double eb)
+/* y[i] = dequantized q (or q itself for a code array). */
+static inline void put_y(void *y, int kind, size_t i, int32_t q, double eb)
 {
-    if (dbl) ((double *)y)[i] = dequant_d(q, eb);
-    else ((float *)y)[i] = dequant(q, (float)eb);
+    if (kind == KIND_DOUBLE) ((double *)y)[i] = dequant_d(q, eb);
+    else if (kind == KIND_FLOAT) ((float *)y)[i] = dequant(q, (float)eb);
+    else ((int32_t *)y)[i] = q;
 }
 
 static inline void put_u32le(unsigned char *p, uint32_t v)
@@ -312,13 +321,13 @@ static size_t encode_segment_fm2(const void *x, int dbl, size_t lo, size_t hi, d
     return w;
 }
 
-/* Compressor body for float (dbl = 0, eb header 4 bytes) or double data
- * (dbl = 1, 8 bytes); inv and the header bytes come from the caller. */
+/* Compressor body for an array of the given kind (float data: eb header 4
+ * bytes; double data: 8); inv and the header bytes come from the caller. */
 static int compress_any(const void *x, int dbl, size_t n, double inv, const unsigned char *ebb, int L, int T,
                         int mode, unsigned char *out, size_t cap, size_t *out_size)
 {
     if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || !out || !out_size) return SZO_ERR_ARG;
-    const size_t hb = dbl ? 8 : 4;
+    const size_t hb = kind_hb(dbl);
     size_t head = hb + 8 * (size_t)T;
     if (cap < head) return SZO_ERR_CAP;
     memcpy(out, ebb, hb);
@@ -445,12 +454,12 @@ static int decode_segment_fm2(const unsigned char *p, const unsigned char *end, 
     return SZO_OK;
 }
 
-/* Decompressor body: stream (len bytes, including the eb header of hb
- * bytes), explicit T.  Validates offsets against len. */
+/* Decompressor body: stream (len bytes, including the eb header of the
+ * kind's width), explicit T.  Validates offsets against len. */
 static int decompress_any(const unsigned char *stream, size_t len, size_t n, int L, int T, int mode, double eb,
                           int dbl, void *y)
 {
-    const size_t hb = dbl ? 8 : 4;
+    const size_t hb = kind_hb(dbl);
     size_t head = hb + 8 * (size_t)T;
     if (len < head) return SZO_ERR_STREAM;
     const unsigned char *data = stream + head;
@@ -502,6 +511,34 @@ int szo_decompress_d(const unsigned char *stream, size_t len, size_t n, int L, i
     double eb;
     memcpy(&eb, ebb, 8);
     return decompress_any(stream, len, n, L, T, mode, eb, 1, y);
+}
+
+/* Homomorphic sum of two streams of the same eb, blockSize, T and mode
+ * (not a reference function: the hZCCL use of fZ-light streams).  The result
+ * is the stream whose quantization codes are qa[i] + qb[i] (wrapping int32
+ * arithmetic, as the codecs' deltas wrap), under a's eb header: it
+ * decompresses to (qa[i] + qb[i]) * eb.  hb = 4 for float streams, 8 for
+ * double streams.  Headers that differ are an argument error. */
+int szo_reduce_sum(const unsigned char *a, size_t alen, const unsigned char *b, size_t blen, size_t n, int L, int T,
+                   int mode, int hb, unsigned char *out, size_t cap, size_t *out_size)
+{
+    if (L <= 0 || T <= 0 || (mode != 1 && mode != 2) || (hb != 4 && hb != 8) || !a || !b || !out || !out_size)
+        return SZO_ERR_ARG;
+    if (alen < (size_t)hb || blen < (size_t)hb) return SZO_ERR_STREAM;
+    if (memcmp(a, b, (size_t)hb) != 0) return SZO_ERR_ARG;
+    const int kind = hb == 8 ? KIND_Q_D : KIND_Q_F;
+    int32_t *qa = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    int32_t *qb = (int32_t *)malloc(sizeof(int32_t) * (n ? n : 1));
+    int rc = (qa && qb) ? SZO_OK : SZO_ERR_NOMEM;
+    if (rc == SZO_OK) rc = decompress_any(a, alen, n, L, T, mode, 0.0, kind, qa);
+    if (rc == SZO_OK) rc = decompress_any(b, blen, n, L, T, mode, 0.0, kind, qb);
+    if (rc == SZO_OK) {
+        for (size_t i = 0; i < n; i++) qa[i] = (int32_t)((uint32_t)qa[i] + (uint32_t)qb[i]);
+        rc = compress_any(qa, kind, n, 0.0, a, L, T, mode, out, cap, out_size);
+    }
+    free(qa);
+    free(qb);
+    return rc;
 }
 
 /* REL bound: serial min/max and (max-min)*(float)rel in float,

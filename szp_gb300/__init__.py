@@ -68,6 +68,8 @@ _sig("szp_gb300_compress_dev_f64", ctypes.c_int, [ctypes.c_int, _vp, _sz, ctypes
                                                   ctypes.c_double, ctypes.c_int, ctypes.c_int, _vp, _sz, _szp, _vp])
 _sig("szp_gb300_decompress_dev_f64", ctypes.c_int, [ctypes.c_int, _vp, _sz, _sz, ctypes.c_int, ctypes.c_int, _vp,
                                                     _vp])
+_sig("szp_gb300_reduce_sum_dev", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _vp, _sz, _vp, _sz, _sz, ctypes.c_int,
+                                                ctypes.c_int, _vp, _sz, _szp, _vp])
 for _n in ("szp_double_openmp_threadblock", "szp_double_openmp_threadblock_randomaccess"):
     _sig(_n, _vp, [_vp, _szp, ctypes.c_double, _sz, ctypes.c_int])
 for _n in ("szp_double_openmp_threadblock_arg", "szp_double_single_thread_arg",
@@ -364,6 +366,18 @@ def compress_dev_f64(d_data, n, d_out, capacity, err_bound_mode=ABS, abs_err_bou
                                          block_size, segments, d_out, capacity, ctypes.byref(size), stream or None)
     if rc != 0:
         raise SzpError(rc, "compress_dev_f64 failed: %s" % last_error())
+    return size.value
+
+
+def reduce_sum_dev(d_a, len_a, d_b, len_b, n, d_out, capacity, block_size=32, segments=0, fast_mode=1,
+                   data_type=SZ_FLOAT, stream=0):
+    """Homomorphic sum of two device streams of the same bound; returns the
+    result's size (szp_gb300_reduce_sum_dev)."""
+    size = ctypes.c_size_t(0)
+    rc = _lib.szp_gb300_reduce_sum_dev(fast_mode, data_type, d_a, len_a, d_b, len_b, n, block_size, segments, d_out,
+                                       capacity, ctypes.byref(size), stream or None)
+    if rc != 0:
+        raise SzpError(rc, "reduce_sum_dev failed: %s" % last_error())
     return size.value
 
 

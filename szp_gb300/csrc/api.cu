@@ -300,6 +300,11 @@ struct CompressJob {
   bool dbl = false;               // float64 data: d_xd and eb_abs_d, 8-byte eb header
   const double* d_xd = nullptr;
   double eb_abs_d = 0.0;
+  // int32 codes to pack as they are (the homomorphic reduction): ABS with
+  // eb_abs (float stream) or eb_abs_d (dbl: float64 stream), no quantization;
+  // with d_codes_add, d_codes[i] += d_codes_add[i] first (in place)
+  int32_t* d_codes = nullptr;
+  const int32_t* d_codes_add = nullptr;
 };
 
 int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
@@ -307,15 +312,18 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   if (j.T <= 0) return fail(SZP_GB300_EINVAL, "segment count must be positive");
   if (j.fm != 1 && j.fm != 2) return fail(SZP_GB300_EINVAL, "fastMode must be 1 or 2 (got %d)", j.fm);
   const bool dbl = j.dbl;
-  const void* xin = dbl ? (const void*)j.d_xd : (const void*)j.d_x;
+  const bool codes = j.d_codes != nullptr;
+  const void* xin = codes ? (const void*)j.d_codes : dbl ? (const void*)j.d_xd : (const void*)j.d_x;
   if (j.n && !xin) return fail(SZP_GB300_EINVAL, "null input");
-  if ((uintptr_t)xin & (dbl ? 7 : 3)) return fail(SZP_GB300_EINVAL, "input not aligned to its element size");
+  if ((uintptr_t)xin & (dbl && !codes ? 7 : 3)) return fail(SZP_GB300_EINVAL, "input not aligned to its element size");
+  if (codes && (j.eb_mode != ABS || !f64_pipe_supported((uint32_t)j.L)))
+    return fail(SZP_GB300_EINVAL, "code streams take blockSize 8..256 (got %d)", j.L);
   const uint64_t head = (dbl ? 8 : 4) + 8ull * j.T;
   if (j.cap < head) return fail(SZP_GB300_ECAPACITY, "output buffer smaller than the stream header");
   const bool fm2 = j.fm == 2;
   // float64 data on blockSizes the pipelines take: a quantization pass, then
   // the pipeline over int32 q
-  const bool qpipe = dbl && f64_pipe_supported((uint32_t)j.L);
+  const bool qpipe = codes || (dbl && f64_pipe_supported((uint32_t)j.L));
   Segments sg = make_segments(j.n, j.T, j.L);
   uint32_t bpw = 1;
   uint32_t tb = dbl && !qpipe ? compress_blocks_per_tile_f64((uint32_t)j.L, bpw)
@@ -350,6 +358,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   a.xd = j.d_xd;
   a.ebd = j.eb_abs_d;
   a.invd = dbl ? 1.0 / j.eb_abs_d : 0.0;  // binary64 division, as the reference's inverse
+  a.qhb = dbl ? 8 : 4;
 
   int launches = 0;
   if (j.eb_mode == REL && dbl) {
@@ -394,12 +403,19 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   size_t smem = dbl && !qpipe ? compress_smem_bytes_f64((uint32_t)j.L, tb) : compress_smem_bytes((uint32_t)j.L, tb);
   if (smem > 200 * 1024) return fail(SZP_GB300_EINVAL, "blockSize %d too large", j.L);
   int32_t* q = nullptr;
-  if (qpipe) {
+  if (qpipe && !codes) {
     CU(w.qbuf.ensure((j.n + 4) * sizeof(int32_t)));
     q = f64_q_view(w.qbuf.p, j.d_xd);
   }
   w.mark(kSlotCompress, 0, st);
-  if (qpipe) {
+  if (codes) {
+    if (j.d_codes_add) {
+      CU(launch_add_codes(j.d_codes, j.d_codes_add, j.n, a.err, (uint32_t)w.sm_count, st));
+      launches++;
+    }
+    a.x = reinterpret_cast<const float*>(j.d_codes);
+    CU(launch_compress_q(a, fm2, st));
+  } else if (qpipe) {
     CU(launch_quantize_f64(j.d_xd, q, j.n, a.invd, a.invd_dev, a.err, (uint32_t)w.sm_count, st));
     a.x = reinterpret_cast<const float*>(q);
     CU(launch_compress_q(a, fm2, st));
@@ -439,6 +455,7 @@ struct DecompressJob {
   float* d_y;
   bool dbl = false;        // float64 stream: output of doubles in d_yd (8-byte eb header)
   double* d_yd = nullptr;
+  int32_t* d_codes = nullptr;  // output of the int32 codes instead (the homomorphic reduction)
 };
 
 int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
@@ -448,11 +465,14 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   const bool dbl = j.dbl;
   const uint64_t head = (dbl ? 8 : 4) + 8ull * j.T;
   if (j.len < head) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
-  void* yout = dbl ? (void*)j.d_yd : (void*)j.d_y;
+  const bool codes = j.d_codes != nullptr;
+  void* yout = codes ? (void*)j.d_codes : dbl ? (void*)j.d_yd : (void*)j.d_y;
   if (j.n && !yout) return fail(SZP_GB300_EINVAL, "null output");
-  if ((uintptr_t)yout & (dbl ? 7 : 3)) return fail(SZP_GB300_EINVAL, "output not aligned to its element size");
+  if ((uintptr_t)yout & (dbl && !codes ? 7 : 3)) return fail(SZP_GB300_EINVAL, "output not aligned to its element size");
+  if (codes && !f64_pipe_supported((uint32_t)j.L))
+    return fail(SZP_GB300_EINVAL, "code streams take blockSize 8..256 (got %d)", j.L);
   const bool fm2 = j.fm == 2;
-  const bool qpipe = dbl && f64_pipe_supported((uint32_t)j.L);  // the pipeline, writing doubles
+  const bool qpipe = codes || (dbl && f64_pipe_supported((uint32_t)j.L));  // a pipeline writing doubles or codes
   Segments sg = make_segments(j.n, j.T, j.L);
   const uint32_t maxsz = fm2 ? (j.L == 1 ? 5u : 4 + block_bytes((uint32_t)j.L - 1, kMaxBitCount))
                              : max_block_bytes((uint32_t)j.L);
@@ -519,7 +539,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   if (((!dbl || qpipe) && decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) ||
       locate_smem_bytes(SC, a.overlap, maxsz) > 200 * 1024)
     return fail(SZP_GB300_EINVAL, "blockSize too large");
-  if (qpipe) f.y = reinterpret_cast<float*>(j.d_yd);  // the pipeline's output slot; it writes doubles
+  if (qpipe) f.y = reinterpret_cast<float*>(codes ? (void*)j.d_codes : (void*)j.d_yd);  // it writes doubles or codes
   CU(cudaMemsetAsync(dm->verify, 0, sizeof(uint32_t), st));
 
   w.mark(kSlotSetup, 0, st);
@@ -529,7 +549,8 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   CU(launch_locate(a, st));
   w.mark(kSlotLocate, 1, st);
   w.mark(kSlotDecode, 0, st);
-  CU(qpipe ? launch_decode_q(a, st) : dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
+  CU(codes ? launch_decode_codes(a, st)
+            : qpipe ? launch_decode_q(a, st) : dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
   w.mark(kSlotDecode, 1, st);
   count_launches(3);
   return SZP_GB300_OK;
@@ -1149,6 +1170,68 @@ int szp_gb300_decompress_dev_f64(int fastMode, const unsigned char* d_bytes, siz
   j.d_yd = d_out;
   rc = decompress_launch(*w, j, st);
   if (rc == SZP_GB300_OK) rc = finish_sync(*w, st, nullptr);
+  w->end(st);
+  return rc;
+}
+
+int szp_gb300_reduce_sum_dev(int fastMode, int dataType, const unsigned char* d_a, size_t lenA,
+                             const unsigned char* d_b, size_t lenB, size_t nbEle, int blockSize, int segments,
+                             unsigned char* d_out, size_t out_capacity, size_t* outSize, void* stream) {
+  clear_error();
+  if (outSize) *outSize = 0;
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  if (!d_a || !d_b || !d_out) return fail(SZP_GB300_EINVAL, "null stream");
+  if (dataType != SZ_FLOAT && dataType != SZ_DOUBLE) return fail(SZP_GB300_EINVAL, "unknown dataType %d", dataType);
+  const bool dbl = dataType == SZ_DOUBLE;
+  const size_t hb = dbl ? 8 : 4;
+  if (lenA < hb || lenB < hb) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
+  const int T = resolve_segments(segments);
+  cudaStream_t st = w->begin(stream);
+  // both error bounds, from the headers: they must be the same bytes
+  uint8_t* h = w->h_small + 16;
+  rc = SZP_GB300_OK;
+  if (cudaMemcpyAsync(h, d_a, hb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(h + 8, d_b, hb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    rc = fail(SZP_GB300_ECUDA, "reading the stream headers failed");
+  } else if (memcmp(h, h + 8, hb) != 0) {
+    rc = fail(SZP_GB300_EINVAL, "the streams were compressed with different error bounds");
+  }
+  // codes of a and b, 16-byte aligned, in the workspace
+  const size_t span = (nbEle + 3) & ~(size_t)3;
+  if (rc == SZP_GB300_OK && w->qbuf.ensure(2 * (span + 4) * sizeof(int32_t)) != cudaSuccess)
+    rc = fail(SZP_GB300_ENOMEM, "no device memory for the codes");
+  int32_t* qa = rc == SZP_GB300_OK ? w->qbuf.as<int32_t>() : nullptr;
+  int32_t* qb = qa ? qa + span + 4 : nullptr;
+  for (int k = 0; k < 2 && rc == SZP_GB300_OK; k++) {
+    DecompressJob d{k ? d_b : d_a, k ? lenB : lenA, nullptr, nbEle, blockSize, T, fastMode, nullptr};
+    d.dbl = dbl;
+    d.d_codes = k ? qb : qa;
+    rc = decompress_launch(*w, d, st);
+    if (rc == SZP_GB300_OK) rc = finish_sync(*w, st, nullptr);  // each decode reports its own errors
+  }
+  if (rc == SZP_GB300_OK) {
+    CompressJob c{nullptr, nbEle, ABS, 0.0f, 0.0, blockSize, T, fastMode, d_out, out_capacity, nullptr};
+    c.dbl = dbl;
+    c.d_codes = qa;
+    c.d_codes_add = qb;
+    if (dbl) {
+      uint64_t u = 0;
+      for (int i = 0; i < 8; i++) u = (u << 8) | h[i];
+      memcpy(&c.eb_abs_d, &u, 8);
+    } else {
+      const uint32_t u = ((uint32_t)h[0] << 24) | ((uint32_t)h[1] << 16) | ((uint32_t)h[2] << 8) | h[3];
+      memcpy(&c.eb_abs, &u, 4);
+    }
+    rc = compress_launch(*w, c, st);
+    if (rc == SZP_GB300_OK) {
+      size_t sz = 0;
+      rc = finish_sync(*w, st, &sz);
+      if (outSize) *outSize = sz;
+    }
+  }
   w->end(st);
   return rc;
 }

@@ -794,9 +794,12 @@ __device__ __forceinline__ void lds_le64(const uint8_t* b, uint32_t o, uint32_t&
 // tile's nel elements starting at dst = y + e0; 16-byte stores for the aligned
 // middle, the words picked from two aligned shared-memory lines when dst is not
 // 16-byte aligned.  stage is 16-byte aligned and readable for nel + 4 words.
+// CODES: the quantization codes themselves are stored (their bits), for the
+// homomorphic reduction.
+template <bool CODES = false>
 __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
                                                   uint32_t nel, uint32_t base, float eb, bool ebsp) {
-  auto dq = [eb, ebsp](uint32_t q) -> float { return dequant(q, eb, ebsp); };
+  auto dq = [eb, ebsp](uint32_t q) -> float { return CODES ? __uint_as_float(q) : dequant(q, eb, ebsp); };
   const uint32_t tid = threadIdx.x;
   if (nel == 0) return;
   const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 2) & 3);
@@ -886,7 +889,11 @@ __device__ __forceinline__ void cta_dequant_store_d(double* __restrict__ dst, co
 // Control warp c: tiles c, c + kDecControl, ... of this CTA.  Finds each
 // tile's base q (the segment's seed plus the deltas of the tiles before it) and
 // hands it to the compute warps, which finish the tile.
-template <int NS, int NC, bool QO = false>
+// Output kinds of the decode pipeline: floats, doubles (float64 streams,
+// dequantized in integer arithmetic, see DequantD), or the int32 codes.
+enum { kOutFloat = 0, kOutDouble = 1, kOutCodes = 2 };
+
+template <int NS, int NC, int OUT = kOutFloat>
 __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSlot* meta, const uint32_t* s_agg,
                                             uint32_t* s_base, uint64_t* full, uint64_t* aggb, uint64_t* based,
                                             const uint32_t* s_epoch, const volatile uint32_t* s_stop_k) {
@@ -906,8 +913,10 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
       base = meta[s].seed;
       if (lane == 0) {
         const float eb = meta[s].eb;
-        if (QO) {
+        if (OUT == kOutDouble) {
           reinterpret_cast<unsigned long long*>(meta[s].y)[meta[s].e0 - 1] = DequantD(meta[s].ebd)(base);
+        } else if (OUT == kOutCodes) {
+          meta[s].y[meta[s].e0 - 1] = __uint_as_float(base);
         } else {
           meta[s].y[meta[s].e0 - 1] = dequant(base, eb, !isfinite(eb));
         }
@@ -924,9 +933,9 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
   }
 }
 
-// QO: float64 streams; y is an array of doubles (dequantized in integer
-// arithmetic, see DequantD).
-template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false, bool QO = false>
+// OUT: what y holds (kOutFloat, kOutDouble: an array of doubles, kOutCodes:
+// int32 codes).
+template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false, int OUT = kOutFloat>
 __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_constant__ DecArgs a,
                                                                   uint32_t slot_bytes) {
   constexpr int NS = kDecSlots, NC = kDecControl, WARPS = 8;
@@ -969,7 +978,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
   if (warp >= WARPS) {
     // fastmode2 blocks carry their own seeds: no look-back, nothing to control
     if (!FM2)
-      dec_control<NS, NC, QO>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
+      dec_control<NS, NC, OUT>(warp - WARPS, a, s_meta, s_agg, s_base, s_full, s_aggb, s_based, &s_epoch, &s_stop_k);
     return;
   }
 
@@ -983,11 +992,12 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
     mbar_wait_or_flag(&s_based[sp_], (kp / NS) & 1, a.err);
     const float ebp = s_meta[sp_].eb;
     const uint32_t* stage = reinterpret_cast<const uint32_t*>(s_slots + (size_t)sp_ * slot_bytes + PB);
-    if (QO) {
+    if (OUT == kOutDouble) {
       cta_dequant_store_d(reinterpret_cast<double*>(s_meta[sp_].y) + s_meta[sp_].e0, stage, s_meta[sp_].nel,
                           s_base[sp_], s_meta[sp_].ebd);
     } else {
-      cta_dequant_store(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp));
+      cta_dequant_store<OUT == kOutCodes>(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp,
+                                          !isfinite(ebp));
     }
     compute_sync();  // every read of the slot is done
     if (threadIdx.x == 0) mbar_arrive(&s_empty[sp_]);
@@ -1154,10 +1164,10 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       }
       compute_sync();
       const float ebp = s_meta[s].eb;
-      if (QO) {
+      if (OUT == kOutDouble) {
         cta_dequant_store_d(reinterpret_cast<double*>(s_meta[s].y) + s_meta[s].e0, stage, nel, 0u, s_meta[s].ebd);
       } else {
-        cta_dequant_store(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
+        cta_dequant_store<OUT == kOutCodes>(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
       }
       compute_sync();  // every read of the slot is done
       if (threadIdx.x == 0) mbar_arrive(&s_empty[s]);
@@ -1480,9 +1490,9 @@ static uint32_t dec_slot_bytes(uint32_t L, uint32_t tb, uint32_t maxsz) {
   return (uint32_t)((dec_pos_bytes(tb) + (span > stage ? span : stage) + 15) & ~(size_t)15);
 }
 
-template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds, bool FM2 = false, bool QO = false>
+template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds, bool FM2 = false, int OUT = kOutFloat>
 static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
-  auto k = decode_pipe<LPB, BATCH, ROUNDS, FM2, QO>;
+  auto k = decode_pipe<LPB, BATCH, ROUNDS, FM2, OUT>;
   const uint32_t slot = dec_slot_bytes(8 * LPB, a.tb, a.maxsz);
   const size_t smem = (size_t)kDecSlots * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
@@ -1529,22 +1539,46 @@ cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st) {
 cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st) {
   if (a.fm2) {
     switch (dec_lanes_per_block(a.f.seg.L)) {
-      case 1: return launch_dec_lanes<1, false, kDecRounds, true, true>(a, st);
-      case 2: return launch_dec_lanes<2, false, kDecRounds, true, true>(a, st);
-      case 4: return launch_dec_lanes<4, false, kDecRounds, true, true>(a, st);
-      case 8: return launch_dec_lanes<8, false, kDecRounds, true, true>(a, st);
-      case 16: return launch_dec_lanes<16, false, kDecRounds, true, true>(a, st);
-      case 32: return launch_dec_lanes<32, false, kDecRounds, true, true>(a, st);
+      case 1: return launch_dec_lanes<1, false, kDecRounds, true, kOutDouble>(a, st);
+      case 2: return launch_dec_lanes<2, false, kDecRounds, true, kOutDouble>(a, st);
+      case 4: return launch_dec_lanes<4, false, kDecRounds, true, kOutDouble>(a, st);
+      case 8: return launch_dec_lanes<8, false, kDecRounds, true, kOutDouble>(a, st);
+      case 16: return launch_dec_lanes<16, false, kDecRounds, true, kOutDouble>(a, st);
+      case 32: return launch_dec_lanes<32, false, kDecRounds, true, kOutDouble>(a, st);
       default: return cudaErrorInvalidValue;
     }
   }
   switch (dec_lanes_per_block(a.f.seg.L)) {
-    case 1: return launch_dec_lanes<1, false, kDecRounds, false, true>(a, st);
-    case 2: return launch_dec_lanes<2, false, kDecRounds, false, true>(a, st);
-    case 4: return launch_dec_lanes<4, false, kDecRounds, false, true>(a, st);
-    case 8: return launch_dec_lanes<8, false, kDecRounds, false, true>(a, st);
-    case 16: return launch_dec_lanes<16, false, kDecRounds, false, true>(a, st);
-    case 32: return launch_dec_lanes<32, false, kDecRounds, false, true>(a, st);
+    case 1: return launch_dec_lanes<1, false, kDecRounds, false, kOutDouble>(a, st);
+    case 2: return launch_dec_lanes<2, false, kDecRounds, false, kOutDouble>(a, st);
+    case 4: return launch_dec_lanes<4, false, kDecRounds, false, kOutDouble>(a, st);
+    case 8: return launch_dec_lanes<8, false, kDecRounds, false, kOutDouble>(a, st);
+    case 16: return launch_dec_lanes<16, false, kDecRounds, false, kOutDouble>(a, st);
+    case 32: return launch_dec_lanes<32, false, kDecRounds, false, kOutDouble>(a, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// The fastmode pipelines writing the int32 codes to a.f.y (blockSize 8..256).
+cudaError_t launch_decode_codes(const DecArgs& a, cudaStream_t st) {
+  if (a.fm2) {
+    switch (dec_lanes_per_block(a.f.seg.L)) {
+      case 1: return launch_dec_lanes<1, false, kDecRounds, true, kOutCodes>(a, st);
+      case 2: return launch_dec_lanes<2, false, kDecRounds, true, kOutCodes>(a, st);
+      case 4: return launch_dec_lanes<4, false, kDecRounds, true, kOutCodes>(a, st);
+      case 8: return launch_dec_lanes<8, false, kDecRounds, true, kOutCodes>(a, st);
+      case 16: return launch_dec_lanes<16, false, kDecRounds, true, kOutCodes>(a, st);
+      case 32: return launch_dec_lanes<32, false, kDecRounds, true, kOutCodes>(a, st);
+      default: return cudaErrorInvalidValue;
+    }
+  }
+  switch (dec_lanes_per_block(a.f.seg.L)) {
+    case 1: return launch_dec_lanes<1, false, kDecRounds, false, kOutCodes>(a, st);
+    case 2: return launch_dec_lanes<2, false, kDecRounds, false, kOutCodes>(a, st);
+    case 4: return launch_dec_lanes<4, false, kDecRounds, false, kOutCodes>(a, st);
+    case 8: return launch_dec_lanes<8, false, kDecRounds, false, kOutCodes>(a, st);
+    case 16: return launch_dec_lanes<16, false, kDecRounds, false, kOutCodes>(a, st);
+    case 32: return launch_dec_lanes<32, false, kDecRounds, false, kOutCodes>(a, st);
     default: return cudaErrorInvalidValue;
   }
 }
