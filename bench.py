@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-fm2", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--no-reduce", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serving-window", type=float, default=0.2, help="seconds of arrivals per rate")
     ap.add_argument("--batched-fields", type=int, default=1024)
@@ -638,6 +639,41 @@ def main():
                "kernels_ms": {k: round(v, 4) for k, v in avg.items()}}
         del xd, yd, d_sd
 
+    # homomorphic sum of two streams: the field and its mirror image
+    # at one ABS bound: device time of both decodes, the add and the encode
+    reduce = None
+    if not args.no_reduce:
+        ebr = 1e-3 * float(x.max() - x.min())
+        x2 = torch.flip(x, [0])
+        capr = szp.max_stream_bytes(n, L, T, 1)
+        bufs = [torch.empty(capr, dtype=torch.uint8, device=dev) for _ in range(3)]
+        szr = [szp.compress_dev(v.data_ptr(), n, b.data_ptr(), capr, szp.ABS, ebr, 0.0, L, T, 1, st)
+               for v, b in zip((x, x2), bufs)]
+        del x2
+        szp.set_timing(True)
+        wall = []
+        for i in range(4):
+            if i == 1:
+                torch.cuda.synchronize()
+                for slot in range(5):
+                    szp.kernel_time(slot)  # drop the first
+            t0 = time.perf_counter()
+            szo = szp.reduce_sum_dev(bufs[0].data_ptr(), szr[0], bufs[1].data_ptr(), szr[1], n, bufs[2].data_ptr(),
+                                     capr, L, T, 1, szp.SZ_FLOAT, st)
+            if i:
+                wall.append(time.perf_counter() - t0)
+        kt = {name: szp.kernel_time(slot) for slot, name in
+              enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
+        szp.set_timing(False)
+        dev_ms = sum(v[0] for v in kt.values()) / 3
+        reduce = {"bound": "ABS 1e-3 of the range", "inputs": "the field and its mirror image along the first axis",
+                  "stream_bytes": [int(szr[0]), int(szr[1]), int(szo)],
+                  "kernels_ms_per_sum": {k: round(v[0] / 3, 4) for k, v in kt.items() if v[1]},
+                  "device_ms": round(dev_ms, 4), "wall_ms": round(1e3 * min(wall), 4),
+                  "fields_gbs": round(2 * 4.0 * n / (dev_ms / 1e3) / 1e9, 2),
+                  "metric": "uncompressed bytes of both fields per device time of the sum"}
+        del bufs
+
     batched = None
     if not args.no_batched:
         batched = batched_workload(szp, torch, dev, T, args.batched_fields)
@@ -678,6 +714,7 @@ def main():
             "e2e": e2e,
             "fastmode2": fm2,
             "float64": f64,
+            "reduce": reduce,
             "batched": batched,
             "serving": serving,
             "gpu_launches": int(launches),
