@@ -379,6 +379,17 @@ def dist_setup(args):
     return rank, world, local, pg
 
 
+def max_over_ranks(pg, value, device="cpu"):
+    """The largest of every rank's value (the job's time is its slowest
+    replica's); the value itself on one process."""
+    if not pg:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def field(side, seed, device):
     from szp_gb300.workloads import fourier3d_torch
     return fourier3d_torch(side, seed, device=device)
@@ -496,10 +507,7 @@ def main():
     ktimes = {name: szp.kernel_time(slot) for slot, name in
               enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
     szp.set_timing(False)
-    if pg:
-        t = torch.tensor([ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(pg, ms, dev)
 
     mean_out = float(np.mean([sizes[RELS[i % 3]] for i in range(args.steps)]))
     gbs = world * 4.0 * n * args.steps / (ms / 1e3) / 1e9
