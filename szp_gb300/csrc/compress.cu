@@ -1599,10 +1599,12 @@ cudaError_t launch_add_codes(int32_t* qa, const int32_t* qb, uint64_t n, uint32_
   return cudaGetLastError();
 }
 
-// qbuf holds n + 4 int32; the view starts 0-3 elements in so that the q of
-// element i shares its 16-byte phase with x[i] (doubles: phase 0 or 8 bytes).
-int32_t* f64_q_view(void* qbuf, const void* xy) {
-  const uint32_t h = ((uintptr_t)xy & 15) ? 1u : 0u;  // elements before the first 16-byte boundary
+// qbuf (16-byte aligned) holds n + 4 int32; the view starts 0 or 3 elements
+// in so that q + h and x + h are both 16-byte aligned, h being the doubles
+// before x's first 16-byte boundary (0 or 1): the quantization pass then
+// moves whole vectors.
+int32_t* f64_q_view(void* qbuf, const void* x) {
+  const uint32_t h = ((uintptr_t)x & 15) ? 1u : 0u;
   return reinterpret_cast<int32_t*>(qbuf) + ((4 - h) & 3);
 }
 

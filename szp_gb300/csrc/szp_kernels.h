@@ -160,7 +160,7 @@ cudaError_t launch_rel_bound_f64(const RelArgs& a, uint32_t grid, cudaStream_t s
 // (a.x = q, a.ebd/a.ebd_dev the header's eb).  The decode pipeline writes the
 // doubles itself.
 bool f64_pipe_supported(uint32_t L);
-int32_t* f64_q_view(void* qbuf, const void* x_or_y);  // q array aligned with x (or y) on 16 bytes
+int32_t* f64_q_view(void* qbuf, const void* x);  // q array whose 16-byte boundaries match x's
 cudaError_t launch_quantize_f64(const double* x, int32_t* q, uint64_t n, double invd, const double* invd_dev,
                                 uint32_t* err, uint32_t sm_count, cudaStream_t st);
 cudaError_t launch_compress_q(const CompressArgs& a, bool fm2, cudaStream_t st);
