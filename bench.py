@@ -408,6 +408,42 @@ def cpu_port_roundtrip(port, x, rel, T, reps=1):
     return best
 
 
+def cpu_row_baselines(port, xs, T, reps=2):
+    """The oracle on the host cores for the rows beyond fastmode1, on bounded
+    samples: fastmode2 and the homomorphic sum on xs (floats), float64 on the
+    first 2^24 values of xs as doubles.  GB/s of uncompressed input."""
+    def best(fn):
+        fn()
+        t = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            t.append(time.perf_counter() - t0)
+        return min(t)
+    out = {}
+
+    def fm2():
+        eb = port.rel_bound(xs, 1e-3)
+        s = port.compress(xs, eb, L, T, 2)
+        port.decompress(s, xs.size, L, T, 2)
+    out["fastmode2"] = {"gbs": round(4.0 * xs.size / best(fm2) / 1e9, 3),
+                        "sample": "%d floats, REL 1e-3 round trip" % xs.size}
+    xd = xs[: 1 << 24].astype(np.float64)
+
+    def f64():
+        eb = port.rel_bound_d(xd, 1e-6)
+        s = port.compress_d(xd, eb, L, T, 1)
+        port.decompress_d(s, xd.size, L, T, 1)
+    out["float64"] = {"gbs": round(8.0 * xd.size / best(f64) / 1e9, 3),
+                      "sample": "%d doubles, REL 1e-6 round trip" % xd.size}
+    eb = 1e-3 * float(xs.max() - xs.min())
+    sa = port.compress(xs, eb, L, T, 1)
+    sb = port.compress(np.ascontiguousarray(xs[::-1]), eb, L, T, 1)
+    out["reduce"] = {"gbs": round(8.0 * xs.size / best(lambda: port.reduce_sum(sa, sb, xs.size, L, T, 1, 4)) / 1e9, 3),
+                     "sample": "two streams of %d floats" % xs.size}
+    return out
+
+
 def run_reference(args, rank, world, pg):
     """The reference's CPU algorithm on the host cores (rank 0 only)."""
     if rank != 0:
@@ -647,7 +683,7 @@ def main():
                "kernels_ms": {k: round(v, 4) for k, v in avg.items()}}
         del xd, yd, d_sd
 
-    # homomorphic sum of two streams: the field and its mirror image
+    # homomorphic sum of two streams: the field and its values reversed
     # at one ABS bound: device time of both decodes, the add and the encode
     reduce = None
     if not args.no_reduce:
@@ -674,7 +710,7 @@ def main():
               enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
         szp.set_timing(False)
         dev_ms = sum(v[0] for v in kt.values()) / 3
-        reduce = {"bound": "ABS 1e-3 of the range", "inputs": "the field and its mirror image along the first axis",
+        reduce = {"bound": "ABS 1e-3 of the range", "inputs": "the field and its values in reverse order",
                   "stream_bytes": [int(szr[0]), int(szr[1]), int(szo)],
                   "kernels_ms_per_sum": {k: round(v[0] / 3, 4) for k, v in kt.items() if v[1]},
                   "device_ms": round(dev_ms, 4), "wall_ms": round(1e3 * min(wall), 4),
@@ -700,6 +736,11 @@ def main():
         sec = cpu_port_roundtrip(port, xs, 1e-3, Tc, reps=3)
         cpu = {"value": round(4.0 * xs.size / sec / 1e9, 3), "unit": "GB/s", "cores": Tc, "kind": "port",
                "sample": "2^25 floats of the field, REL 1e-3 round trip, best of 3"}
+        # the oracle beside each further row's GPU number
+        rows = cpu_row_baselines(port, xs, Tc)
+        for key, leg in (("fastmode2", fm2), ("float64", f64), ("reduce", reduce)):
+            if leg is not None:
+                leg["cpu_port"] = rows[key]
 
     if rank == 0:
         line = {

@@ -301,10 +301,8 @@ struct CompressJob {
   const double* d_xd = nullptr;
   double eb_abs_d = 0.0;
   // int32 codes to pack as they are (the homomorphic reduction): ABS with
-  // eb_abs (float stream) or eb_abs_d (dbl: float64 stream), no quantization;
-  // with d_codes_add, d_codes[i] += d_codes_add[i] first (in place)
-  int32_t* d_codes = nullptr;
-  const int32_t* d_codes_add = nullptr;
+  // eb_abs (float stream) or eb_abs_d (dbl: float64 stream), no quantization
+  const int32_t* d_codes = nullptr;
 };
 
 int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
@@ -409,10 +407,6 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   }
   w.mark(kSlotCompress, 0, st);
   if (codes) {
-    if (j.d_codes_add) {
-      CU(launch_add_codes(j.d_codes, j.d_codes_add, j.n, a.err, (uint32_t)w.sm_count, st));
-      launches++;
-    }
     a.x = reinterpret_cast<const float*>(j.d_codes);
     CU(launch_compress_q(a, fm2, st));
   } else if (qpipe) {
@@ -456,6 +450,7 @@ struct DecompressJob {
   bool dbl = false;        // float64 stream: output of doubles in d_yd (8-byte eb header)
   double* d_yd = nullptr;
   int32_t* d_codes = nullptr;  // output of the int32 codes instead (the homomorphic reduction)
+  bool accumulate = false;     // ... added to the codes already in d_codes
 };
 
 int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
@@ -549,7 +544,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   CU(launch_locate(a, st));
   w.mark(kSlotLocate, 1, st);
   w.mark(kSlotDecode, 0, st);
-  CU(codes ? launch_decode_codes(a, st)
+  CU(codes ? launch_decode_codes(a, j.accumulate, st)
             : qpipe ? launch_decode_q(a, st) : dbl ? launch_decode_f64(a, st) : launch_decode(a, st));
   w.mark(kSlotDecode, 1, st);
   count_launches(3);
@@ -1199,24 +1194,23 @@ int szp_gb300_reduce_sum_dev(int fastMode, int dataType, const unsigned char* d_
   } else if (memcmp(h, h + 8, hb) != 0) {
     rc = fail(SZP_GB300_EINVAL, "the streams were compressed with different error bounds");
   }
-  // codes of a and b, 16-byte aligned, in the workspace
-  const size_t span = (nbEle + 3) & ~(size_t)3;
-  if (rc == SZP_GB300_OK && w->qbuf.ensure(2 * (span + 4) * sizeof(int32_t)) != cudaSuccess)
+  // the codes, in the workspace: a's, then b's added to them by its decode
+  if (rc == SZP_GB300_OK && w->qbuf.ensure((nbEle + 4) * sizeof(int32_t)) != cudaSuccess)
     rc = fail(SZP_GB300_ENOMEM, "no device memory for the codes");
-  int32_t* qa = rc == SZP_GB300_OK ? w->qbuf.as<int32_t>() : nullptr;
-  int32_t* qb = qa ? qa + span + 4 : nullptr;
+  int32_t* q = rc == SZP_GB300_OK ? w->qbuf.as<int32_t>() : nullptr;
   for (int k = 0; k < 2 && rc == SZP_GB300_OK; k++) {
     DecompressJob d{k ? d_b : d_a, k ? lenB : lenA, nullptr, nbEle, blockSize, T, fastMode, nullptr};
     d.dbl = dbl;
-    d.d_codes = k ? qb : qa;
+    d.d_codes = q;
+    d.accumulate = k == 1;
     rc = decompress_launch(*w, d, st);
     if (rc == SZP_GB300_OK) rc = finish_sync(*w, st, nullptr);  // each decode reports its own errors
   }
+  const bool wrapped = t_notices != 0;  // a sum that wrapped (b's decode added the codes)
   if (rc == SZP_GB300_OK) {
     CompressJob c{nullptr, nbEle, ABS, 0.0f, 0.0, blockSize, T, fastMode, d_out, out_capacity, nullptr};
     c.dbl = dbl;
-    c.d_codes = qa;
-    c.d_codes_add = qb;
+    c.d_codes = q;
     if (dbl) {
       uint64_t u = 0;
       for (int i = 0; i < 8; i++) u = (u << 8) | h[i];
@@ -1230,6 +1224,7 @@ int szp_gb300_reduce_sum_dev(int fastMode, int dataType, const unsigned char* d_
       size_t sz = 0;
       rc = finish_sync(*w, st, &sz);
       if (outSize) *outSize = sz;
+      if (wrapped) t_notices = 1;
     }
   }
   w->end(st);

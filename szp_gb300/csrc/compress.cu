@@ -1560,45 +1560,6 @@ __global__ void __launch_bounds__(256) quantize_f64_kernel(const double* __restr
 
 bool f64_pipe_supported(uint32_t L) { return lanes_per_block(L) != 0; }
 
-// Homomorphic reduction: qa[i] += qb[i] in wrapping int32 arithmetic, four
-// codes per step (both arrays 16-byte aligned); a sum that wraps sets the
-// quantization flag (its stream still holds the wrapped codes).
-__global__ void __launch_bounds__(256) add_codes_kernel(int32_t* __restrict__ qa, const int32_t* __restrict__ qb,
-                                                        uint64_t n, uint32_t* err) {
-  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  bool wrap = false;
-  auto add = [&wrap](int32_t x, int32_t y) -> int32_t {
-    const int32_t z = (int32_t)((uint32_t)x + (uint32_t)y);
-    wrap |= ((x ^ z) & (y ^ z)) < 0;  // both operands' sign differs from the sum's
-    return z;
-  };
-  const uint64_t n4 = n >> 2;
-  int4* a4 = reinterpret_cast<int4*>(qa);
-  const int4* b4 = reinterpret_cast<const int4*>(qb);
-  for (uint64_t i = tid; i < n4; i += stride) {
-    int4 x = a4[i];
-    const int4 y = __ldcs(b4 + i);
-    x.x = add(x.x, y.x);
-    x.y = add(x.y, y.y);
-    x.z = add(x.z, y.z);
-    x.w = add(x.w, y.w);
-    a4[i] = x;
-  }
-  for (uint64_t i = 4 * n4 + tid; i < n; i += stride) qa[i] = add(qa[i], qb[i]);
-  if (__any_sync(0xffffffffu, wrap) && (threadIdx.x & 31) == 0) atomicOr(err, kErrQuantRange);
-}
-
-cudaError_t launch_add_codes(int32_t* qa, const int32_t* qb, uint64_t n, uint32_t* err, uint32_t sm_count,
-                             cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  const uint64_t want = (n / 4 + 255) / 256;
-  const uint64_t lim = (uint64_t)(sm_count ? sm_count : 1) * 8;
-  const uint32_t grid = (uint32_t)(want < 1 ? 1 : (want > lim ? lim : want));
-  add_codes_kernel<<<grid, 256, 0, st>>>(qa, qb, n, err);
-  return cudaGetLastError();
-}
-
 // qbuf (16-byte aligned) holds n + 4 int32; the view starts 0 or 3 elements
 // in so that q + h and x + h are both 16-byte aligned, h being the doubles
 // before x's first 16-byte boundary (0 or 1): the quantization pass then

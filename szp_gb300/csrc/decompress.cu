@@ -795,11 +795,21 @@ __device__ __forceinline__ void lds_le64(const uint8_t* b, uint32_t o, uint32_t&
 // middle, the words picked from two aligned shared-memory lines when dst is not
 // 16-byte aligned.  stage is 16-byte aligned and readable for nel + 4 words.
 // CODES: the quantization codes themselves are stored (their bits), for the
-// homomorphic reduction.
-template <bool CODES = false>
+// homomorphic reduction; with ACC they are added to the codes already in dst
+// (wrapping int32; a wrap sets kErrQuantRange in *err).
+template <bool CODES = false, bool ACC = false>
 __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const uint32_t* __restrict__ stage,
-                                                  uint32_t nel, uint32_t base, float eb, bool ebsp) {
+                                                  uint32_t nel, uint32_t base, float eb, bool ebsp,
+                                                  uint32_t* err = nullptr) {
   auto dq = [eb, ebsp](uint32_t q) -> float { return CODES ? __uint_as_float(q) : dequant(q, eb, ebsp); };
+  bool wrap = false;
+  auto acc = [&wrap](float old, uint32_t q) -> float {  // old + q as int32 codes
+    const int32_t x = (int32_t)__float_as_uint(old), y = (int32_t)q;
+    const int32_t z = (int32_t)((uint32_t)x + (uint32_t)y);
+    wrap |= ((x ^ z) & (y ^ z)) < 0;
+    return __uint_as_float((uint32_t)z);
+  };
+  auto put = [&](float* p, uint32_t q) { *p = ACC ? acc(*p, q) : dq(q); };
   const uint32_t tid = threadIdx.x;
   if (nel == 0) return;
   const uint32_t ph = (uint32_t)(((uintptr_t)dst >> 2) & 3);
@@ -807,42 +817,50 @@ __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const
   const uint32_t end = ph + nel;
   const uint32_t c0 = (ph + 3) >> 2, c1 = end >> 2;  // whole float4 chunks [c0, c1)
   if (c0 >= c1) {
-    if (tid < nel) g0[ph + tid] = dq(base + stage[tid]);
-    return;
-  }
-  if (tid < 4 * c0 - ph) g0[ph + tid] = dq(base + stage[tid]);
-  if (tid >= 32 && tid - 32 < end - 4 * c1)
-    g0[4 * c1 + tid - 32] = dq(base + stage[4 * c1 + tid - 32 - ph]);
-  const uint4* s4 = reinterpret_cast<const uint4*>(stage);
-  // four chunks per thread per pass: their shared-memory loads are in flight together
-  constexpr int U = 4;
-  for (uint32_t cb = c0; cb < c1; cb += 256 * U) {
-    uint4 w[U];
+    if (tid < nel) put(g0 + ph + tid, base + stage[tid]);
+  } else {
+    if (tid < 4 * c0 - ph) put(g0 + ph + tid, base + stage[tid]);
+    if (tid >= 32 && tid - 32 < end - 4 * c1) put(g0 + 4 * c1 + tid - 32, base + stage[4 * c1 + tid - 32 - ph]);
+    const uint4* s4 = reinterpret_cast<const uint4*>(stage);
+    // four chunks per thread per pass: their shared-memory loads are in flight together
+    constexpr int U = 4;
+    for (uint32_t cb = c0; cb < c1; cb += 256 * U) {
+      uint4 w[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      const uint32_t c = min(cb + tid + 256 * u, c1 - 1);  // clamped: always a readable chunk
-      if (ph == 0) {
-        w[u] = s4[c];
-      } else {
-        const uint4 a = s4[c - 1], b = s4[c];  // stage words [4c-4, 4c+4); chunk c wants [4c-ph, 4c-ph+4)
-        if (ph == 1) w[u] = make_uint4(a.w, b.x, b.y, b.z);
-        else if (ph == 2) w[u] = make_uint4(a.z, a.w, b.x, b.y);
-        else w[u] = make_uint4(a.y, a.z, a.w, b.x);
+      for (int u = 0; u < U; u++) {
+        const uint32_t c = min(cb + tid + 256 * u, c1 - 1);  // clamped: always a readable chunk
+        if (ph == 0) {
+          w[u] = s4[c];
+        } else {
+          const uint4 a = s4[c - 1], b = s4[c];  // stage words [4c-4, 4c+4); chunk c wants [4c-ph, 4c-ph+4)
+          if (ph == 1) w[u] = make_uint4(a.w, b.x, b.y, b.z);
+          else if (ph == 2) w[u] = make_uint4(a.z, a.w, b.x, b.y);
+          else w[u] = make_uint4(a.y, a.z, a.w, b.x);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const uint32_t c = cb + tid + 256 * u;
+        if (c < c1) {
+          float4 o;
+          if (ACC) {
+            const float4 p = reinterpret_cast<const float4*>(g0)[c];
+            o.x = acc(p.x, base + w[u].x);
+            o.y = acc(p.y, base + w[u].y);
+            o.z = acc(p.z, base + w[u].z);
+            o.w = acc(p.w, base + w[u].w);
+          } else {
+            o.x = dq(base + w[u].x);
+            o.y = dq(base + w[u].y);
+            o.z = dq(base + w[u].z);
+            o.w = dq(base + w[u].w);
+          }
+          reinterpret_cast<float4*>(g0)[c] = o;
+        }
       }
     }
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const uint32_t c = cb + tid + 256 * u;
-      if (c < c1) {
-        float4 o;
-        o.x = dq(base + w[u].x);
-        o.y = dq(base + w[u].y);
-        o.z = dq(base + w[u].z);
-        o.w = dq(base + w[u].w);
-        reinterpret_cast<float4*>(g0)[c] = o;
-      }
-    }
   }
+  if (ACC && wrap) atomicOr(err, kErrQuantRange);
 }
 
 // (double)q * eb of float64 data as bits: integer arithmetic for every eb
@@ -890,8 +908,9 @@ __device__ __forceinline__ void cta_dequant_store_d(double* __restrict__ dst, co
 // tile's base q (the segment's seed plus the deltas of the tiles before it) and
 // hands it to the compute warps, which finish the tile.
 // Output kinds of the decode pipeline: floats, doubles (float64 streams,
-// dequantized in integer arithmetic, see DequantD), or the int32 codes.
-enum { kOutFloat = 0, kOutDouble = 1, kOutCodes = 2 };
+// dequantized in integer arithmetic, see DequantD), the int32 codes, or the
+// codes added to those already in y (the homomorphic reduction).
+enum { kOutFloat = 0, kOutDouble = 1, kOutCodes = 2, kOutCodesAdd = 3 };
 
 template <int NS, int NC, int OUT = kOutFloat>
 __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSlot* meta, const uint32_t* s_agg,
@@ -917,6 +936,11 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
           reinterpret_cast<unsigned long long*>(meta[s].y)[meta[s].e0 - 1] = DequantD(meta[s].ebd)(base);
         } else if (OUT == kOutCodes) {
           meta[s].y[meta[s].e0 - 1] = __uint_as_float(base);
+        } else if (OUT == kOutCodesAdd) {
+          float* p = meta[s].y + meta[s].e0 - 1;
+          const int32_t x = (int32_t)__float_as_uint(*p), z = (int32_t)((uint32_t)x + base);
+          *p = __uint_as_float((uint32_t)z);
+          if (((x ^ z) & ((int32_t)base ^ z)) < 0) atomicOr(meta[s].err, kErrQuantRange);
         } else {
           meta[s].y[meta[s].e0 - 1] = dequant(base, eb, !isfinite(eb));
         }
@@ -996,8 +1020,9 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       cta_dequant_store_d(reinterpret_cast<double*>(s_meta[sp_].y) + s_meta[sp_].e0, stage, s_meta[sp_].nel,
                           s_base[sp_], s_meta[sp_].ebd);
     } else {
-      cta_dequant_store<OUT == kOutCodes>(s_meta[sp_].y + s_meta[sp_].e0, stage, s_meta[sp_].nel, s_base[sp_], ebp,
-                                          !isfinite(ebp));
+      cta_dequant_store<OUT >= kOutCodes, OUT == kOutCodesAdd>(s_meta[sp_].y + s_meta[sp_].e0, stage,
+                                                               s_meta[sp_].nel, s_base[sp_], ebp, !isfinite(ebp),
+                                                               s_meta[sp_].err);
     }
     compute_sync();  // every read of the slot is done
     if (threadIdx.x == 0) mbar_arrive(&s_empty[sp_]);
@@ -1167,7 +1192,8 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       if (OUT == kOutDouble) {
         cta_dequant_store_d(reinterpret_cast<double*>(s_meta[s].y) + s_meta[s].e0, stage, nel, 0u, s_meta[s].ebd);
       } else {
-        cta_dequant_store<OUT == kOutCodes>(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp, !isfinite(ebp));
+        cta_dequant_store<OUT >= kOutCodes, OUT == kOutCodesAdd>(s_meta[s].y + s_meta[s].e0, stage, nel, 0u, ebp,
+                                                                 !isfinite(ebp), s_meta[s].err);
       }
       compute_sync();  // every read of the slot is done
       if (threadIdx.x == 0) mbar_arrive(&s_empty[s]);
@@ -1559,28 +1585,34 @@ cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st) {
   }
 }
 
-// The fastmode pipelines writing the int32 codes to a.f.y (blockSize 8..256).
-cudaError_t launch_decode_codes(const DecArgs& a, cudaStream_t st) {
+// The fastmode pipelines writing the int32 codes to a.f.y, or adding them to
+// the codes there (accumulate); blockSize 8..256.
+template <int OUT>
+static cudaError_t launch_decode_codes_t(const DecArgs& a, cudaStream_t st) {
   if (a.fm2) {
     switch (dec_lanes_per_block(a.f.seg.L)) {
-      case 1: return launch_dec_lanes<1, false, kDecRounds, true, kOutCodes>(a, st);
-      case 2: return launch_dec_lanes<2, false, kDecRounds, true, kOutCodes>(a, st);
-      case 4: return launch_dec_lanes<4, false, kDecRounds, true, kOutCodes>(a, st);
-      case 8: return launch_dec_lanes<8, false, kDecRounds, true, kOutCodes>(a, st);
-      case 16: return launch_dec_lanes<16, false, kDecRounds, true, kOutCodes>(a, st);
-      case 32: return launch_dec_lanes<32, false, kDecRounds, true, kOutCodes>(a, st);
+      case 1: return launch_dec_lanes<1, false, kDecRounds, true, OUT>(a, st);
+      case 2: return launch_dec_lanes<2, false, kDecRounds, true, OUT>(a, st);
+      case 4: return launch_dec_lanes<4, false, kDecRounds, true, OUT>(a, st);
+      case 8: return launch_dec_lanes<8, false, kDecRounds, true, OUT>(a, st);
+      case 16: return launch_dec_lanes<16, false, kDecRounds, true, OUT>(a, st);
+      case 32: return launch_dec_lanes<32, false, kDecRounds, true, OUT>(a, st);
       default: return cudaErrorInvalidValue;
     }
   }
   switch (dec_lanes_per_block(a.f.seg.L)) {
-    case 1: return launch_dec_lanes<1, false, kDecRounds, false, kOutCodes>(a, st);
-    case 2: return launch_dec_lanes<2, false, kDecRounds, false, kOutCodes>(a, st);
-    case 4: return launch_dec_lanes<4, false, kDecRounds, false, kOutCodes>(a, st);
-    case 8: return launch_dec_lanes<8, false, kDecRounds, false, kOutCodes>(a, st);
-    case 16: return launch_dec_lanes<16, false, kDecRounds, false, kOutCodes>(a, st);
-    case 32: return launch_dec_lanes<32, false, kDecRounds, false, kOutCodes>(a, st);
+    case 1: return launch_dec_lanes<1, false, kDecRounds, false, OUT>(a, st);
+    case 2: return launch_dec_lanes<2, false, kDecRounds, false, OUT>(a, st);
+    case 4: return launch_dec_lanes<4, false, kDecRounds, false, OUT>(a, st);
+    case 8: return launch_dec_lanes<8, false, kDecRounds, false, OUT>(a, st);
+    case 16: return launch_dec_lanes<16, false, kDecRounds, false, OUT>(a, st);
+    case 32: return launch_dec_lanes<32, false, kDecRounds, false, OUT>(a, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_decode_codes(const DecArgs& a, bool accumulate, cudaStream_t st) {
+  return accumulate ? launch_decode_codes_t<kOutCodesAdd>(a, st) : launch_decode_codes_t<kOutCodes>(a, st);
 }
 
 cudaError_t launch_decode(const DecArgs& a, cudaStream_t st) {

@@ -164,9 +164,7 @@ int32_t* f64_q_view(void* qbuf, const void* x);  // q array whose 16-byte bounda
 cudaError_t launch_quantize_f64(const double* x, int32_t* q, uint64_t n, double invd, const double* invd_dev,
                                 uint32_t* err, uint32_t sm_count, cudaStream_t st);
 cudaError_t launch_compress_q(const CompressArgs& a, bool fm2, cudaStream_t st);
-// qa[i] += qb[i] (wrapping int32); any wrap sets kErrQuantRange in *err.
-cudaError_t launch_add_codes(int32_t* qa, const int32_t* qb, uint64_t n, uint32_t* err, uint32_t sm_count,
-                             cudaStream_t st);
+
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st);
 cudaError_t launch_compress_batch(const CompressArgs& a, uint32_t L, int rounds, cudaStream_t st);
 cudaError_t prepare_compress_batch();
@@ -189,7 +187,8 @@ cudaError_t launch_decode(const DecArgs& a, cudaStream_t st);
 uint32_t decode_blocks_per_tile_f64(uint32_t L, uint32_t& bpw);
 cudaError_t launch_decode_f64(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode_q(const DecArgs& a, cudaStream_t st);      // a.f.y: the output doubles
-cudaError_t launch_decode_codes(const DecArgs& a, cudaStream_t st);  // a.f.y: the int32 codes
+// a.f.y: the int32 codes (accumulate: added to the codes already there)
+cudaError_t launch_decode_codes(const DecArgs& a, bool accumulate, cudaStream_t st);
 // batched decompression (fastmode1, blockSize 32)
 cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStream_t st);
 cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st);

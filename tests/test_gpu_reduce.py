@@ -80,3 +80,21 @@ def test_reduce_sum_refusals(szp, torch):
     # the device still works
     size = szp.reduce_sum_dev(a.data_ptr(), sa, a.data_ptr(), sa, n, out.data_ptr(), cap, L, T, 1, szp.SZ_FLOAT, st)
     assert size > 0
+
+
+def test_reduce_sum_wraps_with_notice(szp, port, torch):
+    """Codes near 1.5e9 sum past 2^31: the result holds the wrapped codes,
+    as the oracle's, and the call reports a notice."""
+    rng = np.random.default_rng(11)
+    n, T, L = 200_000, 3, 32
+    x = (1.5e9 + 128.0 * rng.integers(-1000, 1000, n)).astype(np.float32)  # exact floats, codes ~1.5e9 at eb 1
+    st = torch.cuda.current_stream().cuda_stream
+    cap = szp.max_stream_bytes(n, L, T, 1)
+    a = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    out = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    dx = torch.from_numpy(x).cuda()
+    sa = szp.compress_dev(dx.data_ptr(), n, a.data_ptr(), cap, szp.ABS, 1.0, 0.0, L, T, 1, st)
+    size = szp.reduce_sum_dev(a.data_ptr(), sa, a.data_ptr(), sa, n, out.data_ptr(), cap, L, T, 1, szp.SZ_FLOAT, st)
+    assert szp._lib.szp_gb300_last_notices() == 1
+    sbytes = a[:sa].cpu().numpy().tobytes()
+    assert out[:size].cpu().numpy().tobytes() == port.reduce_sum(sbytes, sbytes, n, L, T, 1, hb=4)
