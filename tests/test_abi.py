@@ -75,3 +75,10 @@ def test_no_cpu_fallback_without_gpu(szp):
     assert e.value.status == szp.ECUDA
     with pytest.raises(szp.SzpError):
         szp.szp_decompress(b"\0" * 64, 10)
+    with pytest.raises(szp.SzpError) as e:
+        szp.szp_compress(x.astype(np.float64), szp.ABS, 1e-3, 0.0, 32, 1, szp.SZ_DOUBLE)
+    assert e.value.status == szp.ECUDA
+    # the device entry points fail before touching their (here meaningless) pointers
+    with pytest.raises(szp.SzpError) as e:
+        szp.reduce_sum_dev(1 << 20, 64, 1 << 21, 64, 10, 1 << 22, 4096)
+    assert e.value.status == szp.ECUDA
