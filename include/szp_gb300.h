@@ -85,8 +85,9 @@ void szp_float_single_thread_arg(unsigned char *output, float *oriData, size_t *
                                  size_t nbEle, int blockSize);
 
 /* Replaces SZp/include/szp_float.h:39 (SZp/src/szp_float.cc:607-750).
- * Same stream as szp_float_single_thread_arg; returns the bytes the GPU
- * kernels moved (4*nbEle read + stream written), not the CPU's counter. */
+ * Same stream as szp_float_single_thread_arg; returns the reference's
+ * `total_memaccess` tally for that stream (its own count of the bytes each
+ * statement of the CPU loop touches), 0 on an error. */
 size_t szp_float_single_thread_arg_record(unsigned char *output, float *oriData, size_t *outSize,
                                           float absErrBound, size_t nbEle, int blockSize);
 
@@ -112,7 +113,7 @@ void szp_float_decompress_single_thread_arg(float *newData, size_t nbEle, float 
                                             unsigned char *cmpBytes);
 
 /* Replaces SZp/include/szpd_float.h:27 (SZp/src/szpd_float.cc:216-318);
- * returns the bytes the GPU kernels moved. */
+ * returns the reference's `total_memaccess` tally, 0 on an error. */
 size_t szp_float_decompress_single_thread_arg_record(float *newData, size_t nbEle, float absErrBound,
                                                      int blockSize, unsigned char *cmpBytes);
 
@@ -142,7 +143,7 @@ void szp_double_single_thread_arg(unsigned char *output, double *oriData, size_t
                                   size_t nbEle, int blockSize);
 
 /* Replaces SZp/include/szp_double.h:39 (SZp/src/szp_double.cc:613-757);
- * returns the bytes the GPU kernels moved. */
+ * returns the reference's `total_memaccess` tally, 0 on an error. */
 size_t szp_double_single_thread_arg_record(unsigned char *output, double *oriData, size_t *outSize,
                                            double absErrBound, size_t nbEle, int blockSize);
 
@@ -167,7 +168,7 @@ void szp_double_decompress_single_thread_arg(double *newData, size_t nbEle, doub
                                              unsigned char *cmpBytes);
 
 /* Replaces SZp/include/szpd_double.h:27 (SZp/src/szpd_double.cc:219-321);
- * returns the bytes the GPU kernels moved. */
+ * returns the reference's `total_memaccess` tally, 0 on an error. */
 size_t szp_double_decompress_single_thread_arg_record(double *newData, size_t nbEle, double absErrBound,
                                                       int blockSize, unsigned char *cmpBytes);
 

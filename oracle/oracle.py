@@ -74,7 +74,23 @@ class Port:
         lib.szo_reduce_sum.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                                        ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_void_p, ctypes.c_size_t, _c_size_p]
+        for name in ("szo_record_compress", "szo_record_decompress"):
+            f = getattr(lib, name)
+            f.restype = ctypes.c_uint64
+            f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
         self.lib = lib
+
+    def record_compress(self, stream, n, L=32, dbl=False):
+        """The reference's single-thread compressor _record tally for the
+        T = 1 stream it writes (szp_float.cc:607-750, szp_double.cc:613-756)."""
+        buf = np.frombuffer(stream, dtype=np.uint8)
+        return int(self.lib.szo_record_compress(buf.ctypes.data, buf.size, n, L, int(dbl)))
+
+    def record_decompress(self, stream, n, L=32, dbl=False):
+        """The reference's single-thread decompressor _record tally
+        (szpd_float.cc:216-318, szpd_double.cc:219-321)."""
+        buf = np.frombuffer(stream, dtype=np.uint8)
+        return int(self.lib.szo_record_decompress(buf.ctypes.data, buf.size, n, L, int(dbl)))
 
     def max_threads(self):
         return self.lib.szo_max_threads()
@@ -221,6 +237,34 @@ def _ref_arg_setup(lib):
         f = getattr(lib, name)
         f.restype = None
         f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]
+
+
+def reference_record(ref, x, eb, L):
+    """The reference's single-thread _record pair on x (float32 or float64)
+    at absolute bound eb: (stream, compress tally, decompressed values,
+    decompress tally).  Callers keep the stream within the reference's own
+    4n-byte (8n for doubles) working buffer (szp_float.cc:634)."""
+    lib = ref.lib
+    dbl = np.asarray(x).dtype == np.float64
+    x = np.ascontiguousarray(x, dtype=np.float64 if dbl else np.float32)
+    ct = ctypes.c_double if dbl else ctypes.c_float
+    pre = "szp_double" if dbl else "szp_float"
+    fc = getattr(lib, pre + "_single_thread_arg_record")
+    fc.restype = ctypes.c_size_t
+    fc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _c_size_p, ct, ctypes.c_size_t, ctypes.c_int]
+    fd = getattr(lib, pre + "_decompress_single_thread_arg_record")
+    fd.restype = ctypes.c_size_t
+    fd.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ct, ctypes.c_int, ctypes.c_void_p]
+    hb = 8 if dbl else 4
+    cap = 64 + hb + 16 * x.size + 200 * (x.size // max(L, 1) + 2)
+    out = np.zeros(cap, dtype=np.uint8)
+    size = ctypes.c_size_t(0)
+    rc = int(fc(out.ctypes.data, x.ctypes.data, ctypes.byref(size), ct(eb), x.size, L))
+    s = out[: size.value].tobytes()
+    y = np.zeros(max(x.size, 1), dtype=x.dtype)
+    buf = np.frombuffer(s, dtype=np.uint8).copy()
+    rd = int(fd(y.ctypes.data, x.size, ct(eb), L, buf.ctypes.data + hb))
+    return s, rc, y[: x.size], rd
 
 
 def reference_compress_arg(ref, x, eb, L, T, mode):

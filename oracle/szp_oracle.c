@@ -617,3 +617,88 @@ int szo_max_threads(void)
     return 1;
 #endif
 }
+
+/* The `total_memaccess` tallies returned by the reference's single-thread
+ * _record entry points, restated step by step over a T = 1 fastmode1 stream
+ * (the stream the matching single-thread compressor writes).  The counts are
+ * the reference's own bookkeeping of the bytes each statement touches, not a
+ * measurement.  q = 4 for float data, 8 for double data.
+ *
+ * Compressor, szp_float.cc:607-750 (szp_double.cc:613-756 for double data):
+ *   8 for *outSize (:622); for n > 0 the seed: q read + 2*4 (:651,653);
+ *   per element q read + 1 + 4 for the temp arrays (:672,695); per block
+ *   1 for the bit count (:700,708), and for a non-zero block the m sign
+ *   reads, the sign bytes, the 4m magnitude reads and the payload bytes
+ *   (:713-722); at the end 8 + 8 + 3*8 + 2*8 + 2 * segment bytes (:728-739).
+ * Decompressor, szpd_float.cc:216-318 (szpd_double.cc:219-321):
+ *   8 for the offset (:239); for n > 0 2*4 for the seed + 2q for x'[0]
+ *   (:246,251); per block 1 for the bit count (:266); a zero block 2q per
+ *   element (:275); a non-zero block its sign bytes + m, its payload bytes +
+ *   4m, and 1 + 4 + 2q per element (:283-309).
+ * Returns 0 for a stream that does not parse. */
+uint64_t szo_record_compress(const unsigned char *stream, size_t len, size_t n, int L, int dbl)
+{
+    if (L <= 0) return 0;
+    const uint64_t q = dbl ? 8 : 4;
+    const size_t hb = dbl ? 8 : 4;
+    uint64_t acc = 8;
+    if (len < hb + 8) return 0;
+    const unsigned char *p = stream + hb + 8, *end = stream + len;
+    uint64_t seg = 0;
+    if (n > 0) {
+        acc += q + 8;
+        p += 4;
+        seg += 4;
+    }
+    for (size_t i = 1; i < n; i += (size_t)L) {
+        size_t m = (i + (size_t)L > n) ? n - i : (size_t)L;
+        if (p >= end || p[0] > 33) return 0;
+        int bc = p[0];
+        size_t nb = block_bytes(m, bc);
+        acc += (q + 5) * m;               /* each element: x read, temp sign, temp magnitude */
+        acc += 1;                         /* the bit-count byte */
+        if (bc) {
+            size_t nsign = (m + 7) / 8;
+            acc += m + nsign;             /* temp signs read, sign bytes written */
+            acc += 4 * m + (nb - 1 - nsign); /* magnitudes read, payload written */
+        }
+        p += nb;
+        seg += nb;
+    }
+    if (p > end) return 0;
+    acc += 8 + 8 + 3 * 8 + 2 * 8;
+    acc += 2 * seg;
+    return acc;
+}
+
+uint64_t szo_record_decompress(const unsigned char *stream, size_t len, size_t n, int L, int dbl)
+{
+    if (L <= 0) return 0;
+    const uint64_t q = dbl ? 8 : 4;
+    const size_t hb = dbl ? 8 : 4;
+    uint64_t acc = 8;
+    if (len < hb + 8) return 0;
+    const unsigned char *p = stream + hb + 8, *end = stream + len;
+    if (n > 0) {
+        acc += 2 * 4 + 2 * q;
+        p += 4;
+    }
+    for (size_t i = 1; i < n; i += (size_t)L) {
+        size_t m = (i + (size_t)L > n) ? n - i : (size_t)L;
+        if (p >= end || p[0] > 33) return 0;
+        int bc = p[0];
+        size_t nb = block_bytes(m, bc);
+        acc += 1;
+        if (bc == 0) {
+            acc += 2 * q * m;
+        } else {
+            size_t nsign = (m + 7) / 8;
+            acc += nsign + m;                   /* sign bytes read, temp signs written */
+            acc += (nb - 1 - nsign) + 4 * m;    /* payload read, temp magnitudes written */
+            acc += (1 + 4 + 2 * q) * m;         /* per element: temps read, x' stored */
+        }
+        p += nb;
+    }
+    if (p > end) return 0;
+    return acc;
+}

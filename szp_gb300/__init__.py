@@ -214,6 +214,12 @@ def last_status():
     return _lib.szp_gb300_last_status()
 
 
+def last_notices():
+    """1 when the last call met a value the reference quantizes outside its
+    int32 range (NaN or |x/eb| >= 2^31), else 0."""
+    return _lib.szp_gb300_last_notices()
+
+
 def _raise(what):
     raise SzpError(last_status(), "%s failed: %s" % (what, last_error()))
 
@@ -333,6 +339,40 @@ def szp_float_decompress_arg(stream, n, block_size=32, which="openmp_threadblock
     if last_status() != 0:
         _raise("szp_float_decompress_" + which)
     return y[:n]
+
+
+def single_thread_arg_record(data, abs_err_bound, block_size=32):
+    """szp_float_single_thread_arg_record / szp_double_single_thread_arg_record
+    (SZp/include/szp_float.h:39, szp_double.h:39) on a float32 or float64 host
+    array: returns (stream, the reference's memory-access tally)."""
+    dbl = np.asarray(data).dtype == np.float64
+    x = np.ascontiguousarray(data, dtype=np.float64).ravel() if dbl else _f32(data)
+    out = np.zeros(max(x.itemsize * (x.size + 1), 1), dtype=np.uint8)
+    size = ctypes.c_size_t(0)
+    fn = _lib.szp_double_single_thread_arg_record if dbl else _lib.szp_float_single_thread_arg_record
+    tally = fn(out.ctypes.data, x.ctypes.data, ctypes.byref(size), abs_err_bound, x.size, block_size)
+    if size.value == 0 or last_status() != 0:
+        _raise("single_thread_arg_record")
+    return out[: size.value].tobytes(), int(tally)
+
+
+def decompress_single_thread_arg_record(stream, n, block_size=32, data_type=SZ_FLOAT):
+    """szp_float_decompress_single_thread_arg_record (szpd_float.h:27) or its
+    double twin (szpd_double.h:27): returns (values, the reference's
+    memory-access tally)."""
+    buf = np.frombuffer(stream, dtype=np.uint8)
+    if data_type == SZ_DOUBLE:
+        eb = float(np.frombuffer(bytes(stream[:8])[::-1], dtype=np.float64)[0])
+        y = np.empty(max(n, 1), dtype=np.float64)
+        tally = _lib.szp_double_decompress_single_thread_arg_record(y.ctypes.data, n, eb, block_size,
+                                                                    buf.ctypes.data + 8)
+    else:
+        y = np.empty(max(n, 1), dtype=np.float32)
+        tally = _lib.szp_float_decompress_single_thread_arg_record(y.ctypes.data, n, _eb_of(stream), block_size,
+                                                                   buf.ctypes.data + 4)
+    if last_status() != 0:
+        _raise("decompress_single_thread_arg_record")
+    return y[:n], int(tally)
 
 
 def compress_dev(d_data, n, d_out, capacity, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0,

@@ -586,6 +586,52 @@ int host_stream_length(const uint8_t* stream, size_t n, int L, int T, int fm, si
   return SZP_GB300_OK;
 }
 
+// The reference's single-thread _record entry points return
+// `total_memaccess`, their own tally of the bytes each statement touches
+// (szp_float.cc:607-750, szpd_float.cc:216-318, szp_double.cc:613-756,
+// szpd_double.cc:219-321).  In closed form over the T = 1 fastmode1 stream
+// those functions write and read, with q the value size (4 float, 8 double),
+// S the segment's bytes (seed and blocks), E0 the elements of zero blocks and
+// E1 the elements of the other blocks:
+//   compress    64 + [n>0](q + 4) + (q + 5)(n - 1) + 3S + 5 E1
+//   decompress  8 + [n>0](8 + 2q) + (S - 4[n>0]) + 2q E0 + (10 + 2q) E1
+// The blocks' bit counts come from one host walk of the segment.
+struct RecordTally {
+  uint64_t seg_bytes = 0, e0 = 0, e1 = 0;
+};
+
+static int host_record_tally(const uint8_t* stream, size_t len, size_t n, int L, int hb, RecordTally* t) {
+  *t = RecordTally();
+  if (L <= 0) return fail(SZP_GB300_EINVAL, "bad blockSize");
+  const uint64_t head = (uint64_t)hb + 8;
+  if (len < head) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
+  uint64_t off = 0;
+  memcpy(&off, stream + hb, 8);
+  if (n == 0) return SZP_GB300_OK;
+  uint64_t p = head + off + 4;  // the seed
+  for (uint64_t i = 1; i < n; i += (uint64_t)L) {
+    const uint32_t m = (uint32_t)std::min<uint64_t>((uint64_t)L, n - i);
+    if (p >= len) return fail(SZP_GB300_ECORRUPT, "stream ends inside its blocks");
+    const uint32_t bc = stream[p];
+    if (bc > (uint32_t)kMaxBitCount) return fail(SZP_GB300_ECORRUPT, "invalid bit count %u", bc);
+    (bc ? t->e1 : t->e0) += m;
+    p += block_bytes(m, bc);
+  }
+  if (p > len) return fail(SZP_GB300_ECORRUPT, "stream ends inside its blocks");
+  t->seg_bytes = p - head - off;
+  return SZP_GB300_OK;
+}
+
+static size_t record_compress_tally(const RecordTally& t, size_t n, uint64_t q) {
+  const uint64_t nz = n > 0, e = n > 0 ? n - 1 : 0;
+  return (size_t)(64 + nz * (q + 4) + (q + 5) * e + 3 * t.seg_bytes + 5 * t.e1);
+}
+
+static size_t record_decompress_tally(const RecordTally& t, size_t n, uint64_t q) {
+  const uint64_t nz = n > 0;
+  return (size_t)(8 + nz * (8 + 2 * q) + (t.seg_bytes - 4 * nz) + 2 * q * t.e0 + (10 + 2 * q) * t.e1);
+}
+
 // ------------------------------------------------- host-buffer pipelines --
 size_t host_page_bytes() {
   static const size_t page = [] {
@@ -951,7 +997,10 @@ void szp_float_single_thread_arg(unsigned char* output, float* oriData, size_t* 
 size_t szp_float_single_thread_arg_record(unsigned char* output, float* oriData, size_t* outSize,
                                           float absErrBound, size_t nbEle, int blockSize) {
   fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, 1, 1);
-  return outSize && *outSize ? 4 * nbEle + *outSize : 0;
+  if (t_status || !outSize || !*outSize) return 0;
+  RecordTally t;
+  if (host_record_tally(output, *outSize, nbEle, blockSize, 4, &t)) return 0;
+  return record_compress_tally(t, nbEle, 4);
 }
 
 unsigned char* szp_float_openmp_threadblock_randomaccess(float* oriData, size_t* outSize, float absErrBound,
@@ -983,7 +1032,10 @@ void szp_double_single_thread_arg(unsigned char* output, double* oriData, size_t
 size_t szp_double_single_thread_arg_record(unsigned char* output, double* oriData, size_t* outSize,
                                            double absErrBound, size_t nbEle, int blockSize) {
   fm_compress_arg(output, oriData, outSize, absErrBound, nbEle, blockSize, 1, 1);
-  return outSize && *outSize ? 8 * nbEle + *outSize : 0;
+  if (t_status || !outSize || !*outSize) return 0;
+  RecordTally t;
+  if (host_record_tally(output, *outSize, nbEle, blockSize, 8, &t)) return 0;
+  return record_compress_tally(t, nbEle, 8);
 }
 
 unsigned char* szp_double_openmp_threadblock_randomaccess(double* oriData, size_t* outSize, double absErrBound,
@@ -1019,7 +1071,9 @@ size_t szp_float_decompress_single_thread_arg_record(float* newData, size_t nbEl
   if (t_status) return 0;
   size_t len = 0;
   if (host_stream_length(cmpBytes - 4, nbEle, blockSize, 1, 1, &len)) return 0;
-  return len + 4 * nbEle;
+  RecordTally t;
+  if (host_record_tally(cmpBytes - 4, len, nbEle, blockSize, 4, &t)) return 0;
+  return record_decompress_tally(t, nbEle, 4);
 }
 
 float* szp_float_decompress_openmp_threadblock_randomaccess(size_t nbEle, float absErrBound, int blockSize,
@@ -1055,7 +1109,9 @@ size_t szp_double_decompress_single_thread_arg_record(double* newData, size_t nb
   if (t_status) return 0;
   size_t len = 0;
   if (host_stream_length(cmpBytes - 8, nbEle, blockSize, 1, 1, &len, 8)) return 0;
-  return len + 8 * nbEle;
+  RecordTally t;
+  if (host_record_tally(cmpBytes - 8, len, nbEle, blockSize, 8, &t)) return 0;
+  return record_decompress_tally(t, nbEle, 8);
 }
 
 double* szp_double_decompress_openmp_threadblock_randomaccess(size_t nbEle, double absErrBound, int blockSize,

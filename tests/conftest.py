@@ -65,3 +65,13 @@ def eb_of(stream):
 
 def eb_of_double(stream):
     return float(np.frombuffer(bytes(stream[:8])[::-1], dtype=np.float64)[0])
+
+
+@pytest.fixture(scope="session")
+def golden_record():
+    """The reference's single-thread _record entry points: stream, tallies
+    (rec_c compress, rec_d decompress) and decompressed values."""
+    path = os.path.join(ROOT, "tests", "golden", "golden_record.npz")
+    z = np.load(path)
+    meta = json.loads(bytes(z["meta"]).decode())
+    return [dict(m, x=z["x%d" % i], s=z["s%d" % i].tobytes(), y=z["y%d" % i]) for i, m in enumerate(meta)]

@@ -1,11 +1,13 @@
-"""Writes tests/golden/golden.npz (float32) and golden_double.npz (float64):
+"""Writes tests/golden/golden.npz (float32), golden_double.npz (float64) and
+golden_record.npz (the single-thread _record entry points' return values):
 inputs, streams and decompressed outputs produced by the REFERENCE library
 (built from its own sources by oracle/Makefile into oracle/_ref/).  Run here,
 where the reference sources exist; the fixtures then travel with the
 repository.
 
-    python tests/golden/make_golden.py            # both files
-    python tests/golden/make_golden.py --double   # golden_double.npz only
+    python tests/golden/make_golden.py            # all three files
+    python tests/golden/make_golden.py --double   # golden_double.npz and golden_record.npz
+    python tests/golden/make_golden.py --record   # golden_record.npz only
 
 Each case records x (float32 input), the reference stream, the reference
 decompressed values, and meta (L, T, fastmode, eb mode and bound).  Cases are
@@ -219,7 +221,59 @@ def main_double():
     print("wrote %d cases to %s (%d bytes)" % (len(cases), path, os.path.getsize(path)))
 
 
+def main_record():
+    """The single-thread _record entry points: the reference's stream, its
+    `total_memaccess` return values (szp_float.cc:607-750, szpd_float.cc:216-318
+    and the double twins) and decompressed values, float32 and float64."""
+    from oracle.oracle import reference_record
+    ref, port = Reference(), Port()
+    rng = np.random.default_rng(20261204)
+    out, meta = {}, []
+
+    def add(name, x, L, bound):
+        dbl = x.dtype == np.float64
+        pred = port.compress_d(x, bound, L, 1, 1) if dbl else port.compress(x, bound, L, 1, 1)
+        hb = 8 if dbl else 4
+        if len(pred) - hb - 8 > x.itemsize * x.size:
+            print("skip %s: reference per-thread buffer would overflow" % name)
+            return
+        s, rc, y, rd = reference_record(ref, x, bound, L)
+        assert s == pred, name
+        i = len(meta)
+        out["x%d" % i], out["s%d" % i], out["y%d" % i] = x, np.frombuffer(s, np.uint8).copy(), y
+        meta.append(dict(name=name, L=L, n=int(x.size), bound=bound, dbl=bool(dbl), rec_c=rc, rec_d=rd))
+        print("case", name, rc, rd, flush=True)
+
+    w = walk(100000, rng)
+    eb = float(np.float32(1e-3 * (w.max() - w.min())))
+    add("walk_L32", w, 32, eb)
+    for L in (8, 7, 64):
+        add("walk_L%d" % L, w[:12000], L, eb)
+    for n in (1, 2, 3, 33, 34, 65):
+        add("walk_n%d" % n, w[:n], 32, eb)
+    f = fourier3d(16, rng).ravel()
+    add("fourier", f, 32, float(np.float32(1e-4 * (f.max() - f.min()))))
+    z = laplace_zero_patches(64, 64, rng).ravel()
+    add("zeros", z, 32, 1e-5)
+    add("bitcounts", bitcount_sweep(rng), 32, 1.0)
+    w64 = walk64(12000, rng)
+    ebd = 1e-6 * float(w64.max() - w64.min())
+    for L in (32, 16, 9):
+        add("walk64_L%d" % L, w64, L, ebd)
+    for n in (1, 2, 33):
+        add("walk64_n%d" % n, w64[:n], 32, ebd)
+    add("zeros64", z.astype(np.float64), 32, 1e-5)
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    path = os.path.join(HERE, "golden_record.npz")
+    np.savez_compressed(path, **out)
+    print("wrote %d cases to %s (%d bytes)" % (len(meta), path, os.path.getsize(path)))
+
+
 if __name__ == "__main__":
+    if "--record" in sys.argv:
+        main_record()
+        sys.exit(0)
     if "--double" not in sys.argv:
         main()
     main_double()
+    main_record()
