@@ -885,6 +885,7 @@ void host_segment_blocks(size_t n, int T, int L, uint64_t& nb_reg, uint64_t& nb_
   nb_last = seg_blocks_host(sg, sg.T - 1, false);
 }
 int host_fail(int status, const char* msg) { return fail(status, "%s", msg); }
+void host_set_notices(uint32_t err) { t_notices = (err & kErrQuantRange) ? 1 : 0; }
 void host_clear_error() { clear_error(); }
 void host_count_launches(int k) { count_launches(k); }
 }  // namespace szp

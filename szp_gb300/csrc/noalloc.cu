@@ -74,6 +74,7 @@ extern "C" int szp_gb300_compress_dev_noalloc(const float* d_data, size_t nbEle,
   if (outSize) *outSize = 0;
   if (blockSize <= 0) return host_fail(SZP_GB300_EINVAL, "blockSize must be positive");
   if (!d_out || (nbEle && !d_data)) return host_fail(SZP_GB300_EINVAL, "null device buffer");
+  if ((uintptr_t)d_data & 3) return host_fail(SZP_GB300_EINVAL, "input not aligned to its element size");
   const int T = host_resolve_segments(segments);
   const uint64_t head = 4 + 8ull * (uint64_t)T;
   if (out_capacity < head) return host_fail(SZP_GB300_ECAPACITY, "output buffer smaller than the stream header");
@@ -146,7 +147,6 @@ extern "C" int szp_gb300_compress_dev_noalloc(const float* d_data, size_t nbEle,
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return host_fail(SZP_GB300_ECUDA, cudaGetErrorString(e));
   if (outSize) *outSize = (size_t)size;
-  if (err & kErrCapacity) return host_fail(SZP_GB300_ECAPACITY, "stream does not fit the output buffer");
-  if (err & kErrLookbackTimeout) return host_fail(SZP_GB300_ETIMEOUT, "a device look-back wait gave up");
-  return SZP_GB300_OK;
+  host_set_notices(err);  // NaN or |x/eb| >= 2^31 met, as szp_gb300_compress_dev reports it
+  return host_status_from_err(err);
 }

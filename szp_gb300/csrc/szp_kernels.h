@@ -206,6 +206,9 @@ uint64_t host_block_count(size_t n, int T, int L);
 size_t host_max_stream_bytes(size_t n, int L, int T);
 int host_status_from_err(uint32_t err);
 int host_fail(int status, const char* msg);
+// Records the non-fatal notices of a finished launch's error word (what
+// szp_gb300_last_notices() returns).
+void host_set_notices(uint32_t err);
 void host_clear_error();
 void host_count_launches(int k);
 

@@ -37,7 +37,9 @@ def _make_fields(rng, szp, T):
     return out
 
 
-def _single(szp, f, T):
+def _single(szp, port, f, T):
+    """The single-field device calls on f, each checked against the oracle
+    (so a batch that matches them matches the oracle too)."""
     import torch
     d_s = torch.zeros(f["cap"], dtype=torch.uint8, device="cuda")
     abs_eb = f["bound"] if f["mode"] == szp.ABS else 0.0
@@ -45,18 +47,23 @@ def _single(szp, f, T):
     size = szp.compress_dev(f["x"].data_ptr(), f["n"], d_s.data_ptr(), f["cap"], f["mode"], abs_eb, rel, 32, T, 1, 0)
     y = torch.empty(max(f["n"], 1), dtype=torch.float32, device="cuda")
     szp.decompress_dev(d_s.data_ptr(), size, f["n"], y.data_ptr(), 32, T, 1, 0)
-    return d_s[:size].cpu().numpy().tobytes(), y[:f["n"]].cpu()
+    stream, yv = d_s[:size].cpu().numpy().tobytes(), y[:f["n"]].cpu()
+    x = f["x"][:f["n"]].cpu().numpy()
+    eb = port.rel_bound(x, rel) if f["mode"] == szp.REL else float(np.float32(abs_eb))
+    assert stream == port.compress(x, eb, 32, T, 1), f["n"]
+    assert np.array_equal(yv.numpy().view(np.uint32), port.decompress(stream, f["n"], 32, T, 1).view(np.uint32))
+    return stream, yv
 
 
 @pytest.mark.parametrize("T,flags", [(16, "autotune"), (7, "rounds1"), (16, "rounds2"), (3, "nograph")])
-def test_batch_matches_single_field_calls(szp, T, flags):
+def test_batch_matches_single_field_calls(szp, port, T, flags):
     import torch
 
     fl = {"autotune": szp.BATCH_AUTOTUNE, "rounds1": 1 << 8, "rounds2": 2 << 8,
           "nograph": szp.BATCH_NO_GRAPH | (4 << 8)}[flags]
     rng = np.random.default_rng(77 + T)
     fields = _make_fields(rng, szp, T)
-    ref = [_single(szp, f, T) for f in fields]
+    ref = [_single(szp, port, f, T) for f in fields]
     streams = [torch.full((f["cap"],), 0xCD, dtype=torch.uint8, device="cuda") for f in fields]
     outs = [torch.full((max(f["n"], 1),), float("nan"), dtype=torch.float32, device="cuda") for f in fields]
     cf = [dict(input=f["x"].data_ptr(), output=s.data_ptr(), output_bytes=f["cap"], nbEle=f["n"],

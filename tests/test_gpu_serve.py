@@ -2,8 +2,8 @@
 
 Each request's result must be the same alone (a server that runs one request
 at a time) and in the mix (requests batched and overlapped on several lanes),
-and equal to the single-field calls: streams byte-identical, decoded values
-bit-identical.  Under an HBM budget smaller than all results together, every
+and equal to the oracle's: streams byte-identical, decoded values
+bit-identical (decompress requests read streams the oracle wrote).  Under an HBM budget smaller than all results together, every
 request still completes as the client releases earlier results, and the
 server never holds more than the budget.
 """
@@ -15,7 +15,11 @@ pytestmark = pytest.mark.gpu
 T = 8
 
 
-def _pool(szp, rng):
+def _pool(szp, port, rng):
+    """Fields with their oracle stream and decoded values.  Decompress
+    requests read the oracle's stream (uploaded to the device); compress
+    results and decoded values are compared with the oracle's, and the
+    single-field device calls are checked against it too."""
     import torch
     from szp_gb300.workloads import walk, laplace_zero_patches
 
@@ -36,8 +40,14 @@ def _pool(szp, rng):
         size = szp.compress_dev(dx.data_ptr(), n, d_s.data_ptr(), cap, mode, abs_eb, rel, 32, T, 1, 0)
         y = torch.empty(max(n, 1), dtype=torch.float32, device="cuda")
         szp.decompress_dev(d_s.data_ptr(), size, n, y.data_ptr(), 32, T, 1, 0)
-        pool.append(dict(x=dx, n=n, mode=mode, abs=abs_eb, rel=rel, stream=d_s, size=size,
-                         ref_stream=d_s[:size].cpu().numpy().tobytes(), ref_y=y[:n].cpu()))
+        eb = port.rel_bound(x, rel) if mode == szp.REL else float(np.float32(abs_eb))
+        o_stream = port.compress(x, eb, 32, T, 1)
+        o_y = port.decompress(o_stream, n, 32, T, 1)
+        assert d_s[:size].cpu().numpy().tobytes() == o_stream
+        assert np.array_equal(y[:n].cpu().numpy().view(np.uint32), o_y.view(np.uint32))
+        d_o = torch.from_numpy(np.frombuffer(o_stream, dtype=np.uint8).copy()).cuda()
+        pool.append(dict(x=dx, n=n, mode=mode, abs=abs_eb, rel=rel, stream=d_o, size=len(o_stream),
+                         ref_stream=o_stream, ref_y=torch.from_numpy(o_y)))
     return pool
 
 
@@ -97,9 +107,9 @@ def _copy(dst, src, nbytes):
 _CUDART = []
 
 
-def test_results_same_alone_and_in_the_mix(szp):
+def test_results_same_alone_and_in_the_mix(szp, port):
     rng = np.random.default_rng(5)
-    pool = _pool(szp, rng)
+    pool = _pool(szp, port, rng)
     reqs = _requests(szp, pool, rng, 160)
     # alone: one request at a time
     alone = szp.Server(512 << 20, max_batch=1, lanes=1, segments=T)
@@ -121,9 +131,9 @@ def test_results_same_alone_and_in_the_mix(szp):
     mix.close()
 
 
-def test_admission_under_a_tight_budget(szp):
+def test_admission_under_a_tight_budget(szp, port):
     rng = np.random.default_rng(9)
-    pool = _pool(szp, rng)
+    pool = _pool(szp, port, rng)
     reqs = _requests(szp, pool, rng, 120)
     budget = 24 << 20  # far below what all results need together
     srv = szp.Server(budget, max_batch=32, lanes=2, segments=T)
