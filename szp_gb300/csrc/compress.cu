@@ -108,12 +108,6 @@ __device__ __forceinline__ void write_header_common(uint8_t* out, double eb, con
   }
 }
 
-// Offset of segment t, after an eb header of hb bytes (4 float, 8 double).
-__device__ __forceinline__ void write_offset(uint8_t* out, uint32_t t, uint64_t off, uint32_t hb = 4) {
-  uint8_t* p = out + hb + 8ull * t;
-  for (int i = 0; i < 8; i++) p[i] = (uint8_t)(off >> (8 * i));
-}
-
 // CTA-wide exclusive scan of per-warp byte counts; returns the tile aggregate.
 template <int WARPS>
 __device__ __forceinline__ uint32_t scan_warps(uint32_t* s_w, uint32_t mine, int warp, int lane, uint32_t& excl,
@@ -219,77 +213,6 @@ struct SlotMeta {
   uint64_t* out_size;
   uint32_t* err;       // the field's error word
 };
-
-// eb (big-endian) and, when every segment but the last is empty (n < T),
-// their zero offsets (szp_float.cc:164,280-289); one warp.
-__device__ __forceinline__ void write_header_warp(uint8_t* out, float eb, const Segments& sg, int lane) {
-  const uint32_t b = __float_as_uint(eb);
-  if (lane < 4) out[lane] = (uint8_t)(b >> (24 - 8 * lane));
-  if (sg.tsz == 0) {
-    const uint32_t nz = 8 * (sg.n == 0 ? sg.T : sg.T - 1);
-    for (uint32_t i = lane; i < nz; i += 32) out[4 + i] = 0;
-  }
-}
-
-// The float64 stream's header: eb as 8 big-endian bytes, zero offsets as above.
-__device__ __forceinline__ void write_header_warp(uint8_t* out, double eb, const Segments& sg, int lane) {
-  const uint64_t b = (uint64_t)__double_as_longlong(eb);
-  if (lane < 8) out[lane] = (uint8_t)(b >> (56 - 8 * lane));
-  if (sg.tsz == 0) {
-    const uint32_t nz = 8 * (sg.n == 0 ? sg.T : sg.T - 1);
-    for (uint32_t i = lane; i < nz; i += 32) out[8 + i] = 0;
-  }
-}
-
-// One warp copies len bytes from shared memory src (16-byte aligned, readable
-// for len + 16 bytes) to global dst (any alignment): 16-byte stores for the
-// aligned middle, the bytes shifted into place with funnel shifts; byte
-// stores for the ragged ends, which neighbouring tiles share.
-__device__ __forceinline__ void warp_store_span(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
-                                                uint32_t len, int lane) {
-  if (len == 0) return;
-  const uint32_t a = (uint32_t)((uintptr_t)dst & 15);
-  uint8_t* g0 = dst - a;                             // 16-byte aligned
-  const uint32_t end = a + len;                      // the span is [a, end) from g0
-  const uint32_t c0 = (a + 15) >> 4, c1 = end >> 4;  // whole 16-byte chunks [c0, c1)
-  if (c0 >= c1) {
-    for (uint32_t b = a + (uint32_t)lane; b < end; b += 32) g0[b] = src[b - a];
-    return;
-  }
-  if ((uint32_t)lane < 16 * c0 - a) g0[a + lane] = src[lane];
-  if ((uint32_t)lane < end - 16 * c1) g0[16 * c1 + lane] = src[16 * c1 + lane - a];
-  const uint32_t sh = (16 - a) & 15;  // chunk c starts at src byte 16c - a = 16(c - 1) + sh when a != 0
-  if (sh == 0) {
-    for (uint32_t c = c0 + lane; c < c1; c += 32)
-      *reinterpret_cast<uint4*>(g0 + 16 * c) = *reinterpret_cast<const uint4*>(src + 16 * c);
-    return;
-  }
-  const uint32_t q = sh >> 2, bs = 8 * (sh & 3);
-  // two chunks per lane per pass: their shared-memory loads are in flight together
-  for (uint32_t cb = c0; cb < c1; cb += 64) {
-    uint4 o[2];
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const uint32_t c = min(cb + lane + 32 * k, c1 - 1);  // clamped: always a readable chunk
-      const uint4* line = reinterpret_cast<const uint4*>(src + 16 * (c - 1));
-      const uint4 u = line[0], v = line[1];
-      const uint32_t w[8] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
-#define SZP_FS(i) __funnelshift_r(w[(i)], w[(i) + 1], bs)
-      switch (q) {
-        case 0: o[k] = make_uint4(SZP_FS(0), SZP_FS(1), SZP_FS(2), SZP_FS(3)); break;
-        case 1: o[k] = make_uint4(SZP_FS(1), SZP_FS(2), SZP_FS(3), SZP_FS(4)); break;
-        case 2: o[k] = make_uint4(SZP_FS(2), SZP_FS(3), SZP_FS(4), SZP_FS(5)); break;
-        default: o[k] = make_uint4(SZP_FS(3), SZP_FS(4), SZP_FS(5), SZP_FS(6)); break;
-      }
-#undef SZP_FS
-    }
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const uint32_t c = cb + lane + 32 * k;
-      if (c < c1) *reinterpret_cast<uint4*>(g0 + 16 * c) = o[k];
-    }
-  }
-}
 
 // Producer: one thread.  Draws tickets, and for each tile computes its
 // geometry and bulk-copies its input window [e0-1, e0+nel) into a free slot
@@ -1358,6 +1281,7 @@ static cudaError_t launch_lanes(const CompressArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st) {
+  if (!fm2 && compress32_supported(a)) return launch_compress32(a, st);
   size_t smem = compress_smem_bytes(a.seg.L, a.tb);
   if (fm2) {
     switch (lanes_per_block(a.seg.L)) {

@@ -150,6 +150,10 @@ struct DecArgs {
 uint32_t compress_blocks_per_tile(uint32_t L, uint32_t& bpw);
 size_t compress_smem_bytes(uint32_t L, uint32_t tb);
 cudaError_t launch_compress(const CompressArgs& a, bool fm2, cudaStream_t st);
+// fastmode1, blockSize 32, one field (fm1_pipes.cu); launch_compress takes it
+// whenever it applies
+bool compress32_supported(const CompressArgs& a);
+cudaError_t launch_compress32(const CompressArgs& a, cudaStream_t st);
 // float64 data: every blockSize on the one-warp-per-block kernels
 uint32_t compress_blocks_per_tile_f64(uint32_t L, uint32_t& bpw);
 size_t compress_smem_bytes_f64(uint32_t L, uint32_t tb);
