@@ -9,11 +9,13 @@
 // configuration needs.
 //
 // Structure: a tile's input slot is freed as soon as its analysis is done,
-// and its packed bytes go to a ring in shared memory, from which the control
-// warp copies them to the stream once the look-back has placed the tile.  A
-// tile's position waits for its slowest predecessor anywhere on the GPU; with
-// the ring that wait holds no input slot, and the compute warps only stall
-// when the ring (several tiles) is full.
+// and its packed bytes go to a ring in shared memory.  The control warp only
+// places tiles (decoupled look-back, header and segment offsets); the compute
+// warps copy a tile from the ring to the stream two tiles later, all 256
+// threads at once.  A tile's position waits for its slowest predecessor
+// anywhere on the GPU; with the ring that wait holds no input slot, and the
+// compute warps only wait when a position is still unknown two tiles on, or
+// the ring is full.
 //
 // Compute:
 //   * the analysis is compiled once per 16-byte phase of the tile's input in
@@ -75,6 +77,7 @@ struct C32Meta {
 // before its warp's arrival on the record's barrier.
 struct C32Rec {
   uint64_t end;    // ring bytes allocated up to and including this tile
+  uint64_t gpos;   // stream position, written by the control warp (~0: does not fit)
   uint32_t tile;   // launch tile
   uint32_t seg;    // segment
   uint32_t first;  // first tile of its segment (the stream has elements)
@@ -151,42 +154,76 @@ __device__ __forceinline__ void c32_producer(const CompressArgs& a, uint8_t* slo
 
 // Control warp: for each of the CTA's tiles in order, the stream position
 // (the eb header for the first tile, the decoupled look-back for the others),
-// the segment offset of a segment's first tile, the stream size after the
-// last tile; then the copy of the packed bytes from the ring to the stream
-// and the release of their ring space.
-__device__ __forceinline__ void c32_control(const CompressArgs& a, const C32Rec* rec, uint64_t* recb,
-                                            const uint8_t* ring, volatile uint64_t* s_tail,
-                                            volatile uint32_t* s_released, const uint32_t* s_epoch,
-                                            const volatile uint32_t* s_stop_k, float eb) {
+// the segment offset of a segment's first tile and the stream size after the
+// last tile.  The position goes back to the compute warps in the record.
+__device__ __forceinline__ void c32_control(const CompressArgs& a, C32Rec* rec, uint64_t* recb, uint64_t* based,
+                                            const uint32_t* s_epoch, const volatile uint32_t* s_stop_k, float eb) {
   const int lane = threadIdx.x & 31;
   const uint64_t head = 4 + 8ull * a.seg.T;
   for (uint32_t k = 0;; k++) {
     const int p = (int)(k % kRecs);
     if (!control_wait_full(&recb[p], (k / kRecs) & 1, k, s_stop_k, a.err)) return;
-    const C32Rec r = rec[p];
+    C32Rec& r = rec[p];
+    const uint32_t tile = r.tile, agg = r.agg;
     const uint32_t epoch = *s_epoch;
     uint64_t excl = 0;
-    if (r.tile == 0) {
+    if (tile == 0) {
       write_header_warp(a.out, eb, a.seg, lane);
     } else {
-      excl = lookback_sum(a.status, r.tile, 0, epoch, a.err);
-      if (lane == 0) st_relaxed_u64(a.status + r.tile, make_status(epoch, kFlagInclusive, excl + r.agg));
+      excl = lookback_sum(a.status, tile, 0, epoch, a.err);
+      if (lane == 0) st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, excl + agg));
     }
-    const uint64_t gpos = head + excl;
-    const bool fits = gpos + r.agg <= a.cap;
     if (lane == 0) {
-      if (r.tile == a.ntiles - 1) *a.out_size = gpos + r.agg;
+      const uint64_t gpos = head + excl;
+      const bool fits = gpos + agg <= a.cap;
+      if (tile == a.ntiles - 1) *a.out_size = gpos + agg;
       if (r.first && fits) write_offset(a.out, r.seg, excl);
       if (!fits) atomicOr(a.err, kErrCapacity);
-    }
-    if (fits) warp_store_span(a.out + gpos, ring + r.rpos, r.agg, lane);
-    __syncwarp();
-    if (lane == 0) {
-      __threadfence_block();  // the ring reads are done before the space is handed back
-      *s_tail = r.end;
-      *s_released = k + 1;
+      r.gpos = fits ? gpos : ~0ull;
+      mbar_arrive(&based[p]);
     }
     __syncwarp();
+  }
+}
+
+// The 256 compute threads copy len bytes staged at src (16-byte aligned,
+// readable for len + 16 bytes) to global dst (any alignment): 16-byte stores
+// of the aligned middle, each chunk funnel-shifted out of two aligned lines;
+// byte stores at the ragged ends, which neighbouring tiles share.
+__device__ __forceinline__ void cta_store_span(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src, uint32_t len,
+                                               uint32_t tid) {
+  if (len == 0) return;
+  const uint32_t a = (uint32_t)((uintptr_t)dst & 15);
+  uint8_t* g0 = dst - a;                             // 16-byte aligned
+  const uint32_t end = a + len;                      // the span is [a, end) from g0
+  const uint32_t c0 = (a + 15) >> 4, c1 = end >> 4;  // whole 16-byte chunks [c0, c1)
+  if (c0 >= c1) {
+    if (tid < len) g0[a + tid] = src[tid];
+    return;
+  }
+  if (tid < 16 * c0 - a) g0[a + tid] = src[tid];
+  if (tid >= 32 && tid - 32 < end - 16 * c1) g0[16 * c1 + tid - 32] = src[16 * c1 + tid - 32 - a];
+  const uint32_t sh = (16 - a) & 15;  // chunk c starts at src byte 16c - a = 16(c - 1) + sh when a != 0
+  if (sh == 0) {
+    for (uint32_t c = c0 + tid; c < c1; c += kW * 32)
+      *reinterpret_cast<uint4*>(g0 + 16 * c) = *reinterpret_cast<const uint4*>(src + 16 * c);
+    return;
+  }
+  const uint32_t q = sh >> 2, bs = 8 * (sh & 3);
+  for (uint32_t c = c0 + tid; c < c1; c += kW * 32) {
+    const uint4* line = reinterpret_cast<const uint4*>(src + 16 * (c - 1));
+    const uint4 u = line[0], v = line[1];
+    const uint32_t w[8] = {u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
+    uint4 o;
+#define SZP_FS(i) __funnelshift_r(w[(i)], w[(i) + 1], bs)
+    switch (q) {
+      case 0: o = make_uint4(SZP_FS(0), SZP_FS(1), SZP_FS(2), SZP_FS(3)); break;
+      case 1: o = make_uint4(SZP_FS(1), SZP_FS(2), SZP_FS(3), SZP_FS(4)); break;
+      case 2: o = make_uint4(SZP_FS(2), SZP_FS(3), SZP_FS(4), SZP_FS(5)); break;
+      default: o = make_uint4(SZP_FS(3), SZP_FS(4), SZP_FS(5), SZP_FS(6)); break;
+    }
+#undef SZP_FS
+    *reinterpret_cast<uint4*>(g0 + 16 * c) = o;
   }
 }
 
@@ -382,9 +419,7 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
   __shared__ uint32_t s_epoch;
   __shared__ volatile uint32_t s_stop_k;    // the producer's stop position
   __shared__ volatile uint32_t s_cstop_k;   // the compute warps' stop position (for the control warp)
-  __shared__ volatile uint64_t s_tail;      // ring bytes released
-  __shared__ volatile uint32_t s_released;  // tiles whose ring space is released
-  __shared__ __align__(8) uint64_t s_full[kNS], s_empty[kNS], s_recb[kRecs];
+  __shared__ __align__(8) uint64_t s_full[kNS], s_empty[kNS], s_recb[kRecs], s_based[kRecs];
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x < 36) s_thr[threadIdx.x] = a.thr.thr[threadIdx.x];
@@ -394,11 +429,12 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
       mbar_init(&s_full[s], 1);
       mbar_init(&s_empty[s], 1);
     }
-    for (int p = 0; p < kRecs; p++) mbar_init(&s_recb[p], kW);  // one arrival per compute warp
+    for (int p = 0; p < kRecs; p++) {
+      mbar_init(&s_recb[p], kW);  // one arrival per compute warp
+      mbar_init(&s_based[p], 1);
+    }
     s_stop_k = kStopTile;
     s_cstop_k = kStopTile;
-    s_tail = 0;
-    s_released = 0;
   }
   __syncthreads();
   const float eb = a.eb_dev ? *a.eb_dev : a.eb;
@@ -408,7 +444,7 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
     return;
   }
   if (warp == kW) {
-    c32_control(a, s_rec, s_recb, s_ring, &s_tail, &s_released, &s_epoch, &s_cstop_k, eb);
+    c32_control(a, s_rec, s_recb, s_based, &s_epoch, &s_cstop_k, eb);
     return;
   }
 
@@ -416,13 +452,27 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
   const float inv = __fdiv_rn(1.0f, eb);
   const int sub = lane & 3, grp = lane >> 2;
   const uint32_t tid = threadIdx.x;
-  uint64_t rhead = 0;  // ring bytes allocated, the same in every compute thread
+  // Ring state, the same in every compute thread: bytes allocated and
+  // released, the next position to copy out, and the end of a copied tile
+  // whose space is released at the next barrier.
+  uint64_t rhead = 0, rtail = 0, pend_end = 0;
+  uint32_t ncopy = 0;
+  // Copies position j out of the ring once the control warp has placed it.
+  auto copy_out = [&](uint32_t j) {
+    const int pj = (int)(j % kRecs);
+    mbar_wait_or_flag(&s_based[pj], (j / kRecs) & 1, a.err);
+    const uint64_t gpos = s_rec[pj].gpos;
+    if (gpos != ~0ull) cta_store_span(a.out + gpos, s_ring + s_rec[pj].rpos, s_rec[pj].agg, tid);
+    pend_end = s_rec[pj].end;
+  };
+  constexpr uint32_t kDefer = 2;  // tiles between packing a tile and copying it out
   for (uint32_t k = 0;; k++) {
     const int s = (int)(k % kNS);
     mbar_wait_or_flag(&s_full[s], (k / kNS) & 1, a.err);
     const C32Meta g = s_meta[s];
     if (g.tile >= a.ntiles) {
       if (tid == 0) s_cstop_k = k;  // the control warp ends after the tiles before k
+      for (; ncopy < k; ncopy++) copy_out(ncopy);
       return;
     }
     const float* sx = reinterpret_cast<const float*>(s_slots + (size_t)s * kSlotBytes);
@@ -491,7 +541,8 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
     // after the next tile's barrier, which every reader of it has passed
     uint32_t* wtot = s_wtot[k & 1];
     if (lane == 0) wtot[warp] = tot0 + tot1 + tot2 + tot3;
-    compute_sync();  // also ends every read of the input slot
+    compute_sync();  // also ends every read of the input slot and of the last copied tile
+    rtail = pend_end;
     const uint32_t front = seed ? 4u : 0u;
     uint32_t wexcl = front, agg = front;
 #pragma unroll
@@ -507,22 +558,22 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
     }
 
     // ---- ring space: 16-byte-aligned and contiguous (a tile that would
-    // wrap starts over at offset 0); wait for the control warp to release
-    // older tiles and their records ----
+    // wrap starts over at offset 0); when the older tiles leave too little,
+    // they are copied out now ----
     uint64_t start = rhead;
     const uint32_t pos0 = (uint32_t)(start % kRing);
     if (pos0 + agg > kRing) start += kRing - pos0;
     const uint64_t end = start + ((agg + 15) & ~15u);
     const uint32_t rpos = (uint32_t)(start % kRing);
-    if (lane == 0) {
-      uint32_t i = 0;
-      while ((end - s_tail > kRing || k - s_released >= (uint32_t)kRecs) && i < kWaitLimit) {
-        __nanosleep(64);
-        i++;
+    while (end - rtail > kRing) {
+      if (ncopy == k) {  // nothing waits in the ring: the skipped bytes belong to no tile
+        rtail = start;
+        break;
       }
-      if (i == kWaitLimit) atomicOr(a.err, kErrLookbackTimeout);
+      copy_out(ncopy++);
+      compute_sync();  // the copied bytes are read before they are overwritten
+      rtail = pend_end;
     }
-    __syncwarp();
     rhead = end;
     uint8_t* out = s_ring + rpos;
     const int p = (int)(k % kRecs);
@@ -561,6 +612,9 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&s_recb[p]);  // the warp's share of tile k is packed
+    // ---- copy out the tile packed kDefer tiles ago (its space is released
+    // at the next barrier) ----
+    if (ncopy + kDefer <= k) copy_out(ncopy++);
   }
 }
 
