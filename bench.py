@@ -15,11 +15,15 @@ roofline  the kernel with the most device time: algorithmic bytes per
         launch / its average CUDA-event duration, against the measured HBM
         copy bandwidth.
 cpu_baseline  the oracle (C restatement of the reference, OpenMP on all host
-        cores, same T) on a 2^25-value sample of the field.
+        cores, same T) on the full field: median of 10 round trips after 2
+        warm-ups.
+configs the other single-field configurations: the 2^24-value random walk
+        (ABS 1e-4 of its range) and the 8192^2 Laplace field with 40% zero
+        blocks (ABS 1e-5), GB/s and per-kernel roofline fractions.
 
 --impl reference times the reference's CPU algorithm (the oracle port; the
 reference's sources are not present where the benchmark runs) on the same
-workload.
+full field at T = all host threads, plus the median at T = 1.
 Multi-GPU: replicas only (each rank runs the same step on its own GPU).
 """
 import argparse
@@ -58,6 +62,7 @@ def parse():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-reduce", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the 2^24 walk and 8192^2 Laplace legs")
     ap.add_argument("--serving-window", type=float, default=0.2, help="seconds of arrivals per rate")
     ap.add_argument("--batched-fields", type=int, default=1024)
     return ap.parse_args()
@@ -276,16 +281,18 @@ def batched_workload(szp, torch, dev, T, nfields, reps=3, seed=11):
     return res
 
 
-def serving_workload(szp, torch, dev, T, window, rates=(2000, 5000, 10000, 20000, 50000), seed=13,
-                     budget=40 << 30):
+def serving_workload(szp, torch, dev, T, window, rates=(2000, 5000, 10000, 20000, 50000, 100000, 200000, 400000),
+                     seed=13, budget=40 << 30, npool=192):
     """Poisson arrivals, 60% compress / 40% decompress, sizes log-normal
     (median 1 MB, 4 KB..64 MB), REL log-uniform in [1e-5, 1e-2], results kept
     on the device under a 40 GB admission budget.  The continuous-batching
     server (64 requests per group, 3 lanes) against the same server taking one
-    request at a time; latency is completion minus scheduled arrival."""
+    request at a time; latency is completion minus scheduled arrival.  Rates
+    above the server's capacity show where its GB/s falls below the offered
+    load; above 100k req/s the window shrinks so that each rate offers at
+    most 20k requests."""
     from szp_gb300.workloads import fourier3d_torch, walk_torch
     rng = np.random.default_rng(seed)
-    npool = 48
     ns = [int(b) // 4 for b in np.clip(np.exp(rng.normal(np.log(1 << 20), 1.4, npool)), 4096, 64 << 20)]
     base = fourier3d_torch(256, seed, dev)
     st = torch.cuda.current_stream(dev).cuda_stream  # the stream the fields are made on
@@ -318,7 +325,7 @@ def serving_workload(szp, torch, dev, T, window, rates=(2000, 5000, 10000, 20000
         srv.completed()
         base_bytes = srv.stats()["bytes"]
         r2 = np.random.default_rng(seed + rate)
-        count = max(1, int(rate * window))
+        count = max(1, int(rate * min(window, 20000.0 / rate)))
         arr = np.cumsum(r2.exponential(1.0 / rate, count))
         reqs = []
         for k in range(count):
@@ -357,7 +364,7 @@ def serving_workload(szp, torch, dev, T, window, rates=(2000, 5000, 10000, 20000
                 "gbs": round(nbytes / span / 1e9, 2), "offered_gbs": round(nbytes / (arr[-1] + 1e-9) / 1e9, 2),
                 "peak_memory_gb": round(st["memory_peak"] / 1e9, 2)}
 
-    out = {"window_s": window, "budget_gb": budget / 1e9, "rates": {}}
+    out = {"window_s": window, "budget_gb": budget / 1e9, "pool_fields": npool, "rates": {}}
     for rate in rates:
         out["rates"][str(rate)] = {"batched": run(rate, 64, 3), "one_at_a_time": run(rate, 1, 1)}
     return out
@@ -393,6 +400,79 @@ def max_over_ranks(pg, value, device="cpu"):
 def field(side, seed, device):
     from szp_gb300.workloads import fourier3d_torch
     return fourier3d_torch(side, seed, device=device)
+
+
+def config_leg(szp, torch, dev, T, x, eb, peak, reps=6):
+    """One of the other single-field configurations through the device API:
+    x (host float32) uploaded once, then compress + decompress round trips at
+    ABS bound eb, CUDA-event kernel times (first two round trips dropped).
+    GB/s are uncompressed bytes (4n) per device time; each kernel's achieved
+    bandwidth counts its algorithmic bytes (compress: 4n read + stream
+    written; locate: stream read + 4 B per block written; decode: stream and
+    block positions read + 4n written)."""
+    n = x.size
+    dx = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float32)).to(dev)
+    cap = szp.max_stream_bytes(n, L, T, 1)
+    ds = torch.empty(cap, dtype=torch.uint8, device=dev)
+    dy = torch.empty(n, dtype=torch.float32, device=dev)
+    dsz = torch.zeros(1, dtype=torch.int64, device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    size = szp.compress_dev(dx.data_ptr(), n, ds.data_ptr(), cap, szp.ABS, eb, 0.0, L, T, 1, st)
+    szp.set_timing(True)
+    for i in range(reps + 2):
+        if i == 2:
+            torch.cuda.synchronize()
+            for slot in range(5):
+                szp.kernel_time(slot)
+        szp.compress_dev_async(dx.data_ptr(), n, ds.data_ptr(), cap, dsz.data_ptr(), szp.ABS, eb, 0.0, L, T, 1, st)
+        szp.decompress_dev_async(ds.data_ptr(), cap, dsz.data_ptr(), n, dy.data_ptr(), L, T, 1, st)
+    torch.cuda.synchronize()
+    assert szp.sync_status(st) == 0, szp.last_error()
+    kt = {name: szp.kernel_time(slot) for slot, name in
+          enumerate(["rel_range", "compress", "dec_setup", "locate", "decode"])}
+    szp.set_timing(False)
+    avg = {k: v[0] / v[1] for k, v in kt.items() if v[1]}
+    nb = 4.0 * n / L
+    alg = {"compress": 4.0 * n + size, "locate": size + nb, "decode": size + nb + 4.0 * n}
+    comp = avg["compress"]
+    dec = avg.get("dec_setup", 0) + avg["locate"] + avg["decode"]
+    err = float((dx - dy).abs().max())
+    return {"n": n, "abs_eb": eb, "stream_bytes": int(size), "ratio": round(4.0 * n / size, 3),
+            "compress_gbs": round(4.0 * n / (comp / 1e3) / 1e9, 2),
+            "decompress_gbs": round(4.0 * n / (dec / 1e3) / 1e9, 2),
+            "round_trip_gbs": round(4.0 * n / ((comp + dec) / 1e3) / 1e9, 2),
+            "kernels_ms": {k: round(v, 4) for k, v in avg.items()},
+            "roofline": {k: {"achieved_gbs": round(alg[k] / (avg[k] / 1e3) / 1e9, 1),
+                             "frac": round(alg[k] / (avg[k] / 1e3) / 1e9 / peak, 3),
+                             "alg_bytes": int(alg[k])} for k in alg},
+            "max_abs_err_over_eb": round(err / float(np.float32(eb)), 4)}
+
+
+def config_legs(szp, torch, dev, T, peak):
+    """The 2^24-value random walk at ABS 1e-4 of its range and the 8192^2
+    Laplace field with 40% zero blocks at ABS 1e-5, the seeded inputs of the
+    full-size parity tests."""
+    from szp_gb300.workloads import walk, laplace_zero_patches
+    w = walk(1 << 24, np.random.default_rng(1))
+    eb = float(np.float32(1e-4 * (float(w.max()) - float(w.min()))))
+    out = {"walk2^24": dict(config_leg(szp, torch, dev, T, w, eb, peak), bound="ABS 1e-4 of the range")}
+    del w
+    z = laplace_zero_patches(8192, 8192, np.random.default_rng(3)).ravel()
+    zb = z[1:1 + ((z.size - 1) // L) * L].reshape(-1, L)
+    leg = config_leg(szp, torch, dev, T, z, 1e-5, peak)
+    leg["bound"] = "ABS 1e-5"
+    leg["zero_block_fraction"] = round(float((zb == 0).all(axis=1).mean()), 3)
+    out["laplace8192^2"] = leg
+    return out
+
+
+def cpu_port_median(port, x, T, reps=10, warmup=2, rels=RELS):
+    """Oracle round trips on x at T segments and threads (REL bounds in
+    turn): 2 warm-ups, then the median of reps; seconds per round trip."""
+    for i in range(warmup):
+        cpu_port_roundtrip(port, x, rels[i % len(rels)], T)
+    t = [cpu_port_roundtrip(port, x, rels[i % len(rels)], T) for i in range(reps)]
+    return statistics.median(t)
 
 
 def cpu_port_roundtrip(port, x, rel, T, reps=1):
@@ -445,7 +525,11 @@ def cpu_row_baselines(port, xs, T, reps=2):
 
 
 def run_reference(args, rank, world, pg):
-    """The reference's CPU algorithm on the host cores (rank 0 only)."""
+    """The reference's CPU algorithm (the oracle restatement; the reference's
+    own sources are not where the benchmark runs) on the host cores, rank 0
+    only: each step one round trip of the full field at T = all host threads,
+    REL bounds in turn; then the median of 10 round trips at T = 1 (REL 1e-3)
+    after 2 warm-ups."""
     if rank != 0:
         return
     import torch
@@ -453,24 +537,27 @@ def run_reference(args, rank, world, pg):
     port = Port()
     T = port.max_threads()
     dev = "cuda" if torch.cuda.is_available() else "cpu"
-    x = field(args.side, 2, dev).cpu().numpy()
-    xs = np.ascontiguousarray(x[:CPU_SAMPLE])
+    x = np.ascontiguousarray(field(args.side, 2, dev).cpu().numpy())
     for i in range(args.warmup):
-        cpu_port_roundtrip(port, xs, RELS[i % 3], T)
+        cpu_port_roundtrip(port, x, RELS[i % 3], T)
     times = []
     for i in range(args.steps):
-        times.append(cpu_port_roundtrip(port, xs, RELS[i % 3], T))
+        times.append(cpu_port_roundtrip(port, x, RELS[i % 3], T))
     total = sum(times)
-    gbs = 4.0 * xs.size * args.steps / total / 1e9
+    gbs = 4.0 * x.size * args.steps / total / 1e9
+    t1 = cpu_port_median(port, x, 1, reps=10, warmup=2, rels=(1e-3,))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "median_ms_per_step": round(1e3 * statistics.median(times), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32->int32",
-        "data": "synthetic (seeded %d^3 Fourier field, first 2^25 values)" % args.side,
+        "data": "synthetic (seeded %d^3 Fourier field)" % args.side,
         "config": {"workload": "fourier%d^3 REL {1e-2,1e-3,1e-4} blockSize 32 fastmode1 round trip" % args.side,
-                   "n": int(xs.size), "segments": T, "block_size": L, "l2": "inputs > L2"},
+                   "n": int(x.size), "segments": T, "block_size": L, "l2": "inputs > L2"},
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": T, "kind": "port",
-                         "sample": "2^25 floats of the %d^3 field, compress+decompress per step" % args.side},
+                         "sample": "the full %d^3 field, one compress+decompress per step" % args.side,
+                         "t1": {"value": round(4.0 * x.size / t1 / 1e9, 3), "unit": "GB/s", "cores": 1,
+                                "sample": "the full field at T = 1, REL 1e-3, median of 10 after 2 warm-ups"}},
         "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -614,6 +701,23 @@ def main():
         e2e = {"value": round(world * 4.0 * n * args.steps / dt / 1e9, 3), "unit": "GB/s",
                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps),
                "api": "szp_compress + szp_decompress (C ABI via ctypes; pinned input, library-malloc'd results)"}
+        # the same with the input in ordinary malloc'd (pageable) memory, as
+        # the reference's example drivers pass it
+        hx_pinned = hx
+        hx = torch.from_numpy(np.ascontiguousarray(hx_pinned.numpy()).copy())
+        del hx_pinned
+        p, q, sz = host_step(0)
+        libc.free(p)
+        libc.free(q)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            p, q, sz = host_step(i)
+            libc.free(p)
+            libc.free(q)
+        dt = time.perf_counter() - t0
+        e2e["pageable"] = {"value": round(world * 4.0 * n * args.steps / dt / 1e9, 3), "unit": "GB/s",
+                           "api": "the same calls on a malloc'd (pageable) input array"}
+        del hx
 
     # fastmode2 (SZP_RANDOMACCESS: a seed per block) on the same field, REL 1e-3
     fm2 = None
@@ -718,6 +822,10 @@ def main():
                   "metric": "uncompressed bytes of both fields per device time of the sum"}
         del bufs
 
+    configs = None
+    if not args.no_configs:
+        configs = config_legs(szp, torch, dev, T, peak)
+
     batched = None
     if not args.no_batched:
         batched = batched_workload(szp, torch, dev, T, args.batched_fields)
@@ -731,11 +839,12 @@ def main():
         from oracle.oracle import Port
         port = Port()
         Tc = port.max_threads()
+        xf = np.ascontiguousarray(x.cpu().numpy())
+        sec = cpu_port_median(port, xf, Tc)
+        cpu = {"value": round(4.0 * xf.size / sec / 1e9, 3), "unit": "GB/s", "cores": Tc, "kind": "port",
+               "sample": "the full field, REL 1e-2/1e-3/1e-4 round trips in turn, median of 10 after 2 warm-ups"}
+        del xf
         xs = np.ascontiguousarray(x[:CPU_SAMPLE].cpu().numpy())
-        cpu_port_roundtrip(port, xs, 1e-3, Tc)
-        sec = cpu_port_roundtrip(port, xs, 1e-3, Tc, reps=3)
-        cpu = {"value": round(4.0 * xs.size / sec / 1e9, 3), "unit": "GB/s", "cores": Tc, "kind": "port",
-               "sample": "2^25 floats of the field, REL 1e-3 round trip, best of 3"}
         # the oracle beside each further row's GPU number
         rows = cpu_row_baselines(port, xs, Tc)
         for key, leg in (("fastmode2", fm2), ("float64", f64), ("reduce", reduce)):
@@ -764,6 +873,7 @@ def main():
             "fastmode2": fm2,
             "float64": f64,
             "reduce": reduce,
+            "configs": configs,
             "batched": batched,
             "serving": serving,
             "gpu_launches": int(launches),
