@@ -260,8 +260,7 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
   extern __shared__ __align__(16) uint8_t s_bytes[];
   __shared__ uint32_t s_tk[2];
   __shared__ uint32_t s_h[NT], s_x[NT], s_k[NT];
-  __shared__ uint2 s_aux[NT];
-  __shared__ uint64_t s_val[NT];
+  __shared__ uint64_t s_val[1];
   __shared__ uint32_t s_misc[2 * (NT / 32)];
   __shared__ __align__(8) uint64_t s_bar;
   uint32_t tile, epoch;
@@ -319,16 +318,17 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
   ch.fm2 = FM2;
 
   // ---- speculative walk of each thread's chunk ----
-  // One flat loop advances every lane by one header per iteration, so a warp
-  // stays converged and costs the longest walk of its lanes (nested restart
-  // loops would run the lanes one after another).  A lane's chain starts at
-  // `anchor`; the first position >= cS is the chunk's entry, headers in
+  // A lane's chain starts at `anchor` (a segment's first chunk: at its first
+  // header); the first position >= cS on it is the chunk's entry, headers in
   // [cS, cE) are counted, and the first position >= cE is its exit.  A chain
-  // that meets an invalid header restarts one byte later.
+  // that meets an invalid header restarts one byte after its anchor.  Each
+  // lane runs its own loop of single header steps: lanes finish at different
+  // times, but an iteration is a handful of instructions (a lockstep loop that
+  // applied every outcome with selects cost several times as much).
   const uint32_t nactive = (scE - scS + C - 1) / C;
   const uint32_t cS = scS + tid * C, cE = min(cS + C, scE);
   uint32_t h = kPosEnd, x = kPosEnd, k = 0;
-  {
+  if ((uint32_t)tid < nactive) {
     const bool known = j == 0 && tid == 0;  // a segment's block region starts with a header
     // a wrong guess is caught by the chain checks (inside the CTA, or across
     // CTAs for its first chunk) and re-walked from the true exit
@@ -336,37 +336,34 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
     uint32_t anchor = known ? 0u : (cS > st0 + W ? cS - W : st0);
     uint32_t pos = anchor, entry = anchor >= cS ? anchor : kPosDead, cnt = 0;
     uint32_t budget = 4 * (W + C);
-    bool done = (uint32_t)tid >= nactive;
-    if (!done) {
-      h = kPosDead;
-      x = kPosDead;
+    bool broken = false;
+    h = kPosDead;
+    x = kPosDead;
+    while (pos < cE && budget != 0) {
+      budget--;
+      const uint32_t sz = ch.step(pos);
+      if (sz) {
+        cnt += pos >= cS ? 1u : 0u;
+        const uint32_t np = pos + sz;
+        if (entry == kPosDead && np >= cS) entry = np;
+        pos = np;
+      } else if (!known && anchor + 1 < cE) {
+        anchor++;
+        pos = anchor;
+        cnt = 0;
+        entry = anchor >= cS ? anchor : kPosDead;
+      } else {
+        broken = true;
+        break;
+      }
     }
-    while (__any_sync(0xffffffffu, !done)) {
-      // one header step for every lane still inside its chunk; the outcome is
-      // applied with selects, so the warp takes one path per iteration
-      const bool walking = !done && pos < cE && budget != 0;
-      const uint32_t sz = walking ? ch.step(pos) : 0u;
-      budget -= walking ? 1u : 0u;
-      const bool adv = walking && sz != 0, dead = walking && sz == 0;
-      const bool restart = dead && !known && anchor + 1 < cE;
-      cnt = restart ? 0u : cnt + ((adv && pos >= cS) ? 1u : 0u);
-      const uint32_t np = pos + sz;
-      entry = (adv && entry == kPosDead && np >= cS) ? np : entry;
-      anchor += restart ? 1u : 0u;
-      entry = restart ? (anchor >= cS ? anchor : kPosDead) : entry;
-      pos = restart ? anchor : (adv ? np : pos);
-      const bool reached = !done && pos >= cE;
-      const bool gaveup = !done && !reached && (budget == 0 || (dead && !restart));
-      if (reached) {
-        h = entry >= rlen ? kPosEnd : entry;
-        x = pos >= rlen ? kPosEnd : pos;
-        k = cnt;
-      }
-      if (gaveup && dead && known) {
-        h = 0;
-        k = cnt;  // x stays kPosDead: the true chain is broken
-      }
-      done = done || reached || gaveup;
+    if (pos >= cE) {
+      h = entry >= rlen ? kPosEnd : entry;
+      x = pos >= rlen ? kPosEnd : pos;
+      k = cnt;
+    } else if (broken && known) {
+      h = 0;
+      k = cnt;  // x stays kPosDead: the true chain is broken
     }
   }
   s_h[tid] = h;
@@ -388,7 +385,8 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
     __syncthreads();
   }
 
-  // ---- look-back over header counts, verifying entries ----
+  // ---- look-back over header counts, verifying entries (warp 0; the
+  // other warps wait at the barrier after it) ----
   uint32_t K = 0;
   for (int i = 0; i < NT; i++) K += s_k[i];  // shared reads, same in every thread
   uint32_t h0 = s_h[0], xl = s_x[nactive - 1];
@@ -405,120 +403,114 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
       __threadfence();
       st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, K));
     }
-    uint32_t spins = 0;
-    while (true) {
-      // window: thread i reads tile-1-i (seqlock read of status + aux)
-      int64_t base = (int64_t)tile - 1;
+    if (warp == 0) {
+      // lane l reads tile base - l (seqlock read of status + aux); a window
+      // whose entries are not all ready, or whose chain of (entry, exit)
+      // pairs is broken (an older tile will repair itself), is read again
+      // after a pause
+      uint32_t spins = 0;
+      int verdict = 0;  // 1 done, 2 retry, 3 repair self
       uint64_t acc = 0;
-      uint32_t need_x = h0;       // exit the next-older tile must have
-      uint32_t pred_x = kPosDead;  // exit of the tile just before this one
-      int verdict = 0;             // 1 done, 2 retry, 3 repair self
-      bool self_ok = true;
+      uint32_t pred_x = kPosDead;
       while (true) {
-        const int64_t idx = base - tid;
-        bool inr = idx >= (int64_t)first;
-        uint64_t s1 = 0, s2 = 0;
-        uint2 ax = make_uint2(0, 0);
-        bool ready = true, incl = false;
-        if (inr) {
-          // seqlock read: acquire loads keep the aux read between the two status reads
-          s1 = ld_acquire_u64(a.status + idx);
-          const uint64_t axw = ld_acquire_u64(reinterpret_cast<const uint64_t*>(a.aux + idx));
-          ax = make_uint2((uint32_t)axw, (uint32_t)(axw >> 32));
-          s2 = ld_volatile_u64(a.status + idx);
-          const uint64_t f = status_flag(s1);
-          ready = s1 == s2 && status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
-          incl = ready && f == kFlagInclusive;
-        }
-        s_aux[tid] = ax;
-        s_val[tid] = inr ? status_value(s1) : 0;
-        const int nearest = __syncthreads_or(incl) ? 1 : 0;
-        // nearest inclusive and readiness of everything before it
-        uint32_t jstar = NT;
-        if (nearest) {
+        int64_t base = (int64_t)tile - 1;
+        uint32_t need_x = h0;  // exit the next-older tile must have
+        bool self_ok = true;
+        acc = 0;
+        while (true) {
+          const int64_t idx = base - lane;
+          const bool inr = idx >= (int64_t)first;
+          uint64_t s1 = 0;
+          uint2 ax = make_uint2(0, 0);
+          bool ready = true, incl = false;
+          if (inr) {
+            // acquire loads keep the aux read between the two status reads
+            s1 = ld_acquire_u64(a.status + idx);
+            const uint64_t axw = ld_acquire_u64(reinterpret_cast<const uint64_t*>(a.aux + idx));
+            ax = make_uint2((uint32_t)axw, (uint32_t)(axw >> 32));
+            const uint64_t s2 = ld_volatile_u64(a.status + idx);
+            const uint64_t f = status_flag(s1);
+            ready = s1 == s2 && status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
+            incl = ready && f == kFlagInclusive;
+          }
           const uint32_t bi = __ballot_sync(0xffffffffu, incl);
-          if (lane == 0) s_misc[warp] = bi ? (uint32_t)(warp * 32 + __ffs(bi) - 1) : (uint32_t)NT;
-          __syncthreads();
-          for (int w = 0; w < NT / 32; w++) jstar = min(jstar, s_misc[w]);
-          __syncthreads();
-        }
-        const bool relevant = inr && (uint32_t)tid <= jstar;
-        if (__syncthreads_or(relevant && !ready)) {
-          verdict = 2;
-          break;
-        }
-        // chain checks: the entry of thread i's tile must be the exit of the
-        // next older tile (thread i+1); the inclusive tile is already verified
-        bool broken = false;
-        if (relevant && (uint32_t)tid < jstar && tid + 1 < NT && idx - 1 >= (int64_t)first) {
-          const uint32_t e = ax.x, ox = s_aux[tid + 1].y;
-          broken = (ox == kPosEnd) ? (e != kPosEnd) : (e != ox);
-        }
-        if (__syncthreads_or(broken)) {
-          verdict = 2;  // an older tile's entry is wrong: it will repair itself
-          break;
-        }
-        if (base == (int64_t)tile - 1) {
-          // our own entry against the nearest predecessor's exit
-          const uint32_t px = s_aux[0].y;
-          self_ok = (px == kPosEnd) ? (h0 == kPosEnd && K == 0) : (px == h0);
-          pred_x = px;
-        } else {
-          // window boundary: the nearest of this window must exit where the
-          // farthest of the previous window entered
-          const uint32_t px = s_aux[0].y;
-          if (!((px == kPosEnd) ? (need_x == kPosEnd) : (px == need_x))) {
+          const int jstar = bi ? __ffs(bi) - 1 : 32;  // nearest inclusive of the window
+          const bool relevant = inr && lane <= jstar;
+          if (__any_sync(0xffffffffu, relevant && !ready)) {
             verdict = 2;
             break;
           }
+          // the entry of lane l's tile must be the exit of the next older
+          // tile (lane l + 1); the inclusive tile is already verified
+          const uint32_t ox = __shfl_down_sync(0xffffffffu, ax.y, 1);
+          bool bad = false;
+          if (relevant && lane < jstar && lane < 31 && idx - 1 >= (int64_t)first)
+            bad = (ox == kPosEnd) ? (ax.x != kPosEnd) : (ax.x != ox);
+          if (__any_sync(0xffffffffu, bad)) {
+            verdict = 2;
+            break;
+          }
+          const uint32_t px = __shfl_sync(0xffffffffu, ax.y, 0);
+          if (base == (int64_t)tile - 1) {
+            // our own entry against the nearest predecessor's exit
+            self_ok = (px == kPosEnd) ? (h0 == kPosEnd && K == 0) : (px == h0);
+            pred_x = px;
+          } else if (!((px == kPosEnd) ? (need_x == kPosEnd) : (px == need_x))) {
+            // window boundary: the nearest of this window must exit where the
+            // farthest of the previous window entered
+            verdict = 2;
+            break;
+          }
+          uint64_t v = relevant ? status_value(s1) : 0;
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          acc += v;
+          const uint32_t far_h = __shfl_sync(0xffffffffu, ax.x, 31);
+          if (jstar < 32 || base - 32 < (int64_t)first) {
+            verdict = self_ok ? 1 : 3;
+            break;
+          }
+          need_x = far_h;
+          base -= 32;
         }
-        // sum the counts of the relevant window entries
-        uint64_t v = relevant ? s_val[tid] : 0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) s_misc[NT / 32 + warp] = (uint32_t)v;  // per-warp partials (< 2^32)
-        __syncthreads();
-        uint64_t tot = 0;
-        for (int w = 0; w < NT / 32; w++) tot += s_misc[NT / 32 + w];
-        const uint32_t far_h = s_aux[NT - 1].x;
-        __syncthreads();
-        acc += tot;
-        if (jstar < (uint32_t)NT || base - NT < (int64_t)first) {
-          verdict = self_ok ? 1 : 3;
-          break;
-        }
-        need_x = far_h;
-        base -= NT;
-      }
-      if (verdict == 2) {
+        if (verdict != 2) break;
         if (++spins > kSpinLimit) {
-          if (tid == 0) atomicOr(a.err, kErrLookbackTimeout);
+          if (lane == 0) atomicOr(a.err, kErrLookbackTimeout);
           break;
         }
-        continue;
+        __nanosleep(200);
       }
-      if (verdict == 3) {
-        // our speculative entry was wrong: re-walk from the verified exit
-        if (tid == 0) {
-          st_release_u64(a.status + tile, make_status(epoch, kFlagRepair, 0));
-          __threadfence();
-          s_h[0] = pred_x == kPosDead ? kPosEnd : kPosDead;  // differs from the entry: chunk 0 is re-walked
-          rewalk_from(ch, s_h, s_x, s_k, 0, pred_x, nactive, scS, scE, C);
-          atomicAdd(&a.counters[0], 1u);
-        }
-        __syncthreads();
-        K = 0;
-        for (int i = 0; i < NT; i++) K += s_k[i];
-        h0 = s_h[0];
-        xl = s_x[nactive - 1];
-        if (tid == 0) {
-          a.aux[tile] = make_uint2(h0, xl);
-          __threadfence();
-        }
+      if (lane == 0) {
+        s_misc[0] = (uint32_t)verdict;
+        s_misc[1] = pred_x;
+        s_val[0] = acc;
       }
-      prefix = acc;
-      if (tid == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, prefix + K));
-      break;
     }
+    __syncthreads();
+    const int verdict = (int)s_misc[0];
+    const uint32_t pred_x = s_misc[1];
+    const uint64_t acc = s_val[0];
+    __syncthreads();  // s_misc and s_val are reused below
+    if (verdict == 3) {
+      // our speculative entry was wrong: re-walk from the verified exit
+      if (tid == 0) {
+        st_release_u64(a.status + tile, make_status(epoch, kFlagRepair, 0));
+        __threadfence();
+        s_h[0] = pred_x == kPosDead ? kPosEnd : kPosDead;  // differs from the entry: chunk 0 is re-walked
+        rewalk_from(ch, s_h, s_x, s_k, 0, pred_x, nactive, scS, scE, C);
+        atomicAdd(&a.counters[0], 1u);
+      }
+      __syncthreads();
+      K = 0;
+      for (int i = 0; i < NT; i++) K += s_k[i];
+      h0 = s_h[0];
+      xl = s_x[nactive - 1];
+      if (tid == 0) {
+        a.aux[tile] = make_uint2(h0, xl);
+        __threadfence();
+      }
+    }
+    prefix = acc;
+    if (tid == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, prefix + K));
   }
   // ---- header offsets of every block of every chunk ----
   uint32_t kx = s_k[tid];
