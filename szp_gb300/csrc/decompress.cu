@@ -663,7 +663,15 @@ constexpr int kDecRounds = 4;
 //             deltas of the tiles before it, szpd_float.cc:76-118) while the
 //             compute warps unpack the next tile
 // ---------------------------------------------------------------------------
-constexpr int kDecSlots = 3, kDecControl = 2;
+constexpr int kDecControl = 2;
+// Slots of a decode pipeline with ROUNDS rounds per warp: a tile is finished
+// (dequantized and stored) NS - 2 tiles after it was staged, so that its
+// base (the look-back over the tiles before it) has that long to arrive.
+// Tiles of 2 rounds (half the shared memory of 4) get 6 slots, 4 tiles of slack.
+template <int ROUNDS>
+__host__ __device__ constexpr int dec_slots() {
+  return ROUNDS >= 4 ? 3 : 6;
+}
 constexpr int kDecPipeThreads = (8 + kDecControl + 1) * 32;
 
 struct DecSlot {
@@ -782,10 +790,64 @@ __device__ __forceinline__ void lds_le64(const uint8_t* b, uint32_t o, uint32_t&
   hi = __funnelshift_r(w1, w2, sh);
 }
 
+// The aligned middle of cta_dequant_store, compiled per 16-byte phase PH of
+// dst and per SPECIAL (eb not finite: the x86 NaN rule is applied): output
+// chunk c (4 floats) takes stage words [4c - PH, 4c - PH + 4), picked from
+// two aligned lines by fixed register moves.
+template <bool CODES, bool ACC, int PH, bool SPECIAL>
+__device__ __forceinline__ void cta_dequant_chunks(float* __restrict__ g0, const uint32_t* __restrict__ stage,
+                                                   uint32_t c0, uint32_t c1, uint32_t base, float eb, bool& wrap,
+                                                   uint32_t tid) {
+  auto dq = [eb](uint32_t q) -> float { return CODES ? __uint_as_float(q) : dequant(q, eb, SPECIAL); };
+  auto acc = [&wrap](float old, uint32_t q) -> float {  // old + q as int32 codes
+    const int32_t x = (int32_t)__float_as_uint(old), y = (int32_t)q;
+    const int32_t z = (int32_t)((uint32_t)x + (uint32_t)y);
+    wrap |= ((x ^ z) & (y ^ z)) < 0;
+    return __uint_as_float((uint32_t)z);
+  };
+  const uint4* s4 = reinterpret_cast<const uint4*>(stage);
+  // four chunks per thread per pass: their shared-memory loads are in flight together
+  constexpr int U = 4;
+  for (uint32_t cb = c0; cb < c1; cb += 256 * U) {
+    uint4 w[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint32_t c = min(cb + tid + 256 * u, c1 - 1);  // clamped: always a readable chunk
+      if constexpr (PH == 0) {
+        w[u] = s4[c];
+      } else {
+        const uint4 a = s4[c - 1], b = s4[c];  // stage words [4c-4, 4c+4)
+        const uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        w[u] = make_uint4(v[4 - PH], v[5 - PH], v[6 - PH], v[7 - PH]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint32_t c = cb + tid + 256 * u;
+      if (c < c1) {
+        float4 o;
+        if (ACC) {
+          const float4 p = reinterpret_cast<const float4*>(g0)[c];
+          o.x = acc(p.x, base + w[u].x);
+          o.y = acc(p.y, base + w[u].y);
+          o.z = acc(p.z, base + w[u].z);
+          o.w = acc(p.w, base + w[u].w);
+        } else {
+          o.x = dq(base + w[u].x);
+          o.y = dq(base + w[u].y);
+          o.z = dq(base + w[u].z);
+          o.w = dq(base + w[u].w);
+        }
+        reinterpret_cast<float4*>(g0)[c] = o;
+      }
+    }
+  }
+}
+
 // The 256 compute threads: y[e] = dequant(base + stage[e - e0]) for the
 // tile's nel elements starting at dst = y + e0; 16-byte stores for the aligned
-// middle, the words picked from two aligned shared-memory lines when dst is not
-// 16-byte aligned.  stage is 16-byte aligned and readable for nel + 4 words.
+// middle (cta_dequant_chunks), plain stores at the ragged ends.  stage is
+// 16-byte aligned and readable for nel + 4 words.
 // CODES: the quantization codes themselves are stored (their bits), for the
 // homomorphic reduction; with ACC they are added to the codes already in dst
 // (wrapping int32; a wrap sets kErrQuantRange in *err).
@@ -813,42 +875,19 @@ __device__ __forceinline__ void cta_dequant_store(float* __restrict__ dst, const
   } else {
     if (tid < 4 * c0 - ph) put(g0 + ph + tid, base + stage[tid]);
     if (tid >= 32 && tid - 32 < end - 4 * c1) put(g0 + 4 * c1 + tid - 32, base + stage[4 * c1 + tid - 32 - ph]);
-    const uint4* s4 = reinterpret_cast<const uint4*>(stage);
-    // four chunks per thread per pass: their shared-memory loads are in flight together
-    constexpr int U = 4;
-    for (uint32_t cb = c0; cb < c1; cb += 256 * U) {
-      uint4 w[U];
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const uint32_t c = min(cb + tid + 256 * u, c1 - 1);  // clamped: always a readable chunk
-        if (ph == 0) {
-          w[u] = s4[c];
-        } else {
-          const uint4 a = s4[c - 1], b = s4[c];  // stage words [4c-4, 4c+4); chunk c wants [4c-ph, 4c-ph+4)
-          if (ph == 1) w[u] = make_uint4(a.w, b.x, b.y, b.z);
-          else if (ph == 2) w[u] = make_uint4(a.z, a.w, b.x, b.y);
-          else w[u] = make_uint4(a.y, a.z, a.w, b.x);
-        }
+    if (!CODES && ebsp) {  // eb not finite
+      switch (ph) {
+        case 0: cta_dequant_chunks<CODES, ACC, 0, true>(g0, stage, c0, c1, base, eb, wrap, tid); break;
+        case 1: cta_dequant_chunks<CODES, ACC, 1, true>(g0, stage, c0, c1, base, eb, wrap, tid); break;
+        case 2: cta_dequant_chunks<CODES, ACC, 2, true>(g0, stage, c0, c1, base, eb, wrap, tid); break;
+        default: cta_dequant_chunks<CODES, ACC, 3, true>(g0, stage, c0, c1, base, eb, wrap, tid); break;
       }
-#pragma unroll
-      for (int u = 0; u < U; u++) {
-        const uint32_t c = cb + tid + 256 * u;
-        if (c < c1) {
-          float4 o;
-          if (ACC) {
-            const float4 p = reinterpret_cast<const float4*>(g0)[c];
-            o.x = acc(p.x, base + w[u].x);
-            o.y = acc(p.y, base + w[u].y);
-            o.z = acc(p.z, base + w[u].z);
-            o.w = acc(p.w, base + w[u].w);
-          } else {
-            o.x = dq(base + w[u].x);
-            o.y = dq(base + w[u].y);
-            o.z = dq(base + w[u].z);
-            o.w = dq(base + w[u].w);
-          }
-          reinterpret_cast<float4*>(g0)[c] = o;
-        }
+    } else {
+      switch (ph) {
+        case 0: cta_dequant_chunks<CODES, ACC, 0, false>(g0, stage, c0, c1, base, eb, wrap, tid); break;
+        case 1: cta_dequant_chunks<CODES, ACC, 1, false>(g0, stage, c0, c1, base, eb, wrap, tid); break;
+        case 2: cta_dequant_chunks<CODES, ACC, 2, false>(g0, stage, c0, c1, base, eb, wrap, tid); break;
+        default: cta_dequant_chunks<CODES, ACC, 3, false>(g0, stage, c0, c1, base, eb, wrap, tid); break;
       }
     }
   }
@@ -954,7 +993,8 @@ __device__ __forceinline__ void dec_control(int c, const DecArgs& a, const DecSl
 template <int LPB, bool BATCH, int ROUNDS, bool FM2 = false, int OUT = kOutFloat>
 __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_constant__ DecArgs a,
                                                                   uint32_t slot_bytes) {
-  constexpr int NS = kDecSlots, NC = kDecControl, WARPS = 8;
+  constexpr int NS = dec_slots<ROUNDS>(), NC = kDecControl, WARPS = 8;
+  constexpr uint32_t DEFER = NS - 2;  // fastmode1: tiles between staging a tile and finishing it
   // a control warp's next position must never share a slot phase it has not
   // waited for (an mbarrier parity names one of two phases)
   static_assert(NC <= NS, "more control warps than slots");
@@ -999,8 +1039,9 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
   }
 
   // ---- compute warps ----
-  // Tile k is unpacked and staged, then tile k-1 (whose base the control warps
-  // have looked up meanwhile) is finished: base added, dequantized, stored.
+  // Tile k is unpacked and staged, then tile k - DEFER (whose base the
+  // control warps have looked up meanwhile) is finished: base added,
+  // dequantized, stored.
   const int sub = lane % LPB, grp = lane / LPB;
   const uint32_t wfirst = (uint32_t)warp * ROUNDS * BPR;
   auto finish = [&](uint32_t kp) {
@@ -1026,7 +1067,8 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
     const uint32_t tile = s_meta[s].tile;
     if (threadIdx.x == 0) s_started = k + 1;
     if (tile >= a.ntiles) {
-      if (!FM2 && k) finish(k - 1);  // fastmode2 tiles are finished at once
+      if (!FM2)  // fastmode2 tiles are finished at once
+        for (uint32_t j = k > DEFER ? k - DEFER : 0u; j < k; j++) finish(j);
       return;
     }
     const uint32_t nblk = s_meta[s].nblk, nel = s_meta[s].nel, span0 = s_meta[s].span0;
@@ -1250,7 +1292,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
       }
     }
     compute_sync();  // staged; s_w is free for the next tile
-    if (k) finish(k - 1);
+    if (k >= DEFER) finish(k - DEFER);
   }
 }
 
@@ -1512,7 +1554,7 @@ template <int LPB, bool BATCH = false, int ROUNDS = kDecRounds, bool FM2 = false
 static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
   auto k = decode_pipe<LPB, BATCH, ROUNDS, FM2, OUT>;
   const uint32_t slot = dec_slot_bytes(8 * LPB, a.tb, a.maxsz);
-  const size_t smem = (size_t)kDecSlots * slot;
+  const size_t smem = (size_t)dec_slots<ROUNDS>() * slot;
   // resident CTAs of this instance, cached per device as (device + 1) << 32 | CTAs
   static std::atomic<uint64_t> s_cache{0};
   int dev = 0;
