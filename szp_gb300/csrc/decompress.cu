@@ -339,9 +339,13 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
     bool broken = false;
     h = kPosDead;
     x = kPosDead;
+    const uint8_t* sb = ch.sb - ch.base0;  // region offset p at sb[p]
+    const bool b32 = !FM2 && ch.l8 == 4;  // blockSize 32: a block of 1 or 4b + 5 bytes
     while (pos < cE && budget != 0) {
       budget--;
-      const uint32_t sz = ch.step(pos);
+      // every position read is below cE, inside the staged bytes
+      const uint32_t b = sb[pos];
+      const uint32_t sz = b32 ? (b > (uint32_t)kMaxBitCount ? 0u : (b ? 4 * b + 5 : 1u)) : ch.step(pos);
       if (sz) {
         cnt += pos >= cS ? 1u : 0u;
         const uint32_t np = pos + sz;
