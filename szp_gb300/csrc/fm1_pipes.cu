@@ -73,8 +73,9 @@ struct C32Meta {
   uint32_t has_seg;     // the stream has elements
 };
 
-// What the control warp needs of a packed tile: written by compute thread 0
-// before its warp's arrival on the record's barrier.
+// What the control warp needs of a tile, written by compute thread 0 once the
+// tile's packed size is known (before it is packed); the control warp's
+// stream position comes back in gpos.
 struct C32Rec {
   uint64_t end;    // ring bytes allocated up to and including this tile
   uint64_t gpos;   // stream position, written by the control warp (~0: does not fit)
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
       mbar_init(&s_empty[s], 1);
     }
     for (int p = 0; p < kRecs; p++) {
-      mbar_init(&s_recb[p], kW);  // one arrival per compute warp
+      mbar_init(&s_recb[p], 1);  // compute thread 0, once the tile's size is known
       mbar_init(&s_based[p], 1);
     }
     s_stop_k = kStopTile;
@@ -472,6 +473,10 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
     const C32Meta g = s_meta[s];
     if (g.tile >= a.ntiles) {
       if (tid == 0) s_cstop_k = k;  // the control warp ends after the tiles before k
+      // a tile's position does not mean it is packed: every warp has packed
+      // tile k - 1 after this barrier (the tiles before it are older than
+      // one barrier already)
+      compute_sync();
       for (; ncopy < k; ncopy++) copy_out(ncopy);
       return;
     }
@@ -585,6 +590,7 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
       r.first = g.has_seg && g.first;
       r.agg = agg;
       r.rpos = rpos;
+      mbar_arrive(&s_recb[p]);  // the control warp can place the tile while it is packed
       if (seed) {
         out[0] = (uint8_t)seedv;
         out[1] = (uint8_t)((uint32_t)seedv >> 8);
@@ -610,10 +616,8 @@ __global__ void __launch_bounds__(kThreads, 2) compress32_pipe(const __grid_cons
         c32_pack_masked(out + wexcl + off[r], an.v[r], an.sb[r], an.bc[r], sub, min(kL, g.nel - bt * kL));
       }
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&s_recb[p]);  // the warp's share of tile k is packed
-    // ---- copy out the tile packed kDefer tiles ago (its space is released
-    // at the next barrier) ----
+    // ---- copy out the tile packed kDefer tiles ago (every warp packed it
+    // before the last barrier; its space is released at the next one) ----
     if (ncopy + kDefer <= k) copy_out(ncopy++);
   }
 }
