@@ -700,6 +700,12 @@ struct DecSlot {
 // Bytes of the block-offset area at the front of a slot.
 __host__ __device__ constexpr uint32_t dec_pos_bytes(uint32_t tb) { return 4 * tb + 32; }
 
+// Tile order of a decode pipeline launch.  Batched launches draw tickets (a
+// tile's predecessors have then started before it); a single field's launch
+// is cooperative, so all its CTAs are resident and CTA c takes tiles c,
+// c + grid, c + 2 grid, ...: the producer may run ahead as far as its slots
+// allow, and a tile's predecessors are the tiles the other CTAs hold at the
+// same time.
 template <uint32_t L, uint32_t TB, int NS, bool BATCH, bool FM2>
 __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, uint32_t slot_bytes, DecSlot* meta,
                                              uint64_t* full, uint64_t* empty, uint32_t* s_epoch,
@@ -707,14 +713,39 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
   constexpr uint32_t PB = dec_pos_bytes(TB);
   *s_epoch = *(volatile uint32_t*)&a.ls->epoch;
   __threadfence();
-  for (uint32_t k = 0;;) {
+  // the plan of a single field and the region of the current segment, read once
+  uint32_t bad = 0, cseg = 0xFFFFFFFFu;
+  float eb = 0.0f;
+  double ebd = 0.0;
+  if (!BATCH) {
+    bad = a.f.plan->bad;
+    eb = a.f.plan->eb;
+    ebd = a.f.plan->ebd;
+  }
+  uint64_t R0 = 0;
+  uint32_t rlen = 0;
+  for (uint32_t k = 0, j = 0;; j++) {
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
-    // draw the ticket only once the compute warps have started the previous
-    // position: a tile's predecessors are then never more than a tile behind it
-    // in their work, which keeps the look-back short
-    for (uint32_t i = 0; i < kWaitLimit && *s_started < k; i++) __nanosleep(64);
-    const uint32_t tile = draw_ticket_persistent(a.ls, a.ntiles);
+    uint32_t tile;
+    if (BATCH) {
+      // draw the ticket only once the compute warps have started the previous
+      // position: a tile's predecessors are then never more than a tile behind it
+      // in their work, which keeps the look-back short
+      for (uint32_t i = 0; i < kWaitLimit && *s_started < k; i++) __nanosleep(64);
+      tile = draw_ticket_persistent(a.ls, a.ntiles);
+    } else {
+      tile = blockIdx.x + j * gridDim.x;
+      if (tile >= a.ntiles) {
+        // the last CTA to stop advances the epoch (every CTA has read it)
+        const uint32_t t = atomicAdd(&a.ls->ticket, 1u);
+        if (t == gridDim.x - 1) {
+          a.ls->ticket = 0;
+          __threadfence();
+          atomicAdd(&a.ls->epoch, 1u);
+        }
+      }
+    }
     DecSlot& m = meta[s];
     if (tile >= a.ntiles) {
       drain_copies<NS>(full, k);
@@ -726,17 +757,21 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     const DecField& fd = BATCH ? a.fields[a.tile_field[tile]] : a.f;
     const Segments sg = fd.seg;
     const DecTile dt = dec_tile(sg, tile - fd.tile_base, fd.tiles_per_seg, TB, FM2);
+    if (BATCH) bad = fd.plan->bad;
     // nothing to write: a failed plan, an empty segment, a tile past its segment's blocks
     // (fastmode1 keeps a segment's first tile for its seed)
-    if (fd.plan->bad || !dt.any || (dt.nblk == 0 && (FM2 || !dt.first))) continue;  // the slot stays free
+    if (bad || !dt.any || (dt.nblk == 0 && (FM2 || !dt.first))) continue;  // the slot stays free
     const uint64_t lo = sg.lo(dt.seg), hi = sg.hi(dt.seg);
-    const uint64_t R0 = fd.reg0[dt.seg], R1 = fd.reg1[dt.seg];
-    const uint32_t rlen = (uint32_t)(R1 - R0);
+    if (BATCH || dt.seg != cseg) {
+      R0 = fd.reg0[dt.seg];
+      rlen = (uint32_t)(fd.reg1[dt.seg] - R0);
+      cseg = dt.seg;
+    }
     uint8_t* slot = slots + (size_t)s * slot_bytes;
     m.seg = dt.seg;
     m.seg_tile0 = fd.tile_base + (fd.tiles_per_seg ? dt.seg * fd.tiles_per_seg : 0u);
-    m.eb = fd.plan->eb;
-    m.ebd = fd.plan->ebd;
+    m.eb = BATCH ? fd.plan->eb : eb;
+    m.ebd = BATCH ? fd.plan->ebd : ebd;
     m.y = fd.y;
     m.err = fd.err;
     m.nblk = dt.nblk;
@@ -782,6 +817,19 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     }
     k++;
   }
+}
+
+// All ones when byte k of w has its top bit set, else 0 (prmt's sign
+// replication; the __byte_perm intrinsic takes only the selector's low 3 bits).
+__device__ __forceinline__ uint32_t prmt_sign(uint32_t w, int k) {
+  uint32_t r;
+  switch (k) {
+    case 0: asm("prmt.b32 %0, %1, 0, 0x8888;" : "=r"(r) : "r"(w)); break;
+    case 1: asm("prmt.b32 %0, %1, 0, 0x9999;" : "=r"(r) : "r"(w)); break;
+    case 2: asm("prmt.b32 %0, %1, 0, 0xAAAA;" : "=r"(r) : "r"(w)); break;
+    default: asm("prmt.b32 %0, %1, 0, 0xBBBB;" : "=r"(r) : "r"(w)); break;
+  }
+  return r;
 }
 
 // Little-endian bytes [o, o+8) of shared array b as (lo, hi), from three
@@ -1087,18 +1135,31 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
     uint32_t seedv[ROUNDS];  // fastmode2: each block's seed
     uint32_t wtot = 0;
     bool corrupt = false;
+    // FULL: a fastmode1 tile of TB whole blocks (every tile of a segment but
+    // its last); its rounds skip the per-block element counts
+    auto unpack = [&](auto fullc) {
+    constexpr bool FULL = decltype(fullc)::value;
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
       const uint32_t bt = wfirst + r * BPR + grp;
-      const uint32_t mblk = bt < nblk ? min(L, nel - bt * L) : 0u;
+      const uint32_t mblk = FULL ? L : (bt < nblk ? min(L, nel - bt * L) : 0u);
       const uint32_t m = FM2 ? (mblk ? mblk - 1 : 0u) : mblk;  // values packed in the block
-      const uint32_t ml = m > 8u * sub ? min(8u, m - 8u * sub) : 0u;
+      const uint32_t ml = FULL ? 8u : (m > 8u * sub ? min(8u, m - 8u * sub) : 0u);
       uint32_t d[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) d[j] = 0;
       uint32_t off = 0, bc = 0;
       seedv[r] = 0;
-      if (FM2 && mblk) {
+      if (FULL) {
+        // a corrupt offset is kept inside the slot; a block of bit count b
+        // takes 1 + (L/8)(b+1) bytes (1 when b = 0)
+        off = min(bpos[bt] - span0, spanlen);
+        bc = sp[off];
+        if (bc > 33 || off + (bc ? 1 + (L / 8) * (bc + 1) : 1u) > spanlen) {
+          corrupt = true;
+          bc = 0;
+        }
+      } else if (FM2 && mblk) {
         // fastmode2: the block's 4-byte seed, then its header (a one-element
         // block has no header on the decode side, szpd_float.cc:483)
         const uint32_t b0 = bpos[bt] - span0;
@@ -1125,7 +1186,7 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
         }
       }
       constexpr uint32_t MF = FM2 ? L - 1 : L;  // values of a full block
-      if (__all_sync(0xffffffffu, (m == MF || m == 0) && bc <= 15)) {
+      if (__all_sync(0xffffffffu, (FULL || m == MF || m == 0) && bc <= 15)) {
         // every block of the round is full and has at most one byte plane:
         // the lane's plane and remainder bytes come from aligned word loads
         // (fastmode2: L-1 values, the last lane's eighth is not one of them)
@@ -1139,14 +1200,14 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
           if (B) lds_le64(s_slots, ob + 1 + NSB + 8 * sub, plo, phi);  // byte plane, szp_TypeManager.cc:36-52
           const uint32_t t = __byte_perm(lo, 0, 0x0123);  // remainder bits 0..31, MSB first
           const uint32_t t2 = __funnelshift_l(__byte_perm(hi, 0, 0x0123), t, 4 * rr);  // bits 4rr..
-          const uint32_t rs = 32 - rr, pw = 1u << rr;
-          const int32_t sx = (int32_t)(sb << 24);
+          // byte k of sw0 (sw1) has the sign bit of value k (4 + k) as its top bit
+          const uint32_t sw0 = sb * 0x08040201u, sw1 = (sb << 4) * 0x08040201u;
 #pragma unroll
           for (int j = 0; j < 8; j++) {
-            const uint32_t f = __funnelshift_rc((j < 4 ? t : t2) << (rr * (j & 3)), 0u, rs);
+            // value j: its plane byte above its rr remainder bits, in one funnel shift
             const uint32_t h = __byte_perm(j < 4 ? plo : phi, 0, 0x4440 + (j & 3));
-            const uint32_t v = h * pw + f;
-            const uint32_t sg = (uint32_t)((sx << j) >> 31);
+            const uint32_t v = __funnelshift_l((j < 4 ? t : t2) << (rr * (j & 3)), h, rr);
+            const uint32_t sg = prmt_sign(j < 4 ? sw0 : sw1, j & 3);  // 0 or all ones
             d[j] = (FM2 && j == 7 && sub == LPB - 1) ? 0u : (v ^ sg) - sg;
           }
         }
@@ -1195,6 +1256,12 @@ __global__ void __launch_bounds__(kDecPipeThreads, 2) decode_pipe(const __grid_c
         pre[r][j] = run;
       }
       lex[r] = run;
+    }
+    };
+    if (!FM2 && nblk == TB && nel == TB * L) {
+      unpack(std::true_type{});
+    } else {
+      unpack(std::false_type{});
     }
     if constexpr (FM2) {
       // every block restarts from its seed: a scan over the block's LPB lanes,
@@ -1579,8 +1646,15 @@ static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
   const uint32_t cap = (uint32_t)c;
   const uint32_t grid = a.ntiles < cap ? a.ntiles : cap;
   if (grid == 0) return cudaSuccess;
-  k<<<grid, kDecPipeThreads, smem, st>>>(a, slot);
-  return cudaGetLastError();
+  if (BATCH) {
+    k<<<grid, kDecPipeThreads, smem, st>>>(a, slot);
+    return cudaGetLastError();
+  }
+  // a single field's tiles are scheduled statically: its CTAs must all be resident
+  DecArgs args = a;
+  uint32_t slot_arg = slot;
+  void* params[] = {&args, &slot_arg};
+  return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(kDecPipeThreads), params, smem, st);
 }
 
 uint32_t decode_blocks_per_tile_f64(uint32_t L, uint32_t& bpw) {
