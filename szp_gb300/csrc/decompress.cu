@@ -254,7 +254,28 @@ __device__ __forceinline__ void rewalk_from(const SmemChain& ch, uint32_t* h, ui
   }
 }
 
-template <bool FM2, bool BATCH>
+// PACK: a super-chunk's look-back word carries its (entry, exit) pair too, so
+// one load reads a predecessor (blocks of at most 254 bytes, super-chunks
+// below 2^17 - 2 bytes).  An aggregate's 42-bit value holds the header count
+// (17 bits), the entry relative to the super-chunk's start (17 bits) and the
+// exit relative to its end (8 bits); an inclusive value holds the count
+// prefix and the exit.  Otherwise the pair sits in a second word, read between
+// two reads of the status word.
+constexpr uint32_t kRelDead = 0x1FFFFu, kRelEnd = 0x1FFFEu, kXDead = 0xFFu, kXEnd = 0xFEu;
+
+__device__ __forceinline__ uint64_t loc_word(uint64_t cnt, uint32_t h0, uint32_t xl, uint32_t scS, uint32_t scE,
+                                             bool incl) {
+  const uint64_t xr = xl == kPosDead ? kXDead : xl == kPosEnd ? kXEnd : (uint64_t)(xl - scE);
+  if (incl) return (cnt << 8) | xr;
+  const uint64_t hr = h0 == kPosDead ? kRelDead : h0 == kPosEnd ? kRelEnd : (uint64_t)(h0 - scS);
+  return (cnt << 25) | (hr << 8) | xr;
+}
+
+bool locate_packs(uint32_t super_chunk, uint32_t maxsz) {
+  return maxsz <= 254 && (uint64_t)super_chunk + maxsz < kRelEnd;
+}
+
+template <bool FM2, bool BATCH, bool PACK>
 __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_constant__ DecArgs a) {
   constexpr int NT = kLocThreads;
   extern __shared__ __align__(16) uint8_t s_bytes[];
@@ -397,15 +418,23 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
   uint64_t prefix = 0;
   if (j == 0) {
     if (tid == 0) {
-      a.aux[tile] = make_uint2(h0, xl);
-      __threadfence();
-      st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, K));
+      if (PACK) {
+        st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, loc_word(K, h0, xl, scS, scE, true)));
+      } else {
+        a.aux[tile] = make_uint2(h0, xl);
+        __threadfence();
+        st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, K));
+      }
     }
   } else {
     if (tid == 0) {
-      a.aux[tile] = make_uint2(h0, xl);
-      __threadfence();
-      st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, K));
+      if (PACK) {
+        st_relaxed_u64(a.status + tile, make_status(epoch, kFlagAggregate, loc_word(K, h0, xl, scS, scE, false)));
+      } else {
+        a.aux[tile] = make_uint2(h0, xl);
+        __threadfence();
+        st_release_u64(a.status + tile, make_status(epoch, kFlagAggregate, K));
+      }
     }
     if (warp == 0) {
       // lane l reads tile base - l (seqlock read of status + aux); a window
@@ -424,18 +453,37 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
         while (true) {
           const int64_t idx = base - lane;
           const bool inr = idx >= (int64_t)first;
-          uint64_t s1 = 0;
+          uint64_t s1 = 0, cnt = 0;
           uint2 ax = make_uint2(0, 0);
           bool ready = true, incl = false;
           if (inr) {
-            // acquire loads keep the aux read between the two status reads
-            s1 = ld_acquire_u64(a.status + idx);
-            const uint64_t axw = ld_acquire_u64(reinterpret_cast<const uint64_t*>(a.aux + idx));
-            ax = make_uint2((uint32_t)axw, (uint32_t)(axw >> 32));
-            const uint64_t s2 = ld_volatile_u64(a.status + idx);
-            const uint64_t f = status_flag(s1);
-            ready = s1 == s2 && status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
-            incl = ready && f == kFlagInclusive;
+            if (PACK) {
+              s1 = ld_volatile_u64(a.status + idx);
+              const uint64_t f = status_flag(s1);
+              ready = status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
+              incl = ready && f == kFlagInclusive;
+              const uint64_t v = status_value(s1);
+              const uint32_t sS = (uint32_t)(idx - (int64_t)first) * SC, sE = min(sS + SC, rlen);
+              const uint32_t xr = (uint32_t)v & 0xFFu;
+              ax.y = xr == kXDead ? kPosDead : xr == kXEnd ? kPosEnd : sE + xr;
+              if (incl) {
+                cnt = v >> 8;
+              } else {
+                const uint32_t hr = (uint32_t)(v >> 8) & 0x1FFFFu;
+                ax.x = hr == kRelDead ? kPosDead : hr == kRelEnd ? kPosEnd : sS + hr;
+                cnt = v >> 25;
+              }
+            } else {
+              // acquire loads keep the aux read between the two status reads
+              s1 = ld_acquire_u64(a.status + idx);
+              const uint64_t axw = ld_acquire_u64(reinterpret_cast<const uint64_t*>(a.aux + idx));
+              ax = make_uint2((uint32_t)axw, (uint32_t)(axw >> 32));
+              const uint64_t s2 = ld_volatile_u64(a.status + idx);
+              const uint64_t f = status_flag(s1);
+              ready = s1 == s2 && status_epoch(s1) == (epoch & 0xFFFFF) && (f == kFlagAggregate || f == kFlagInclusive);
+              incl = ready && f == kFlagInclusive;
+              cnt = status_value(s1);
+            }
           }
           const uint32_t bi = __ballot_sync(0xffffffffu, incl);
           const int jstar = bi ? __ffs(bi) - 1 : 32;  // nearest inclusive of the window
@@ -465,7 +513,7 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
             verdict = 2;
             break;
           }
-          uint64_t v = relevant ? status_value(s1) : 0;
+          uint64_t v = relevant ? cnt : 0;
           for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
           acc += v;
           const uint32_t far_h = __shfl_sync(0xffffffffu, ax.x, 31);
@@ -497,8 +545,12 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
     if (verdict == 3) {
       // our speculative entry was wrong: re-walk from the verified exit
       if (tid == 0) {
-        st_release_u64(a.status + tile, make_status(epoch, kFlagRepair, 0));
-        __threadfence();
+        if (PACK) {
+          st_relaxed_u64(a.status + tile, make_status(epoch, kFlagRepair, 0));
+        } else {
+          st_release_u64(a.status + tile, make_status(epoch, kFlagRepair, 0));
+          __threadfence();
+        }
         s_h[0] = pred_x == kPosDead ? kPosEnd : kPosDead;  // differs from the entry: chunk 0 is re-walked
         rewalk_from(ch, s_h, s_x, s_k, 0, pred_x, nactive, scS, scE, C);
         atomicAdd(&a.counters[0], 1u);
@@ -508,13 +560,19 @@ __global__ void __launch_bounds__(kLocThreads) locate_kernel(const __grid_consta
       for (int i = 0; i < NT; i++) K += s_k[i];
       h0 = s_h[0];
       xl = s_x[nactive - 1];
-      if (tid == 0) {
+      if (tid == 0 && !PACK) {
         a.aux[tile] = make_uint2(h0, xl);
         __threadfence();
       }
     }
     prefix = acc;
-    if (tid == 0) st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, prefix + K));
+    if (tid == 0) {
+      if (PACK) {
+        st_relaxed_u64(a.status + tile, make_status(epoch, kFlagInclusive, loc_word(prefix + K, h0, xl, scS, scE, true)));
+      } else {
+        st_release_u64(a.status + tile, make_status(epoch, kFlagInclusive, prefix + K));
+      }
+    }
   }
   // ---- header offsets of every block of every chunk ----
   uint32_t kx = s_k[tid];
@@ -1597,7 +1655,7 @@ cudaError_t launch_dec_setup_batch(const DecArgs& a, uint32_t nfields, cudaStrea
 template <bool FM2, bool BATCH>
 static cudaError_t launch_locate_t(const DecArgs& a, cudaStream_t st) {
   const size_t smem = locate_smem_bytes(a.super_chunk, a.overlap, a.maxsz);
-  auto k = locate_kernel<FM2, BATCH>;
+  auto k = locate_packs(a.super_chunk, a.maxsz) ? locate_kernel<FM2, BATCH, true> : locate_kernel<FM2, BATCH, false>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<a.nlocate_ctas, kLocThreads, smem, st>>>(a);
@@ -1763,7 +1821,9 @@ cudaError_t prepare_decompress_batch() {
   a.super_chunk = locate_super_bytes(a.maxsz);
   a.overlap = locate_overlap_bytes(a.maxsz);
   const size_t smem = locate_smem_bytes(a.super_chunk, a.overlap, a.maxsz);
-  cudaError_t e = cudaFuncSetAttribute(locate_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(locate_kernel<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(locate_kernel<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   for (int r : {1, 2, 4}) {
     if (e != cudaSuccess) return e;
     a.tb = 8u * (uint32_t)r * 8u;
