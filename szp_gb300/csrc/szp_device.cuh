@@ -151,26 +151,24 @@ __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
 // on a CTA that is not resident).  The CTA that draws the last ticket resets
 // the counter and bumps the epoch, so no memset is needed between launches
 // and a captured graph can be replayed.
-struct LaunchState {
-  uint32_t ticket;
+struct alignas(8) LaunchState {
+  uint32_t ticket;  // low word of the pair
   uint32_t epoch;
 };
 
-// Draw a tile ticket; returns (tile, epoch) broadcast to the CTA.
+// Draw a tile ticket; returns (tile, epoch) broadcast to the CTA.  One 64-bit
+// atomic on (epoch, ticket) returns the ticket with the epoch it belongs to;
+// the launch's last draw adds 2^32 - ntiles, which takes the ticket back to 0
+// and carries into the epoch.
 __device__ __forceinline__ void draw_ticket(LaunchState* ls, uint32_t ntiles, uint32_t& tile, uint32_t& epoch,
                                             uint32_t* smem2) {
   if (threadIdx.x == 0) {
-    uint32_t e = *(volatile uint32_t*)&ls->epoch;
-    __threadfence();
-    uint32_t t = atomicAdd(&ls->ticket, 1u);
-    if (t == ntiles - 1) {
-      // every CTA of this launch has read the epoch before drawing its ticket
-      ls->ticket = 0;
-      __threadfence();
-      atomicAdd(&ls->epoch, 1u);
-    }
+    unsigned long long* w = reinterpret_cast<unsigned long long*>(ls);
+    const unsigned long long old = atomicAdd(w, 1ull);
+    const uint32_t t = (uint32_t)old;
+    if (t == ntiles - 1) atomicAdd(w, (1ull << 32) - ntiles);
     smem2[0] = t;
-    smem2[1] = e;
+    smem2[1] = (uint32_t)(old >> 32);
   }
   __syncthreads();
   tile = smem2[0];
