@@ -388,6 +388,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     r.partial = w.rel_partial.as<float>();
     r.counter = &dm->rel_counter;
     r.eb_out = &dm->eb;
+    r.err = &dm->err;
     uint64_t want = (j.n / 4 + 255) / 256;
     uint32_t grid = (uint32_t)(want < 1 ? 1 : want);
     uint32_t lim = (uint32_t)(w.sm_count * 4 < kRelMaxGrid ? w.sm_count * 4 : kRelMaxGrid);

@@ -986,44 +986,12 @@ __global__ void __launch_bounds__(WARPS * 32) compress_generic(CompressArgs a) {
 // serial loop: NaNs are skipped unless x[0] is NaN (then range is NaN);
 // when max == min the same element is both, so range = x - x.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
+// The end of both float range passes: the CTA's min/max go to its partial;
+// the last CTA to finish reduces the partials and writes eb.
+__device__ __forceinline__ void rel_finish(const RelArgs& a, float mn, float mx) {
   __shared__ float s_mn[8], s_mx[8];
   __shared__ bool s_last;
-  float mn = INFINITY, mx = -INFINITY;
   const uint64_t n = a.n;
-  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  // scalar head up to 16-byte alignment, vector body, scalar tail
-  uint64_t mis = ((uintptr_t)a.x & 15) >> 2;
-  uint64_t headn = mis ? (4 - mis) : 0;
-  if (headn > n) headn = n;
-  for (uint64_t i = tid; i < headn; i += stride) {
-    float v = a.x[i];
-    mn = fminf(mn, v);
-    mx = fmaxf(mx, v);
-  }
-  const float4* x4 = reinterpret_cast<const float4*>(a.x + headn);
-  const uint64_t n4 = (n - headn) >> 2;
-  uint64_t i = tid;
-  // four independent 16-byte loads in flight per thread
-  for (; i + 3 * stride < n4; i += 4 * stride) {
-    const float4 v0 = __ldg(x4 + i), v1 = __ldg(x4 + i + stride);
-    const float4 v2 = __ldg(x4 + i + 2 * stride), v3 = __ldg(x4 + i + 3 * stride);
-    mn = fminf(mn, fminf(fminf(fminf(v0.x, v0.y), fminf(v0.z, v0.w)), fminf(fminf(v1.x, v1.y), fminf(v1.z, v1.w))));
-    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v0.x, v0.y), fmaxf(v0.z, v0.w)), fmaxf(fmaxf(v1.x, v1.y), fmaxf(v1.z, v1.w))));
-    mn = fminf(mn, fminf(fminf(fminf(v2.x, v2.y), fminf(v2.z, v2.w)), fminf(fminf(v3.x, v3.y), fminf(v3.z, v3.w))));
-    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v2.x, v2.y), fmaxf(v2.z, v2.w)), fmaxf(fmaxf(v3.x, v3.y), fmaxf(v3.z, v3.w))));
-  }
-  for (; i < n4; i += stride) {
-    float4 v = __ldg(x4 + i);
-    mn = fminf(fminf(mn, v.x), fminf(v.y, fminf(v.z, v.w)));
-    mx = fmaxf(fmaxf(mx, v.x), fmaxf(v.y, fmaxf(v.z, v.w)));
-  }
-  for (uint64_t i = headn + n4 * 4 + tid; i < n; i += stride) {
-    float v = a.x[i];
-    mn = fminf(mn, v);
-    mx = fmaxf(mx, v);
-  }
   for (int o = 16; o > 0; o >>= 1) {
     mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -1082,6 +1050,115 @@ __global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
     range = x86_nan_fix(__fsub_rn(mx, mn), mx, mn);
   }
   *a.eb_out = x86_nan_fix(__fmul_rn(range, a.rel), range, a.rel);
+}
+
+__global__ void __launch_bounds__(256) rel_bound_kernel(RelArgs a) {
+  float mn = INFINITY, mx = -INFINITY;
+  const uint64_t n = a.n;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // scalar head up to 16-byte alignment, vector body, scalar tail
+  uint64_t mis = ((uintptr_t)a.x & 15) >> 2;
+  uint64_t headn = mis ? (4 - mis) : 0;
+  if (headn > n) headn = n;
+  for (uint64_t i = tid; i < headn; i += stride) {
+    float v = a.x[i];
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  const float4* x4 = reinterpret_cast<const float4*>(a.x + headn);
+  const uint64_t n4 = (n - headn) >> 2;
+  uint64_t i = tid;
+  // four independent 16-byte loads in flight per thread
+  for (; i + 3 * stride < n4; i += 4 * stride) {
+    const float4 v0 = __ldg(x4 + i), v1 = __ldg(x4 + i + stride);
+    const float4 v2 = __ldg(x4 + i + 2 * stride), v3 = __ldg(x4 + i + 3 * stride);
+    mn = fminf(mn, fminf(fminf(fminf(v0.x, v0.y), fminf(v0.z, v0.w)), fminf(fminf(v1.x, v1.y), fminf(v1.z, v1.w))));
+    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v0.x, v0.y), fmaxf(v0.z, v0.w)), fmaxf(fmaxf(v1.x, v1.y), fmaxf(v1.z, v1.w))));
+    mn = fminf(mn, fminf(fminf(fminf(v2.x, v2.y), fminf(v2.z, v2.w)), fminf(fminf(v3.x, v3.y), fminf(v3.z, v3.w))));
+    mx = fmaxf(mx, fmaxf(fmaxf(fmaxf(v2.x, v2.y), fmaxf(v2.z, v2.w)), fmaxf(fmaxf(v3.x, v3.y), fmaxf(v3.z, v3.w))));
+  }
+  for (; i < n4; i += stride) {
+    float4 v = __ldg(x4 + i);
+    mn = fminf(fminf(mn, v.x), fminf(v.y, fminf(v.z, v.w)));
+    mx = fmaxf(fmaxf(mx, v.x), fmaxf(v.y, fmaxf(v.z, v.w)));
+  }
+  for (uint64_t i = headn + n4 * 4 + tid; i < n; i += stride) {
+    float v = a.x[i];
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  rel_finish(a, mn, mx);
+}
+
+// The range pass over large inputs: persistent CTAs stream 16 KB chunks of
+// the 16-byte-aligned body through a 3-stage shared-memory ring by bulk copy
+// (CTA c takes chunks c, c + grid, ...); CTA 0 also takes the scalar head and
+// tail.  The same fminf/fmaxf reduction as rel_bound_kernel.
+constexpr int kRelStages = 3;
+constexpr uint32_t kRelChunk = 4096;  // floats per bulk copy
+
+__global__ void __launch_bounds__(256) rel_bound_bulk(RelArgs a, uint64_t body0, uint64_t nbody) {
+  extern __shared__ __align__(16) float s_stage[];  // kRelStages * kRelChunk floats
+  __shared__ __align__(8) uint64_t s_full[kRelStages];
+  float mn = INFINITY, mx = -INFINITY;
+  const uint64_t n = a.n;
+  if (blockIdx.x == 0) {
+    for (uint64_t i = threadIdx.x; i < body0; i += blockDim.x) {
+      const float v = a.x[i];
+      mn = fminf(mn, v);
+      mx = fmaxf(mx, v);
+    }
+    for (uint64_t i = body0 + nbody + threadIdx.x; i < n; i += blockDim.x) {
+      const float v = a.x[i];
+      mn = fminf(mn, v);
+      mx = fmaxf(mx, v);
+    }
+  }
+  const float* body = a.x + body0;  // 16-byte aligned; nbody is a multiple of 4
+  const uint64_t nch = (nbody + kRelChunk - 1) / kRelChunk;
+  if (threadIdx.x == 0)
+    for (int s = 0; s < kRelStages; s++) mbar_init(&s_full[s], 1);
+  __syncthreads();
+  auto issue = [&](uint64_t c, int s) {
+    const uint32_t cnt = (uint32_t)min((uint64_t)kRelChunk, nbody - c * kRelChunk);
+    mbar_arrive_expect_tx(&s_full[s], 4 * cnt);
+    bulk_load(s_stage + (size_t)s * kRelChunk, body + c * kRelChunk, 4 * cnt, &s_full[s]);
+  };
+  if (threadIdx.x == 0)
+    for (int s = 0; s < kRelStages; s++) {
+      const uint64_t c = blockIdx.x + (uint64_t)s * gridDim.x;
+      if (c < nch) issue(c, s);
+    }
+  bool gave_up = false;
+  for (uint32_t k = 0;; k++) {
+    const uint64_t c = blockIdx.x + (uint64_t)k * gridDim.x;
+    if (c >= nch) break;
+    const int s = (int)(k % kRelStages);
+    const uint32_t par = (k / kRelStages) & 1;
+    if (!mbar_wait_ns(&s_full[s], par, kWaitNs)) {
+      gave_up = true;
+      mbar_wait_ns(&s_full[s], par, kWaitNs);  // the copy lands before its stage is reused
+    }
+    const uint32_t cnt = (uint32_t)min((uint64_t)kRelChunk, nbody - c * kRelChunk);
+    const float4* s4 = reinterpret_cast<const float4*>(s_stage + (size_t)s * kRelChunk);
+#pragma unroll
+    for (int u = 0; u < (int)(kRelChunk / 1024); u++) {
+      const uint32_t q = threadIdx.x + 256u * u;
+      if (4 * q < cnt) {
+        const float4 v = s4[q];
+        mn = fminf(mn, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
+        mx = fmaxf(mx, fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w)));
+      }
+    }
+    __syncthreads();  // every thread has read stage s
+    if (threadIdx.x == 0) {
+      const uint64_t cn = c + (uint64_t)kRelStages * gridDim.x;
+      if (cn < nch) issue(cn, s);
+    }
+  }
+  if (gave_up && threadIdx.x == 0 && a.err) atomicOr(a.err, kErrLookbackTimeout);
+  rel_finish(a, mn, mx);
 }
 
 // Order-preserving key of a double's bits (larger value, larger key); NaNs
@@ -1552,7 +1629,35 @@ cudaError_t launch_compress_f64(const CompressArgs& a, bool fm2, cudaStream_t st
   return cudaGetLastError();
 }
 
+// Inputs of at least 64 chunks take the bulk-copy pass, on at most 4 CTAs
+// per SM (the partials hold `grid` CTAs).
 cudaError_t launch_rel_bound(const RelArgs& a, uint32_t grid, cudaStream_t st) {
+  const uintptr_t xa = (uintptr_t)a.x;
+  const uint64_t mis = (xa & 15) >> 2;
+  const uint64_t body0 = min((uint64_t)(mis ? 4 - mis : 0), a.n);
+  const uint64_t nbody = (a.n - body0) & ~3ull;
+  if ((xa & 3) == 0 && nbody >= 64ull * kRelChunk) {
+    static std::atomic<uint64_t> s_sms{0};  // (device + 1) << 32 | SM count
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    uint64_t c = s_sms.load(std::memory_order_relaxed);
+    if ((c >> 32) != (uint64_t)dev + 1) {
+      int sms = 0;
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(rel_bound_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(kRelStages * kRelChunk * sizeof(float)));
+      if (e != cudaSuccess) return e;
+      c = ((uint64_t)dev + 1) << 32 | (uint32_t)sms;
+      s_sms.store(c, std::memory_order_relaxed);
+    }
+    const uint64_t nch = (nbody + kRelChunk - 1) / kRelChunk;
+    uint32_t g = grid < 4 * (uint32_t)c ? grid : 4 * (uint32_t)c;
+    if (g > nch) g = (uint32_t)nch;
+    rel_bound_bulk<<<g, 256, kRelStages * kRelChunk * sizeof(float), st>>>(a, body0, nbody);
+    return cudaGetLastError();
+  }
   rel_bound_kernel<<<grid, 256, 0, st>>>(a);
   return cudaGetLastError();
 }

@@ -122,12 +122,14 @@ extern "C" int szp_gb300_compress_dev_noalloc(const float* d_data, size_t nbEle,
   int launches = 1;
   if (errBoundMode == REL) {
     RelArgs r;
+    memset(&r, 0, sizeof r);
     r.x = d_data;
     r.n = nbEle;
     r.rel = (float)relBoundRatio;
     r.partial = sc->rel_partial;
     r.counter = &sc->rel_counter;
     r.eb_out = &sc->eb;
+    r.err = &sc->err;
     uint64_t want = (nbEle / 4 + 255) / 256;
     uint32_t grid = (uint32_t)(want < 1 ? 1 : (want > kNoAllocRelGrid ? kNoAllocRelGrid : want));
     e = launch_rel_bound(r, grid, st);

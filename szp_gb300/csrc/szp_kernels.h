@@ -90,6 +90,7 @@ struct RelArgs {
   double rel_d;
   double* ebd_out;
   double* invd_out;  // 1/eb, rounded as binary64
+  uint32_t* err;     // optional: a bulk copy that never landed sets kErrLookbackTimeout
 };
 
 // Decompression plan, filled on the device from the stream header.
