@@ -119,6 +119,42 @@ def test_rel_parity_vs_oracle(szp, port):
         assert s == s_or, (it, n, T, rel)
 
 
+def test_rel_range_pass_offsets(szp, port, torch):
+    """The range pass over inputs of 256 Ki values and more streams the
+    16-byte-aligned body by bulk copy and reads the elements before and after
+    it one by one: inputs starting 0-3 floats past a 16-byte boundary, lengths
+    of every residue mod 4, the extremes placed in the head and the tail, and
+    NaNs (skipped, or the range itself when x[0] is NaN)."""
+    rng = np.random.default_rng(86)
+    from szp_gb300.workloads import walk
+    N = 1_200_011
+    base = walk(N, rng)
+    dbase = torch.from_numpy(base).cuda()
+    st = torch.cuda.current_stream().cuda_stream
+    T = 11
+    for off in range(4):
+        for k, case in enumerate(["extremes", "nan_inside", "nan_first"]):
+            n = N - off - 4 - k
+            x = base[off:off + n].copy()
+            if case == "extremes":
+                x[1] = np.float32(x.max() + 7.0)    # in the scalar head when the start is unaligned
+                x[n - 1] = np.float32(x.min() - 5.0)  # in the scalar tail when n - head is not a multiple of 4
+            elif case == "nan_inside":
+                x[n // 2] = np.nan
+            else:
+                x[0] = np.nan
+            dbase[off:off + n].copy_(torch.from_numpy(x))
+            rel = 1e-3
+            cap = szp.max_stream_bytes(n, 32, T, 1)
+            dout = torch.empty(cap, dtype=torch.uint8, device="cuda")
+            ptr = dbase.data_ptr() + 4 * off
+            size = szp.compress_dev(ptr, n, dout.data_ptr(), cap, szp.REL, 0.0, rel, 32, T, 1, st)
+            s = dout[:size].cpu().numpy().tobytes()
+            eb = port.rel_bound(x, rel)
+            assert s == port.compress(x, eb, 32, T, 1), (off, case)
+            dbase[off:off + n].copy_(torch.from_numpy(base[off:off + n]))
+
+
 def test_device_api(szp, port, torch):
     rng = np.random.default_rng(79)
     from szp_gb300.workloads import walk
