@@ -307,6 +307,12 @@ double szp_gb300_kernel_time(int slot, int *launches);
  * often and exercise the repair paths; streams decode the same. */
 void szp_gb300_set_locate_overlap(int bytes);
 
+/* Nonzero: a single field's decode pipeline draws tile tickets instead of its
+ * cooperative launch with a static tile order (the path it takes when a
+ * cooperative launch is refused, e.g. on a partitioned GPU); streams decode
+ * the same.  0 restores the default. */
+void szp_gb300_set_decode_tickets(int on);
+
 /* Chunks whose speculative header walk the last decompression of this
  * thread had to repair in order (statistics; -1 on error). */
 int szp_gb300_last_repairs(void);

@@ -91,6 +91,7 @@ _sig("szp_gb300_bitcount_thresholds", None, [_vp])
 _sig("szp_gb300_bitcount_probe", ctypes.c_int, [_vp, _vp, _sz, _vp])
 _sig("szp_gb300_set_timing", None, [ctypes.c_int])
 _sig("szp_gb300_set_locate_overlap", None, [ctypes.c_int])
+_sig("szp_gb300_set_decode_tickets", None, [ctypes.c_int])
 _sig("szp_gb300_kernel_ms", ctypes.c_double, [ctypes.c_int])
 _sig("szp_gb300_kernel_time", ctypes.c_double, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)])
 _sig("szp_gb300_kernel_launches", ctypes.c_ulonglong, [])
@@ -468,6 +469,12 @@ def bitcount_thresholds():
 def set_locate_overlap(nbytes):
     """Bytes walked before a decompression chunk (-1 = default); for tests."""
     _lib.szp_gb300_set_locate_overlap(int(nbytes))
+
+
+def set_decode_tickets(on):
+    """Single-field decode with tile tickets instead of the cooperative static
+    schedule (the fallback path); for tests."""
+    _lib.szp_gb300_set_decode_tickets(1 if on else 0)
 
 
 def set_timing(on):

@@ -91,6 +91,7 @@ std::mutex g_mu;
 int g_segments = 0;
 int g_timing = 0;
 int g_overlap = -1;  // locate overlap override (tests of the repair paths)
+int g_decode_tickets = 0;  // single-field decode draws tickets (tests of that path)
 unsigned long long g_launches = 0;
 
 int resolve_segments(int requested) {
@@ -532,6 +533,7 @@ int decompress_launch(Workspace& w, const DecompressJob& j, cudaStream_t st) {
   a.tb = tb;
   a.bpw = bpw;
   a.nlocate_ctas = (uint32_t)nlocate;
+  a.static_tiles = g_decode_tickets ? 0u : 1u;
   if (((!dbl || qpipe) && decode_smem_bytes((uint32_t)j.L, tb, fm2) > 200 * 1024) ||
       locate_smem_bytes(SC, a.overlap, maxsz) > 200 * 1024)
     return fail(SZP_GB300_EINVAL, "blockSize too large");
@@ -1364,6 +1366,7 @@ int szp_gb300_wait_probe(unsigned long long limit_ns, unsigned long long* waited
 void szp_gb300_set_timing(int enable) { g_timing = enable ? 1 : 0; }
 
 void szp_gb300_set_locate_overlap(int bytes) { g_overlap = bytes; }
+void szp_gb300_set_decode_tickets(int on) { g_decode_tickets = on ? 1 : 0; }
 
 double szp_gb300_kernel_ms(int slot) {
   Workspace* w;

@@ -758,12 +758,13 @@ struct DecSlot {
 // Bytes of the block-offset area at the front of a slot.
 __host__ __device__ constexpr uint32_t dec_pos_bytes(uint32_t tb) { return 4 * tb + 32; }
 
-// Tile order of a decode pipeline launch.  Batched launches draw tickets (a
-// tile's predecessors have then started before it); a single field's launch
-// is cooperative, so all its CTAs are resident and CTA c takes tiles c,
-// c + grid, c + 2 grid, ...: the producer may run ahead as far as its slots
-// allow, and a tile's predecessors are the tiles the other CTAs hold at the
-// same time.
+// Tile order of a decode pipeline launch.  A single field's launch is
+// cooperative (a.static_tiles), so all its CTAs are resident and CTA c takes
+// tiles c, c + grid, c + 2 grid, ...: the producer may run ahead as far as
+// its slots allow, and a tile's predecessors are the tiles the other CTAs hold
+// at the same time.  Batched launches, and a single field whose cooperative
+// launch was refused, draw tickets (a tile's predecessors have then started
+// before it).
 template <uint32_t L, uint32_t TB, int NS, bool BATCH, bool FM2>
 __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, uint32_t slot_bytes, DecSlot* meta,
                                              uint64_t* full, uint64_t* empty, uint32_t* s_epoch,
@@ -786,7 +787,7 @@ __device__ __forceinline__ void dec_producer(const DecArgs& a, uint8_t* slots, u
     const int s = (int)(k % NS);
     if (k >= (uint32_t)NS) mbar_wait_or_flag(&empty[s], ((k / NS) - 1) & 1, a.err);
     uint32_t tile;
-    if (BATCH) {
+    if (BATCH || !a.static_tiles) {
       // draw the ticket only once the compute warps have started the previous
       // position: a tile's predecessors are then never more than a tile behind it
       // in their work, which keeps the look-back short
@@ -1704,15 +1705,20 @@ static cudaError_t launch_dec_lanes(const DecArgs& a, cudaStream_t st) {
   const uint32_t cap = (uint32_t)c;
   const uint32_t grid = a.ntiles < cap ? a.ntiles : cap;
   if (grid == 0) return cudaSuccess;
-  if (BATCH) {
-    k<<<grid, kDecPipeThreads, smem, st>>>(a, slot);
-    return cudaGetLastError();
+  if (!BATCH && a.static_tiles) {
+    // a single field's tiles are scheduled statically: its CTAs must all be
+    // resident, which a cooperative launch guarantees or refuses
+    DecArgs args = a;
+    uint32_t slot_arg = slot;
+    void* params[] = {&args, &slot_arg};
+    e = cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(kDecPipeThreads), params, smem, st);
+    if (e != cudaErrorCooperativeLaunchTooLarge && e != cudaErrorNotSupported) return e;
+    (void)cudaGetLastError();  // refused (a partitioned GPU): draw tickets instead
   }
-  // a single field's tiles are scheduled statically: its CTAs must all be resident
   DecArgs args = a;
-  uint32_t slot_arg = slot;
-  void* params[] = {&args, &slot_arg};
-  return cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(kDecPipeThreads), params, smem, st);
+  args.static_tiles = 0;
+  k<<<grid, kDecPipeThreads, smem, st>>>(args, slot);
+  return cudaGetLastError();
 }
 
 uint32_t decode_blocks_per_tile_f64(uint32_t L, uint32_t& bpw) {

@@ -142,6 +142,7 @@ struct DecArgs {
   uint32_t tb;
   uint32_t bpw;
   uint32_t nlocate_ctas; // locate tickets of the launch (upper bound)
+  uint32_t static_tiles; // decode pipeline: CTA c takes tiles c, c + grid, ... (a cooperative launch)
   // batched launches
   const DecField* fields;
   const uint32_t* tile_field;  // decode tile -> field

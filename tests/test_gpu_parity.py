@@ -307,3 +307,25 @@ def test_locate_repair_path(szp, port, overlap):
             assert np.array_equal(bits(y), bits(port.decompress(s, n, L, T, 1))), (overlap, T, n, L)
     finally:
         szp.set_locate_overlap(-1)
+
+
+def test_decode_ticket_schedule(szp, port):
+    """A single field's decode runs cooperatively with a static tile order; when
+    a cooperative launch is refused it draws tile tickets instead.  Both
+    schedules must decode every stream the same, fastmode1 and fastmode2."""
+    from szp_gb300.workloads import walk
+    rng = np.random.default_rng(87)
+    cases = ((16, 3_000_001, 32, 1), (7, 1_000_000, 8, 1), (4, 2_000_003, 32, 2))
+    try:
+        for T, n, L, mode in cases:
+            x = walk(n, rng)
+            eb = float(np.float32(1e-4 * (x.max() - x.min())))
+            s = port.compress(x, eb, L, T, mode)
+            want = bits(port.decompress(s, n, L, T, mode))
+            szp.set_segments(T)
+            for tickets in (False, True):
+                szp.set_decode_tickets(tickets)
+                y = szp.szp_decompress(s, n, L, mode)
+                assert np.array_equal(bits(y), want), (T, n, L, mode, tickets)
+    finally:
+        szp.set_decode_tickets(False)
