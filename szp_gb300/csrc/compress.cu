@@ -5,8 +5,9 @@
 // compute warps quantize, analyse and pack each tile in shared memory, control
 // warps find the tile's stream offset by decoupled look-back and write it with
 // 16-byte stores).  Other blockSizes: compress_generic, one warp per block.
-// The REL range pass (rel_bound_kernel, rel_batch_kernel for batches) runs
-// first.  HBM traffic: 4n bytes read (twice with REL), stream bytes written.
+// The REL range pass (rel_bound_bulk over large inputs, rel_bound_kernel over
+// small ones, rel_batch_kernel for batches) runs first.  HBM traffic: 4n
+// bytes read (twice with REL), stream bytes written.
 //
 // Reference semantics followed (SZp/src/szp_float.cc):
 //   quantize  (int)(x * (double)(1.0f/eb))                    :185,209,228
