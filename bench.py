@@ -20,6 +20,8 @@ cpu_baseline  the oracle (C restatement of the reference, OpenMP on all host
 configs the other single-field configurations: the 2^24-value random walk
         (ABS 1e-4 of its range) and the 8192^2 Laplace field with 40% zero
         blocks (ABS 1e-5), GB/s and per-kernel roofline fractions.
+lorenzo the multidimensional Lorenzo variant of the same field at REL 1e-3
+        and 1e-4: its ratio beside fastmode1's, GB/s and per-pass times.
 
 --impl reference times the reference's CPU algorithm (the oracle port; the
 reference's sources are not present where the benchmark runs) on the same
@@ -59,6 +61,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-fm2", action="store_true")
+    ap.add_argument("--no-lorenzo", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-reduce", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
@@ -756,6 +759,45 @@ def main():
                "kernels_ms": {k: round(v, 4) for k, v in avg.items()}}
         del d_s2
 
+    # the multidimensional Lorenzo variant on the same field (its own stream):
+    # ratio against fastmode1's at the same bound, and the device time of its
+    # passes (the codes pass + fastmode1 over the codes; decode of the codes +
+    # the inverse sums)
+    lorenzo = None
+    if not args.no_lorenzo:
+        dims = (args.side, args.side, args.side)
+        capl = szp.lorenzo_max_stream_bytes(dims, T)
+        d_sl = torch.empty(capl, dtype=torch.uint8, device=dev)
+        lorenzo = {"dims": list(dims), "by_rel": {}}
+        for rel in (1e-3, 1e-4):
+            szp.set_timing(True)
+            for i in range(4):
+                szl = szp.lorenzo_compress_dev(x.data_ptr(), dims, d_sl.data_ptr(), capl, szp.REL, 0.0, rel, T, st)
+                szp.lorenzo_decompress_dev(d_sl.data_ptr(), szl, dims, d_y.data_ptr(), T, st)
+                if i == 0:
+                    torch.cuda.synchronize()
+                    for slot in range(7):
+                        szp.kernel_time(slot)  # drop the first round trip
+            torch.cuda.synchronize()
+            kt = {name: szp.kernel_time(slot) for slot, name in
+                  enumerate(["rel_range", "compress", "dec_setup", "locate", "decode", "codes", "inverse"])}
+            szp.set_timing(False)
+            avg = {k: v[0] / v[1] for k, v in kt.items() if v[1]}
+            ebl = rel * float(x.max() - x.min())
+            errl = float((x - d_y).abs().max())
+            # fastmode1's arithmetic: a float inverse of eb and a float product q * eb
+            assert errl <= ebl * (1 + 2.0 ** -22) + float(x.abs().max()) * 2.0 ** -22, \
+                "Lorenzo round trip exceeds the bound"
+            c_ms = avg["rel_range"] + avg["codes"] + avg["compress"]
+            d_ms = avg["dec_setup"] + avg["locate"] + avg["decode"] + avg["inverse"]
+            lorenzo["by_rel"][str(rel)] = {
+                "ratio": round(4.0 * n / szl, 3), "fastmode1_ratio": round(4.0 * n / sizes[rel], 3),
+                "compress_gbs": round(4.0 * n / (c_ms / 1e3) / 1e9, 2),
+                "decompress_gbs": round(4.0 * n / (d_ms / 1e3) / 1e9, 2),
+                "kernels_ms": {k: round(v, 4) for k, v in avg.items()},
+                "max_abs_err_over_eb": round(errl / ebl, 4)}
+        del d_sl
+
     # float64 data (szp_double_*): 2^26 doubles (512 MiB) of the field, REL 1e-6
     f64 = None
     if not args.no_f64:
@@ -871,6 +913,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "fastmode2": fm2,
+            "lorenzo": lorenzo,
             "float64": f64,
             "reduce": reduce,
             "configs": configs,

@@ -227,6 +227,25 @@ int szp_gb300_compress_dev_f64(int fastMode, const double *d_data, size_t nbEle,
 int szp_gb300_decompress_dev_f64(int fastMode, const unsigned char *d_bytes, size_t byteLength, size_t nbEle,
                                  int blockSize, int segments, double *d_out, void *stream);
 
+/* Multidimensional Lorenzo variant (no reference entry point: the reference
+ * predicts along the flattened array, SZp/example/test_multidim.cc).  A field
+ * of nx*ny*nz floats, x fastest, in device memory, with an ABS or REL bound:
+ * the stream is [nx][ny][nz] (u32 little-endian) followed by the fastmode1
+ * stream (blockSize 32, `segments` segments of the flattened array) of the
+ * codes q - q[j-1] - q[k-1] + q[j-1][k-1] (q: fastmode1's quantization codes,
+ * neighbours outside the field 0), whose delta along x is the 3-D Lorenzo
+ * residual.  Every value decompresses within eb, as fastmode1's do.  Waits;
+ * the stream size goes to *outSize.  A 2-D field is nz = 1, a 1-D one
+ * ny = nz = 1. */
+size_t szp_gb300_lorenzo_max_stream_bytes(size_t nx, size_t ny, size_t nz, int segments);
+int szp_gb300_lorenzo_compress_dev(const float *d_data, size_t nx, size_t ny, size_t nz, int errBoundMode,
+                                   double absErrBound, double relBoundRatio, int segments, unsigned char *d_out,
+                                   size_t out_capacity, size_t *outSize, void *stream);
+/* Decompresses a Lorenzo stream of byteLength bytes into d_out; the dims and
+ * segments must be those it was written with (other dims: SZP_GB300_EINVAL). */
+int szp_gb300_lorenzo_decompress_dev(const unsigned char *d_bytes, size_t byteLength, size_t nx, size_t ny,
+                                     size_t nz, int segments, float *d_out, void *stream);
+
 /* Homomorphic sum of two device streams (the hZCCL use of fZ-light streams;
  * no reference entry point): both compressed from nbEle values with the same
  * error bound (identical eb header bytes), blockSize (8..256), segments and
@@ -294,7 +313,8 @@ int szp_gb300_wait_probe(unsigned long long limit_ns, unsigned long long *waited
 
 /* Per-kernel timing with CUDA events on the launching stream.  When enabled,
  * szp_gb300_kernel_ms(slot) returns the duration of the last launch of:
- * 0 REL range, 1 compress, 2 decompress setup, 3 locate, 4 decode. */
+ * 0 REL range, 1 compress, 2 decompress setup, 3 locate, 4 decode, 5 the
+ * Lorenzo variant's codes pass, 6 its inverse sums (both of its passes). */
 void szp_gb300_set_timing(int enable);
 double szp_gb300_kernel_ms(int slot);
 

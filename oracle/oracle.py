@@ -74,6 +74,14 @@ class Port:
         lib.szo_reduce_sum.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
                                        ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_void_p, ctypes.c_size_t, _c_size_p]
+        lib.szo_lorenzo_max_stream_bytes.restype = ctypes.c_size_t
+        lib.szo_lorenzo_max_stream_bytes.argtypes = [ctypes.c_size_t] * 3 + [ctypes.c_int]
+        lib.szo_lorenzo_compress.restype = ctypes.c_int
+        lib.szo_lorenzo_compress.argtypes = [ctypes.c_void_p] + [ctypes.c_size_t] * 3 + [
+            ctypes.c_float, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, _c_size_p]
+        lib.szo_lorenzo_decompress.restype = ctypes.c_int
+        lib.szo_lorenzo_decompress.argtypes = [ctypes.c_void_p, ctypes.c_size_t] + [ctypes.c_size_t] * 3 + [
+            ctypes.c_int, ctypes.c_void_p]
         for name in ("szo_record_compress", "szo_record_decompress"):
             f = getattr(lib, name)
             f.restype = ctypes.c_uint64
@@ -91,6 +99,30 @@ class Port:
         (szpd_float.cc:216-318, szpd_double.cc:219-321)."""
         buf = np.frombuffer(stream, dtype=np.uint8)
         return int(self.lib.szo_record_decompress(buf.ctypes.data, buf.size, n, L, int(dbl)))
+
+    def lorenzo_compress(self, x, dims, eb, T=1):
+        """The multidimensional Lorenzo variant's stream of x (shape dims =
+        (nz, ny, nx), x fastest) at absolute bound eb, T segments."""
+        x = _f32(x)
+        nz, ny, nx = dims
+        assert x.size == nx * ny * nz
+        cap = self.lib.szo_lorenzo_max_stream_bytes(nx, ny, nz, T)
+        out = np.empty(cap, dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        rc = self.lib.szo_lorenzo_compress(x.ctypes.data, nx, ny, nz, ctypes.c_float(eb), T, out.ctypes.data, cap,
+                                           ctypes.byref(size))
+        if rc != 0:
+            raise RuntimeError("oracle lorenzo_compress failed: %d" % rc)
+        return out[: size.value].tobytes()
+
+    def lorenzo_decompress(self, stream, dims, T=1):
+        nz, ny, nx = dims
+        buf = np.frombuffer(stream, dtype=np.uint8)
+        y = np.empty(nx * ny * nz, dtype=np.float32)
+        rc = self.lib.szo_lorenzo_decompress(buf.ctypes.data, buf.size, nx, ny, nz, T, y.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("oracle lorenzo_decompress failed: %d" % rc)
+        return y
 
     def max_threads(self):
         return self.lib.szo_max_threads()

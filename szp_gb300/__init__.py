@@ -92,6 +92,11 @@ _sig("szp_gb300_bitcount_probe", ctypes.c_int, [_vp, _vp, _sz, _vp])
 _sig("szp_gb300_set_timing", None, [ctypes.c_int])
 _sig("szp_gb300_set_locate_overlap", None, [ctypes.c_int])
 _sig("szp_gb300_set_decode_tickets", None, [ctypes.c_int])
+_sig("szp_gb300_lorenzo_max_stream_bytes", _sz, [_sz, _sz, _sz, ctypes.c_int])
+_sig("szp_gb300_lorenzo_compress_dev", ctypes.c_int, [_vp, _sz, _sz, _sz, ctypes.c_int, ctypes.c_double,
+                                                      ctypes.c_double, ctypes.c_int, _vp, _sz,
+                                                      ctypes.POINTER(ctypes.c_size_t), _vp])
+_sig("szp_gb300_lorenzo_decompress_dev", ctypes.c_int, [_vp, _sz, _sz, _sz, _sz, ctypes.c_int, _vp, _vp])
 _sig("szp_gb300_kernel_ms", ctypes.c_double, [ctypes.c_int])
 _sig("szp_gb300_kernel_time", ctypes.c_double, [ctypes.c_int, ctypes.POINTER(ctypes.c_int)])
 _sig("szp_gb300_kernel_launches", ctypes.c_ulonglong, [])
@@ -469,6 +474,32 @@ def bitcount_thresholds():
 def set_locate_overlap(nbytes):
     """Bytes walked before a decompression chunk (-1 = default); for tests."""
     _lib.szp_gb300_set_locate_overlap(int(nbytes))
+
+
+def lorenzo_max_stream_bytes(dims, segments=0):
+    """Capacity that always fits the Lorenzo stream of a (nz, ny, nx) field."""
+    nz, ny, nx = dims
+    return _lib.szp_gb300_lorenzo_max_stream_bytes(nx, ny, nz, segments)
+
+
+def lorenzo_compress_dev(d_data, dims, d_out, capacity, err_bound_mode=ABS, abs_err_bound=0.0, rel_bound_ratio=0.0,
+                         segments=0, stream=0):
+    """Multidimensional Lorenzo compressor of a (nz, ny, nx) device field;
+    returns the stream size in bytes."""
+    nz, ny, nx = dims
+    size = ctypes.c_size_t(0)
+    rc = _lib.szp_gb300_lorenzo_compress_dev(d_data, nx, ny, nz, err_bound_mode, abs_err_bound, rel_bound_ratio,
+                                             segments, d_out, capacity, ctypes.byref(size), stream or None)
+    if rc != 0:
+        raise SzpError(rc, "lorenzo_compress_dev failed: %s" % last_error())
+    return size.value
+
+
+def lorenzo_decompress_dev(d_stream, length, dims, d_out, segments=0, stream=0):
+    nz, ny, nx = dims
+    rc = _lib.szp_gb300_lorenzo_decompress_dev(d_stream, length, nx, ny, nz, segments, d_out, stream or None)
+    if rc != 0:
+        raise SzpError(rc, "lorenzo_decompress_dev failed: %s" % last_error())
 
 
 def set_decode_tickets(on):

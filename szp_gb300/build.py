@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build", platform.machine())
 LIB = os.path.join(HERE, "libszp_gb300.so")
-SOURCES = ["api.cu", "compress.cu", "decompress.cu", "fm1_pipes.cu", "noalloc.cu", "batch.cu", "serve.cu"]
+SOURCES = ["api.cu", "compress.cu", "decompress.cu", "fm1_pipes.cu", "noalloc.cu", "batch.cu", "serve.cu", "lorenzo.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp,-O2",

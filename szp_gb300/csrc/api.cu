@@ -142,7 +142,7 @@ struct DevMisc {
 };
 constexpr int kRelMaxGrid = 1024;
 
-enum { kSlotRel = 0, kSlotCompress, kSlotSetup, kSlotLocate, kSlotDecode, kNumSlots };
+enum { kSlotRel = 0, kSlotCompress, kSlotSetup, kSlotLocate, kSlotDecode, kSlotLorenzo, kSlotLorenzoInv, kNumSlots };
 
 struct Workspace {
   int device = -1;
@@ -304,7 +304,31 @@ struct CompressJob {
   // int32 codes to pack as they are (the homomorphic reduction): ABS with
   // eb_abs (float stream) or eb_abs_d (dbl: float64 stream), no quantization
   const int32_t* d_codes = nullptr;
+  const float* d_eb = nullptr;  // codes: the float header's eb on the device instead of eb_abs
+  bool keep_err = false;        // the caller cleared the error word (earlier passes report into it)
 };
+
+// The REL range pass over float data: eb = range * (float)rel into dm->eb.
+static int launch_rel_float(Workspace& w, const float* d_x, size_t n, double rel, cudaStream_t st) {
+  DevMisc* dm = w.dm();
+  RelArgs r;
+  memset(&r, 0, sizeof r);
+  r.x = d_x;
+  r.n = n;
+  r.rel = (float)rel;
+  r.partial = w.rel_partial.as<float>();
+  r.counter = &dm->rel_counter;
+  r.eb_out = &dm->eb;
+  r.err = &dm->err;
+  uint64_t want = (n / 4 + 255) / 256;
+  uint32_t grid = (uint32_t)(want < 1 ? 1 : want);
+  uint32_t lim = (uint32_t)(w.sm_count * 4 < kRelMaxGrid ? w.sm_count * 4 : kRelMaxGrid);
+  if (grid > lim) grid = lim;
+  w.mark(kSlotRel, 0, st);
+  CU(launch_rel_bound(r, grid, st));
+  w.mark(kSlotRel, 1, st);
+  return SZP_GB300_OK;
+}
 
 int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   if (j.L <= 0) return fail(SZP_GB300_EINVAL, "blockSize must be positive (got %d)", j.L);
@@ -333,7 +357,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     return fail(SZP_GB300_EINVAL, "input too large for one launch");
   CU(w.status.ensure(ntiles * sizeof(uint64_t)));
   DevMisc* dm = w.dm();
-  CU(cudaMemsetAsync(&dm->err, 0, sizeof(uint32_t), st));
+  if (!j.keep_err) CU(cudaMemsetAsync(&dm->err, 0, sizeof(uint32_t), st));
 
   CompressArgs a;
   memset(&a, 0, sizeof a);
@@ -342,7 +366,7 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
   a.cap = j.cap;
   a.seg = sg;
   a.eb = j.eb_abs;
-  a.eb_dev = nullptr;
+  a.eb_dev = codes ? j.d_eb : nullptr;
   a.status = w.status.as<uint64_t>();
   a.ls = &dm->ls;
   a.err = &dm->err;
@@ -381,22 +405,8 @@ int compress_launch(Workspace& w, const CompressJob& j, cudaStream_t st) {
     a.invd_dev = &dm->invd;
     launches++;
   } else if (j.eb_mode == REL) {
-    RelArgs r;
-    memset(&r, 0, sizeof r);
-    r.x = j.d_x;
-    r.n = j.n;
-    r.rel = (float)j.rel;
-    r.partial = w.rel_partial.as<float>();
-    r.counter = &dm->rel_counter;
-    r.eb_out = &dm->eb;
-    r.err = &dm->err;
-    uint64_t want = (j.n / 4 + 255) / 256;
-    uint32_t grid = (uint32_t)(want < 1 ? 1 : want);
-    uint32_t lim = (uint32_t)(w.sm_count * 4 < kRelMaxGrid ? w.sm_count * 4 : kRelMaxGrid);
-    if (grid > lim) grid = lim;
-    w.mark(kSlotRel, 0, st);
-    CU(launch_rel_bound(r, grid, st));
-    w.mark(kSlotRel, 1, st);
+    const int rc = launch_rel_float(w, j.d_x, j.n, j.rel, st);
+    if (rc) return rc;
     a.eb_dev = &dm->eb;
     launches++;
   }
@@ -1287,6 +1297,138 @@ int szp_gb300_reduce_sum_dev(int fastMode, int dataType, const unsigned char* d_
       if (wrapped) t_notices = 1;
     }
   }
+  w->end(st);
+  return rc;
+}
+
+// The multidimensional Lorenzo variant (lorenzo.cu): the fastmode1 stream
+// (blockSize 32) of the codes r after a 12-byte [nx][ny][nz] header.
+static constexpr size_t kLorenzoHead = 12;
+
+static int lorenzo_dims(size_t nx, size_t ny, size_t nz, size_t* n) {
+  if (nx > 0xFFFFFFFFull || ny > 0xFFFFFFFFull || nz > 0xFFFFFFFFull)
+    return fail(SZP_GB300_EINVAL, "a dimension above 2^32 - 1");
+  if ((nx && ny > ~(size_t)0 / nx) || (nx * ny && nz > ~(size_t)0 / (nx * ny)))
+    return fail(SZP_GB300_EINVAL, "nx * ny * nz overflows");
+  *n = nx * ny * nz;
+  return SZP_GB300_OK;
+}
+
+size_t szp_gb300_lorenzo_max_stream_bytes(size_t nx, size_t ny, size_t nz, int segments) {
+  size_t n = 0;
+  if (lorenzo_dims(nx, ny, nz, &n)) return 0;
+  const size_t b = max_stream_bytes(n, 32, resolve_segments(segments), 1);
+  return b ? kLorenzoHead + b : 0;
+}
+
+int szp_gb300_lorenzo_compress_dev(const float* d_data, size_t nx, size_t ny, size_t nz, int errBoundMode,
+                                   double absErrBound, double relBoundRatio, int segments, unsigned char* d_out,
+                                   size_t out_capacity, size_t* outSize, void* stream) {
+  clear_error();
+  if (outSize) *outSize = 0;
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  size_t n = 0;
+  rc = lorenzo_dims(nx, ny, nz, &n);
+  if (rc) return rc;
+  if (!d_out) return fail(SZP_GB300_EINVAL, "null output");
+  if (n && !d_data) return fail(SZP_GB300_EINVAL, "null input");
+  if ((uintptr_t)d_data & 3) return fail(SZP_GB300_EINVAL, "input not aligned to its element size");
+  if (errBoundMode != ABS && errBoundMode != REL) return fail(SZP_GB300_EINVAL, "unknown errBoundMode %d", errBoundMode);
+  const int T = resolve_segments(segments);
+  if (out_capacity < kLorenzoHead + 4 + 8ull * T) return fail(SZP_GB300_ECAPACITY, "output buffer smaller than the stream header");
+  cudaStream_t st = w->begin(stream);
+  DevMisc* dm = w->dm();
+  rc = SZP_GB300_OK;
+  if (cudaMemsetAsync(&dm->err, 0, sizeof(uint32_t), st) != cudaSuccess) rc = fail(SZP_GB300_ECUDA, "memset failed");
+  if (rc == SZP_GB300_OK && errBoundMode == REL) rc = launch_rel_float(*w, d_data, n, relBoundRatio, st);
+  if (rc == SZP_GB300_OK && w->qbuf.ensure((n + 4) * sizeof(int32_t)) != cudaSuccess)
+    rc = fail(SZP_GB300_ENOMEM, "no device memory for the codes");
+  if (rc == SZP_GB300_OK) {
+    LorenzoArgs a;
+    memset(&a, 0, sizeof a);
+    a.x = d_data;
+    a.r = w->qbuf.as<int32_t>();
+    a.head = d_out;
+    a.nx = (uint32_t)nx;
+    a.ny = (uint32_t)ny;
+    a.nz = (uint32_t)nz;
+    a.eb = (float)absErrBound;
+    a.eb_dev = errBoundMode == REL ? &dm->eb : nullptr;
+    a.err = &dm->err;
+    w->mark(kSlotLorenzo, 0, st);
+    cudaError_t e = launch_lorenzo_codes(a, (uint32_t)w->sm_count, st);
+    w->mark(kSlotLorenzo, 1, st);
+    if (e != cudaSuccess) rc = fail(SZP_GB300_ECUDA, "Lorenzo codes pass: %s", cudaGetErrorString(e));
+    count_launches(1);
+  }
+  if (rc == SZP_GB300_OK) {
+    CompressJob c{nullptr, n, ABS, (float)absErrBound, 0.0, 32, T, 1, d_out + kLorenzoHead,
+                  out_capacity - kLorenzoHead, nullptr};
+    c.d_codes = w->qbuf.as<int32_t>();
+    c.d_eb = errBoundMode == REL ? &dm->eb : nullptr;
+    c.keep_err = true;
+    rc = compress_launch(*w, c, st);
+  }
+  if (rc == SZP_GB300_OK) {
+    size_t sz = 0;
+    rc = finish_sync(*w, st, &sz);
+    if (rc == SZP_GB300_OK && outSize) *outSize = sz + kLorenzoHead;
+  }
+  w->end(st);
+  return rc;
+}
+
+int szp_gb300_lorenzo_decompress_dev(const unsigned char* d_bytes, size_t byteLength, size_t nx, size_t ny, size_t nz,
+                                     int segments, float* d_out, void* stream) {
+  clear_error();
+  Workspace* w;
+  int rc = get_ws(&w);
+  if (rc) return rc;
+  size_t n = 0;
+  rc = lorenzo_dims(nx, ny, nz, &n);
+  if (rc) return rc;
+  if (!d_bytes) return fail(SZP_GB300_EINVAL, "null stream");
+  if (n && !d_out) return fail(SZP_GB300_EINVAL, "null output");
+  if (byteLength < kLorenzoHead + 4) return fail(SZP_GB300_ECORRUPT, "stream shorter than its header");
+  const int T = resolve_segments(segments);
+  cudaStream_t st = w->begin(stream);
+  // the dims the stream was written with must be the caller's
+  uint8_t* h = w->h_small + 16;
+  rc = SZP_GB300_OK;
+  if (cudaMemcpyAsync(h, d_bytes, kLorenzoHead, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    rc = fail(SZP_GB300_ECUDA, "reading the stream header failed");
+  } else {
+    uint32_t d[3];
+    for (int i = 0; i < 3; i++)
+      d[i] = (uint32_t)h[4 * i] | ((uint32_t)h[4 * i + 1] << 8) | ((uint32_t)h[4 * i + 2] << 16) |
+             ((uint32_t)h[4 * i + 3] << 24);
+    if (d[0] != nx || d[1] != ny || d[2] != nz)
+      rc = fail(SZP_GB300_EINVAL, "the stream holds a %ux%ux%u field", d[0], d[1], d[2]);
+  }
+  if (rc == SZP_GB300_OK) {
+    DecompressJob j{d_bytes + kLorenzoHead, byteLength - kLorenzoHead, nullptr, n, 32, T, 1, nullptr};
+    j.d_codes = reinterpret_cast<int32_t*>(d_out);
+    rc = decompress_launch(*w, j, st);
+  }
+  if (rc == SZP_GB300_OK) {
+    LorenzoArgs a;
+    memset(&a, 0, sizeof a);
+    a.q = reinterpret_cast<int32_t*>(d_out);
+    a.nx = (uint32_t)nx;
+    a.ny = (uint32_t)ny;
+    a.nz = (uint32_t)nz;
+    a.eb_dev = &w->plan.as<DecPlan>()->eb;  // the decoded stream's bound
+    a.err = &w->dm()->err;
+    w->mark(kSlotLorenzoInv, 0, st);
+    cudaError_t e = launch_lorenzo_inverse(a, (uint32_t)w->sm_count, st);
+    w->mark(kSlotLorenzoInv, 1, st);
+    if (e != cudaSuccess) rc = fail(SZP_GB300_ECUDA, "Lorenzo inverse passes: %s", cudaGetErrorString(e));
+    count_launches(2);
+  }
+  if (rc == SZP_GB300_OK) rc = finish_sync(*w, st, nullptr);
   w->end(st);
   return rc;
 }

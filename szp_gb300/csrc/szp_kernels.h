@@ -201,6 +201,19 @@ cudaError_t launch_locate_batch(const DecArgs& a, cudaStream_t st);
 cudaError_t launch_decode_batch(const DecArgs& a, uint32_t L, int rounds, cudaStream_t st);
 cudaError_t prepare_decompress_batch();
 
+// the multidimensional Lorenzo variant (lorenzo.cu)
+struct LorenzoArgs {
+  const float* x;       // field, x fastest (compression)
+  int32_t* r;           // its codes r (compression)
+  int32_t* q;           // decoded codes, summed and dequantized in place (decompression)
+  uint8_t* head;        // the stream's 12-byte dims header (compression)
+  uint32_t nx, ny, nz;
+  float eb;             // bound, when eb_dev is null
+  const float* eb_dev;  // device bound: the range pass's, or the decoded stream's
+  uint32_t* err;
+};
+cudaError_t launch_lorenzo_codes(const LorenzoArgs& a, uint32_t sm_count, cudaStream_t st);
+cudaError_t launch_lorenzo_inverse(const LorenzoArgs& a, uint32_t sm_count, cudaStream_t st);
 // host helpers (api.cu)
 const BitcountTable& host_bitcount_table();
 int host_resolve_segments(int requested);
