@@ -7,7 +7,8 @@
 // along x makes the packed values the 3-D Lorenzo residual.  The stream starts
 // with [nx][ny][nz] as u32 little-endian.  This file holds the passes around
 // the fastmode1 pipelines (which pack and unpack r as codes):
-//   lorenzo_codes_kernel  x -> r, and the 12-byte dims header
+//   lorenzo_codes_kernel  x -> r, and the 12-byte dims header (lorenzo_codes4_kernel:
+//                         the same by float4s)
 //   lorenzo_ysum_kernel   r -> r summed along y, in place
 //   lorenzo_zsum_kernel   ... summed along z and dequantized, in place
 // The reference predicts along the flattened array only; this variant has no
@@ -56,6 +57,50 @@ __global__ void __launch_bounds__(256) lorenzo_codes_kernel(const LorenzoArgs a)
       j -= ny;
       k++;
     }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 12) {
+    const uint32_t d[3] = {a.nx, a.ny, a.nz};
+    a.head[threadIdx.x] = (uint8_t)(d[threadIdx.x >> 2] >> (8 * (threadIdx.x & 3)));
+  }
+  if (__any_sync(0xffffffffu, flags != 0) && (threadIdx.x & 31) == 0) atomicOr(a.err, kErrQuantRange);
+}
+
+// The same codes, 4 elements per thread: rows of nx = 4 * nx4 values, x and r
+// 16-byte aligned, n / 4 below 2^32.  A flat grid-stride over the float4s of
+// the field; each takes its row's (j, k) by two 32-bit divisions and loads its
+// three neighbours as float4s (from L2: the grid covers several planes at once).
+__global__ void __launch_bounds__(256) lorenzo_codes4_kernel(const LorenzoArgs a) {
+  const float eb = a.eb_dev ? *a.eb_dev : a.eb;
+  const float inv = __fdiv_rn(1.0f, eb);
+  uint32_t flags = 0;
+  const uint32_t nx4 = a.nx >> 2, ny = a.ny;
+  const uint32_t plane4 = nx4 * ny;
+  const uint32_t total = plane4 * a.nz;
+  const float4* __restrict__ x4 = reinterpret_cast<const float4*>(a.x);
+  int4* __restrict__ r4 = reinterpret_cast<int4*>(a.r);
+  auto q4 = [&](float4 v) {
+    return make_int4(quantize(v.x, inv, flags), quantize(v.y, inv, flags), quantize(v.z, inv, flags),
+                     quantize(v.w, inv, flags));
+  };
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i64 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i64 < total; i64 += stride) {
+    const uint32_t it = (uint32_t)i64;
+    const uint32_t row = it / nx4, j = row % ny, k = row / ny;
+    const int4 c = q4(__ldg(x4 + it));
+    uint32_t v0 = (uint32_t)c.x, v1 = (uint32_t)c.y, v2 = (uint32_t)c.z, v3 = (uint32_t)c.w;
+    if (j) {
+      const int4 p = q4(__ldg(x4 + it - nx4));
+      v0 -= (uint32_t)p.x; v1 -= (uint32_t)p.y; v2 -= (uint32_t)p.z; v3 -= (uint32_t)p.w;
+    }
+    if (k) {
+      const int4 p = q4(__ldg(x4 + it - plane4));
+      v0 -= (uint32_t)p.x; v1 -= (uint32_t)p.y; v2 -= (uint32_t)p.z; v3 -= (uint32_t)p.w;
+    }
+    if (j && k) {
+      const int4 p = q4(__ldg(x4 + it - plane4 - nx4));
+      v0 += (uint32_t)p.x; v1 += (uint32_t)p.y; v2 += (uint32_t)p.z; v3 += (uint32_t)p.w;
+    }
+    r4[it] = make_int4((int32_t)v0, (int32_t)v1, (int32_t)v2, (int32_t)v3);
   }
   if (blockIdx.x == 0 && threadIdx.x < 12) {
     const uint32_t d[3] = {a.nx, a.ny, a.nz};
@@ -121,7 +166,12 @@ static uint32_t lorenzo_grid(uint64_t items, uint32_t per_cta, uint32_t cap) {
 }
 
 cudaError_t launch_lorenzo_codes(const LorenzoArgs& a, uint32_t sm_count, cudaStream_t st) {
-  lorenzo_codes_kernel<<<lorenzo_grid((uint64_t)a.ny * a.nz, 1, 8 * sm_count), 256, 0, st>>>(a);
+  const uint64_t n4 = (uint64_t)a.nx * a.ny * a.nz / 4;
+  if ((a.nx & 3) == 0 && n4 > 0 && n4 < (1ull << 32) && ((uintptr_t)a.x & 15) == 0 && ((uintptr_t)a.r & 15) == 0) {
+    lorenzo_codes4_kernel<<<lorenzo_grid(n4, 256, 8 * sm_count), 256, 0, st>>>(a);
+  } else {
+    lorenzo_codes_kernel<<<lorenzo_grid((uint64_t)a.ny * a.nz, 1, 8 * sm_count), 256, 0, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
