@@ -271,7 +271,7 @@ __device__ __forceinline__ uint64_t loc_word(uint64_t cnt, uint32_t h0, uint32_t
   return (cnt << 25) | (hr << 8) | xr;
 }
 
-bool locate_packs(uint32_t super_chunk, uint32_t maxsz) {
+static bool locate_packs(uint32_t super_chunk, uint32_t maxsz) {
   return maxsz <= 254 && (uint64_t)super_chunk + maxsz < kRelEnd;
 }
 
